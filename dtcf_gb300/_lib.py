@@ -1,0 +1,61 @@
+"""ctypes binding of libgbx.so (the C ABI declared in include/gbx.h)."""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgbx.so")
+
+_i = ctypes.c_int
+_d = ctypes.c_double
+_p = ctypes.c_void_p
+_ip = ctypes.POINTER(ctypes.c_int)
+
+# name -> (restype, argtypes); every symbol declared in include/gbx.h
+SIGNATURES = {
+    "gbx_last_error": (ctypes.c_char_p, []),
+    "gbx_version": (ctypes.c_char_p, []),
+    "gbx_transpose": (_i, [_p, _p, _p, _i, _p, _p]),
+    "gbx_transpose_blocks": (_i, [_p, _p, _i, _p, _i, _p, _p]),
+    "gbx_dltc_transpose": (_i, [_p, _p, _p, _p, _i, _p, _p]),
+    "gbx_local_contraction": (_i, [_i, _i, _i, _p, _p, _p, _i, _i, _d, _p]),
+    "gbx_dltc_compute": (_i, [_p, _p, _p, _i, _i, _i, _p]),
+    "gbx_create_big_matrix": (_i, [_i, _p, _p, _i, _p, _p, _i, _i, _i, _p, _ip, _ip, _p]),
+    "gbx_revert_big_matrix": (_i, [_i, _p, _p, _i, _p, _i, _i, _i, _p, _p, _p]),
+    "gbx_plan_create": (_i, [_p, _p, _p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, _i, _i, _i,
+                             ctypes.POINTER(_p)]),
+    "gbx_execute": (_i, [_p, _p, _p, _p, _d, _p]),
+    "gbx_plan_flops": (_d, [_p]),
+    "gbx_plan_destroy": (_i, [_p]),
+    "gbx_grouped_gemm_f64": (_i, [_p, _i, _p]),
+}
+
+_lib = None
+
+
+class GbxError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("gbx error %d: %s" % (code, msg))
+        self.code = code
+
+
+def lib():
+    """Load libgbx.so; raises if it is missing (no fallback path exists)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libgbx.so is not built: run `python -m dtcf_gb300.build` (path %s)" % LIB_PATH)
+        l = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(l, name, None)
+            if f is None:
+                continue
+            f.restype = res
+            f.argtypes = args
+        _lib = l
+    return _lib
+
+
+def check(rc):
+    if rc != 0:
+        raise GbxError(rc, lib().gbx_last_error().decode())
+    return rc

@@ -1,0 +1,123 @@
+// Shared definitions of the gbx library: error state, CUDA checks, the
+// tile-move descriptor used by every permute / pack / unpack, and the GEMM
+// problem descriptors.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/gbx.h"
+
+namespace gbx {
+
+void set_error(const char* fmt, ...);
+int fail(int code, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+
+#define GBX_CUDA(call)                                                         \
+  do {                                                                         \
+    cudaError_t _e = (call);                                                   \
+    if (_e != cudaSuccess) return ::gbx::cuda_fail(_e, #call, __FILE__, __LINE__); \
+  } while (0)
+
+#define GBX_TRY(call)            \
+  do {                           \
+    int _rc = (call);            \
+    if (_rc != GBX_OK) return _rc; \
+  } while (0)
+
+constexpr int kMaxDims = 8;
+
+// Unsigned division by a run-time invariant divisor d (1 <= d < 2^31) as a
+// multiply-high and shift (Granlund & Montgomery, "Division by invariant
+// integers using multiplication", 1994): q = (mulhi(n, m) + n) >> s with
+// s = ceil(log2 d) and m = floor(2^32 (2^s - d) / d) + 1, exact for n < 2^31.
+struct FastDiv {
+  uint32_t d, m, s;
+  static FastDiv make(uint32_t d_) {
+    FastDiv f;
+    f.d = d_;
+    uint32_t s = 0;
+    while ((1ull << s) < d_) ++s;
+    f.s = s;
+    f.m = (uint32_t)(((1ull << 32) * ((1ull << s) - d_)) / d_ + 1);
+    return f;
+  }
+#ifdef __CUDACC__
+  __device__ __forceinline__ uint32_t div(uint32_t n) const {
+    return (uint32_t)(((uint64_t)__umulhi(n, m) + n) >> s);
+  }
+#endif
+};
+
+// One strided tile move: for every index tuple idx over ext[0..rank-1],
+//   dst[dst + sum idx_d * dstr_d]  (op)=  scale * src[src + sum idx_d * sstr_d]
+// op 0 stores (a plain copy when scale == 1, bit-exact), op 1 accumulates with
+// a separately rounded multiply and add, dst + (scale * x).  The host orders
+// the dimensions so that the last one has the smallest destination stride.
+struct MoveDesc {
+  int64_t src, dst;
+  int64_t sstr[kMaxDims];
+  int64_t dstr[kMaxDims];
+  FastDiv div[kMaxDims];
+  uint32_t ext[kMaxDims];
+  uint32_t n;  // elements (product of ext), < 2^31
+  int32_t rank;
+  int32_t op;
+  int32_t pad;
+  double scale;
+};
+
+// Host-side builder: fills a MoveDesc from extents and strides, merging
+// dimensions that are contiguous in both source and destination and ordering
+// the rest by destination stride.
+MoveDesc make_move(int rank, const int64_t* ext, const int64_t* sstr, const int64_t* dstr, int64_t src,
+                   int64_t dst, int op, double scale);
+
+// A set of moves uploaded to the device with its launch schedule.
+struct MoveSet {
+  std::vector<MoveDesc> host;
+  MoveDesc* d_desc = nullptr;
+  uint32_t* d_first = nullptr;  // first chunk of each descriptor (prefix sum)
+  uint32_t nchunks = 0;
+  int ndesc = 0;
+  int upload();   // copies host -> device (allocates)
+  void release();
+  ~MoveSet() { release(); }
+};
+
+// Runs every move of the set on (src, dst) buffers; accumulating moves use
+// scale * alpha.
+int run_moves(const MoveSet& ms, const double* src, double* dst, cudaStream_t st);
+int run_moves_scaled(const MoveSet& ms, const double* src, double* dst, double alpha, cudaStream_t st);
+
+// One FP64 GEMM problem of a grouped launch (element strides).
+struct GemmProblem {
+  const double* A;
+  const double* B;
+  double* C;
+  int64_t a_rs, a_cs, b_rs, b_cs, c_rs;
+  int m, n, k;
+  double alpha;
+  int accumulate;
+};
+
+// Grouped FP64 GEMM: C_p (+)= alpha_p * A_p * B_p^T for all problems in one
+// persistent launch.  d_problems is device memory.
+// d_ticket: a device int used as the work-queue counter (reset by the call),
+// or nullptr for a static round-robin schedule.
+int grouped_gemm_f64(const GemmProblem* d_problems, int nprob, int total_tiles, const int* d_tile_first,
+                     int* d_ticket, cudaStream_t st);
+// Tile decomposition shared by the host planner and the kernel.
+constexpr int kF64TileM = 64;
+constexpr int kF64TileN = 64;
+int f64_tiles(int m, int n);
+
+// Device scratch allocation helpers (the library's own allocations go
+// through these so that OOM surfaces as GBX_ENOMEM).
+int dev_alloc(void** p, size_t bytes);
+void dev_free(void* p);
+
+}  // namespace gbx

@@ -1,0 +1,563 @@
+// Contraction planning over block-sparse tensor layouts (see plan.h).
+#include "plan.h"
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <set>
+
+#include "split.h"
+
+namespace gbx {
+
+std::shared_ptr<BlockDim> BlockDim::uniform(int nblocks, int extent) {
+  return make(std::vector<int>(nblocks, extent), std::vector<int>(nblocks, 0));
+}
+
+std::shared_ptr<BlockDim> BlockDim::make(const std::vector<int>& ext, const std::vector<int>& irrep) {
+  auto b = std::make_shared<BlockDim>();
+  b->ext = ext;
+  b->irrep = irrep;
+  b->start.resize(ext.size());
+  int64_t s = 0;
+  for (size_t i = 0; i < ext.size(); ++i) {
+    b->start[i] = s;
+    s += ext[i];
+  }
+  b->total = s;
+  return b;
+}
+
+void TensorLayout::add_tile(const Coords& c) {
+  index[coord_key(c.data(), rank)] = (int)tiles.size();
+  tiles.push_back(c);
+  off.push_back(nelem);
+  nelem += tile_size(c.data());
+}
+
+int TensorLayout::resolve(const int* v, int* src_dim, double* factor) const {
+  *factor = 1.0;
+  for (int d = 0; d < rank; ++d) src_dim[d] = d;
+  int id = find(v);
+  if (id >= 0) return id;
+  // canonicalise: within each group sort block coords non-increasing (stable),
+  // counting transpositions
+  int order[kMaxDims];
+  for (int d = 0; d < rank; ++d) order[d] = d;
+  int swaps = 0;
+  std::vector<int> gids;
+  for (int d = 0; d < rank; ++d)
+    if (group[d] >= 0 && std::find(gids.begin(), gids.end(), group[d]) == gids.end()) gids.push_back(group[d]);
+  int canon[kMaxDims];
+  for (int d = 0; d < rank; ++d) canon[d] = v[d];
+  for (int g : gids) {
+    std::vector<int> pos;
+    for (int d = 0; d < rank; ++d)
+      if (group[d] == g) pos.push_back(d);
+    // bubble sort positions by coordinate (descending), counting swaps
+    std::vector<int> who(pos.size());  // virtual dim sitting at pos[i]
+    for (size_t i = 0; i < pos.size(); ++i) who[i] = pos[i];
+    for (size_t i = 0; i < pos.size(); ++i)
+      for (size_t j = 0; j + 1 < pos.size() - i; ++j)
+        if (v[who[j]] < v[who[j + 1]]) {
+          std::swap(who[j], who[j + 1]);
+          ++swaps;
+        }
+    for (size_t i = 0; i < pos.size(); ++i) {
+      canon[pos[i]] = v[who[i]];
+      order[pos[i]] = who[i];  // stored dim pos[i] holds virtual dim who[i]
+    }
+  }
+  id = find(canon);
+  if (id < 0) return -1;
+  for (int s = 0; s < rank; ++s) src_dim[order[s]] = s;
+  *factor = (swaps & 1) ? (double)sign : 1.0;
+  return id;
+}
+
+TensorLayout TensorLayout::full(const std::vector<std::shared_ptr<BlockDim>>& dims, const std::vector<int>& group,
+                                int sign, bool canonical_only) {
+  TensorLayout t;
+  t.rank = (int)dims.size();
+  t.dims = dims;
+  t.group = group.empty() ? std::vector<int>(t.rank, -1) : group;
+  t.sign = sign;
+  std::vector<int> c(t.rank, 0);
+  if (t.rank == 0) return t;
+  for (;;) {
+    bool ok = t.irrep_of(c.data()) == 0;
+    if (ok && canonical_only)
+      for (int i = 0; i < t.rank && ok; ++i)
+        for (int j = i + 1; j < t.rank; ++j)
+          if (t.group[i] >= 0 && t.group[i] == t.group[j] && c[i] < c[j]) {
+            ok = false;
+            break;
+          }
+    if (ok) t.add_tile(c);
+    int d = t.rank - 1;
+    for (; d >= 0; --d) {
+      if (++c[d] < (int)dims[d]->ext.size()) break;
+      c[d] = 0;
+    }
+    if (d < 0) break;
+  }
+  return t;
+}
+
+std::vector<std::string> split_labels(const char* s) {
+  std::vector<std::string> out;
+  if (!s) return out;
+  std::string str(s);
+  if (str.find(',') == std::string::npos) {  // one character per index
+    for (char ch : str)
+      if (ch != ' ') out.push_back(std::string(1, ch));
+    return out;
+  }
+  std::string cur;
+  for (char ch : str) {
+    if (ch == ',') {
+      out.push_back(cur);
+      cur.clear();
+    } else if (ch != ' ') {
+      cur += ch;
+    }
+  }
+  out.push_back(cur);
+  return out;
+}
+
+int parse_contraction(const std::vector<std::string>& la, const std::vector<std::string>& lb,
+                      const std::vector<std::string>& lc, ContractionSpec& out) {
+  auto find = [](const std::vector<std::string>& v, const std::string& x) {
+    for (size_t i = 0; i < v.size(); ++i)
+      if (v[i] == x) return (int)i;
+    return -1;
+  };
+  out = ContractionSpec();
+  std::set<std::string> seen;
+  for (auto* v : {&la, &lb, &lc})
+    for (size_t i = 0; i < v->size(); ++i)
+      for (size_t j = i + 1; j < v->size(); ++j)
+        if ((*v)[i] == (*v)[j]) return fail(GBX_EINVAL, "index %s repeated in one tensor", (*v)[i].c_str());
+  for (size_t i = 0; i < la.size(); ++i) {
+    int ib = find(lb, la[i]), ic = find(lc, la[i]);
+    if (ib >= 0 && ic >= 0) return fail(GBX_EUNSUPPORTED, "index %s in A, B and C", la[i].c_str());
+    if (ib < 0 && ic < 0) return fail(GBX_EUNSUPPORTED, "index %s of A is neither contracted nor kept", la[i].c_str());
+    if (ib >= 0) {
+      out.contrA.push_back((int)i);
+      out.contrB.push_back(ib);
+    } else {
+      out.extA.push_back((int)i);
+    }
+  }
+  for (size_t i = 0; i < lb.size(); ++i) {
+    int ia = find(la, lb[i]), ic = find(lc, lb[i]);
+    if (ia < 0 && ic < 0) return fail(GBX_EUNSUPPORTED, "index %s of B is neither contracted nor kept", lb[i].c_str());
+    if (ia < 0) out.extB.push_back((int)i);
+  }
+  out.c_from.assign(lc.size(), 0);
+  for (size_t i = 0; i < lc.size(); ++i) {
+    int ia = find(la, lc[i]), ib = find(lb, lc[i]);
+    if (ia >= 0) {
+      int k = (int)(std::find(out.extA.begin(), out.extA.end(), ia) - out.extA.begin());
+      out.c_from[i] = k;
+    } else if (ib >= 0) {
+      int k = (int)(std::find(out.extB.begin(), out.extB.end(), ib) - out.extB.begin());
+      out.c_from[i] = -(1 + k);
+    } else {
+      return fail(GBX_EINVAL, "index %s of C appears in neither A nor B", lc[i].c_str());
+    }
+  }
+  if (out.extA.size() + out.extB.size() != lc.size()) return fail(GBX_EINVAL, "C indices do not match A and B");
+  return GBX_OK;
+}
+
+// Host-side bounds check of a move set against its buffers (done once per
+// plan, so a bad descriptor can never reach the device).
+int check_moves(const MoveSet& ms, int64_t src_elems, int64_t dst_elems, const char* what) {
+  for (const MoveDesc& m : ms.host) {
+    if (m.n == 0) continue;
+    int64_t smax = m.src, dmax = m.dst;
+    for (int d = 0; d < m.rank; ++d) {
+      if (m.sstr[d] < 0 || m.dstr[d] < 0) return fail(GBX_EINVAL, "%s: negative stride", what);
+      smax += (int64_t)(m.ext[d] - 1) * m.sstr[d];
+      dmax += (int64_t)(m.ext[d] - 1) * m.dstr[d];
+    }
+    if (m.src < 0 || m.dst < 0 || smax >= src_elems || dmax >= dst_elems)
+      return fail(GBX_EINVAL, "%s: move outside its buffers (src %lld/%lld, dst %lld/%lld)", what, (long long)smax,
+                  (long long)src_elems, (long long)dmax, (long long)dst_elems);
+  }
+  return GBX_OK;
+}
+
+namespace {
+
+// Enumerates all block tuples over the given dims (odometer order = lexicographic).
+template <class F>
+void for_tuples(const std::vector<const BlockDim*>& dims, F&& f) {
+  std::vector<int> c(dims.size(), 0);
+  for (const BlockDim* d : dims)
+    if (d->ext.empty()) return;
+  for (;;) {
+    f(c);
+    int d = (int)dims.size() - 1;
+    for (; d >= 0; --d) {
+      if (++c[d] < (int)dims[d]->ext.size()) break;
+      c[d] = 0;
+    }
+    if (d < 0) break;
+  }
+}
+
+struct TupleIndex {  // ordered tuples of one irrep with element offsets
+  std::map<std::vector<int>, int64_t> off;
+  int64_t total = 0;
+};
+
+int tuple_irrep(const std::vector<const BlockDim*>& dims, const std::vector<int>& t) {
+  int h = 0;
+  for (size_t i = 0; i < t.size(); ++i) h ^= dims[i]->irrep[t[i]];
+  return h;
+}
+
+int64_t tuple_size(const std::vector<const BlockDim*>& dims, const std::vector<int>& t) {
+  int64_t n = 1;
+  for (size_t i = 0; i < t.size(); ++i) n *= dims[i]->ext[t[i]];
+  return n;
+}
+
+// strides inside a packed sub-block for a list of dims with given extents:
+// dim j of the list gets base * prod(ext of later dims)
+void sub_strides(const std::vector<int64_t>& ext, int64_t base, std::vector<int64_t>& str) {
+  str.assign(ext.size(), 0);
+  int64_t s = base;
+  for (int j = (int)ext.size() - 1; j >= 0; --j) {
+    str[j] = s;
+    s *= ext[j];
+  }
+}
+
+}  // namespace
+
+ContractionPlan::~ContractionPlan() {
+  dev_free(d_probs);
+  dev_free(d_tile_first);
+  dev_free(d_ticket);
+  if (own_workspace) {
+    dev_free(d_Abig);
+    dev_free(d_Bbig);
+    dev_free(d_Cbig);
+  }
+  destroy_split_plan(split);
+}
+
+int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorLayout& C,
+                     const std::vector<std::string>& la, const std::vector<std::string>& lb,
+                     const std::vector<std::string>& lc, Engine e, int nslices,
+                     std::unique_ptr<ContractionPlan>& out) {
+  if ((int)la.size() != A.rank || (int)lb.size() != B.rank || (int)lc.size() != C.rank)
+    return fail(GBX_EINVAL, "index strings do not match tensor ranks (%d/%d, %d/%d, %d/%d)", (int)la.size(), A.rank,
+                (int)lb.size(), B.rank, (int)lc.size(), C.rank);
+  auto p = std::make_unique<ContractionPlan>();
+  p->A = A;
+  p->B = B;
+  p->C = C;
+  GBX_TRY(parse_contraction(la, lb, lc, p->spec));
+  const ContractionSpec& s = p->spec;
+  // dimension compatibility
+  for (size_t i = 0; i < s.contrA.size(); ++i)
+    if (!A.dims[s.contrA[i]]->same_as(*B.dims[s.contrB[i]]))
+      return fail(GBX_EINVAL, "contracted index %s has different blocking in A and B", la[s.contrA[i]].c_str());
+  std::vector<const BlockDim*> dA, dB, dK;
+  for (int d : s.extA) dA.push_back(A.dims[d].get());
+  for (int d : s.extB) dB.push_back(B.dims[d].get());
+  for (int d : s.contrA) dK.push_back(A.dims[d].get());
+  for (int i = 0; i < C.rank; ++i) {
+    const BlockDim* cd = C.dims[i].get();
+    const BlockDim* src = s.c_from[i] >= 0 ? dA[s.c_from[i]] : dB[-1 - s.c_from[i]];
+    if (!cd->same_as(*src)) return fail(GBX_EINVAL, "index %s has different blocking in C", lc[i].c_str());
+  }
+  // rows / columns needed by C's stored tiles, per irrep
+  std::map<int, TupleIndex> rows, cols, ks;
+  std::vector<std::vector<int>> c_row(C.tiles.size()), c_col(C.tiles.size());
+  for (size_t t = 0; t < C.tiles.size(); ++t) {
+    const Coords& cc = C.tiles[t];
+    std::vector<int> r(s.extA.size()), c(s.extB.size());
+    for (int i = 0; i < C.rank; ++i) {
+      if (s.c_from[i] >= 0) r[s.c_from[i]] = cc[i]; else c[-1 - s.c_from[i]] = cc[i];
+    }
+    c_row[t] = r;
+    c_col[t] = c;
+    rows[tuple_irrep(dA, r)].off[r] = 0;
+    cols[tuple_irrep(dB, c)].off[c] = 0;
+  }
+  for_tuples(dK, [&](const std::vector<int>& k) { ks[tuple_irrep(dK, k)].off[k] = 0; });
+  if (dK.empty()) ks[0].off[std::vector<int>()] = 0;
+  auto assign = [](TupleIndex& ti, const std::vector<const BlockDim*>& dims) {
+    ti.total = 0;
+    for (auto& kv : ti.off) {
+      kv.second = ti.total;
+      ti.total += tuple_size(dims, kv.first);
+    }
+  };
+  for (auto& kv : rows) assign(kv.second, dA);
+  for (auto& kv : cols) assign(kv.second, dB);
+  for (auto& kv : ks) assign(kv.second, dK);
+  // irrep groups present in rows, cols and K
+  int64_t ao = 0, bo = 0, co = 0;
+  std::map<int, int> gidx;
+  for (auto& kv : rows) {
+    int h = kv.first;
+    if (!cols.count(h)) continue;
+    GroupBlock g;
+    g.h = h;
+    g.M = kv.second.total;
+    g.N = cols[h].total;
+    g.K = ks.count(h) ? ks[h].total : 0;
+    g.a_off = ao;
+    g.b_off = bo;
+    g.c_off = co;
+    ao += g.M * g.K;
+    bo += g.N * g.K;
+    co += g.M * g.N;
+    gidx[h] = (int)p->groups.size();
+    p->groups.push_back(g);
+  }
+  p->a_elems = ao;
+  p->b_elems = bo;
+  p->c_elems = co;
+
+  // pack moves: A (rows = extA tuples of irrep h, cols = K tuples of irrep h)
+  auto pack = [&](const TensorLayout& T, const std::vector<int>& ext_dims, const std::vector<int>& contr_dims,
+                  std::map<int, TupleIndex>& rowsets, bool isA, MoveSet& ms, bool& needs_zero) -> int {
+    std::vector<const BlockDim*> dR;
+    for (int d : ext_dims) dR.push_back(T.dims[d].get());
+    for (auto& kv : rowsets) {
+      int h = kv.first;
+      auto gi = gidx.find(h);
+      if (gi == gidx.end()) continue;
+      const GroupBlock& g = p->groups[gi->second];
+      if (g.K == 0) continue;
+      TupleIndex& kt = ks[h];
+      for (auto& rv : kv.second.off) {
+        for (auto& kvv : kt.off) {
+          int v[kMaxDims];
+          for (size_t i = 0; i < ext_dims.size(); ++i) v[ext_dims[i]] = rv.first[i];
+          for (size_t i = 0; i < contr_dims.size(); ++i) v[contr_dims[i]] = kvv.first[i];
+          int src_dim[kMaxDims];
+          double factor;
+          int id = T.resolve(v, src_dim, &factor);
+          if (id < 0) {
+            needs_zero = true;
+            continue;
+          }
+          // stored tile strides
+          const Coords& sc = T.tiles[id];
+          int64_t sstr_st[kMaxDims];
+          sstr_st[T.rank - 1] = 1;
+          for (int d = T.rank - 2; d >= 0; --d) sstr_st[d] = sstr_st[d + 1] * T.dims[d + 1]->ext[sc[d + 1]];
+          // destination strides inside the packed block
+          std::vector<int64_t> eR, eK, sR, sK;
+          for (size_t i = 0; i < ext_dims.size(); ++i) eR.push_back(T.dims[ext_dims[i]]->ext[v[ext_dims[i]]]);
+          for (size_t i = 0; i < contr_dims.size(); ++i) eK.push_back(T.dims[contr_dims[i]]->ext[v[contr_dims[i]]]);
+          sub_strides(eR, g.K, sR);
+          sub_strides(eK, 1, sK);
+          int64_t ext[kMaxDims], sstr[kMaxDims], dstr[kMaxDims];
+          for (int d = 0; d < T.rank; ++d) {
+            ext[d] = T.dims[d]->ext[v[d]];
+            sstr[d] = sstr_st[src_dim[d]];
+          }
+          for (size_t i = 0; i < ext_dims.size(); ++i) dstr[ext_dims[i]] = sR[i];
+          for (size_t i = 0; i < contr_dims.size(); ++i) dstr[contr_dims[i]] = sK[i];
+          int64_t dst = (isA ? g.a_off : g.b_off) + rv.second * g.K + kvv.second;
+          ms.host.push_back(make_move(T.rank, ext, sstr, dstr, T.off[id], dst, 0, factor));
+        }
+      }
+    }
+    return GBX_OK;
+  };
+  std::vector<int> contrB_in_A_order = s.contrB;
+  GBX_TRY(pack(A, s.extA, s.contrA, rows, true, p->packA, p->a_needs_zero));
+  GBX_TRY(pack(B, s.extB, contrB_in_A_order, cols, false, p->packB, p->b_needs_zero));
+
+  // unpack C tiles
+  for (size_t t = 0; t < C.tiles.size(); ++t) {
+    int hr = tuple_irrep(dA, c_row[t]);
+    auto gi = gidx.find(hr);
+    if (gi == gidx.end()) continue;
+    const GroupBlock& g = p->groups[gi->second];
+    if (g.K == 0) continue;
+    const Coords& cc = C.tiles[t];
+    int64_t roff = rows[hr].off[c_row[t]], coff = cols[hr].off[c_col[t]];
+    std::vector<int64_t> eR, eC, sR, sC;
+    for (size_t i = 0; i < s.extA.size(); ++i) eR.push_back(dA[i]->ext[c_row[t][i]]);
+    for (size_t i = 0; i < s.extB.size(); ++i) eC.push_back(dB[i]->ext[c_col[t][i]]);
+    sub_strides(eR, g.N, sR);
+    sub_strides(eC, 1, sC);
+    int64_t ext[kMaxDims], sstr[kMaxDims], dstr[kMaxDims];
+    dstr[C.rank - 1] = 1;
+    for (int d = C.rank - 2; d >= 0; --d) dstr[d] = dstr[d + 1] * C.dims[d + 1]->ext[cc[d + 1]];
+    for (int d = 0; d < C.rank; ++d) {
+      ext[d] = C.dims[d]->ext[cc[d]];
+      sstr[d] = s.c_from[d] >= 0 ? sR[s.c_from[d]] : sC[-1 - s.c_from[d]];
+    }
+    p->unpackC.host.push_back(make_move(C.rank, ext, sstr, dstr, g.c_off + roff * g.N + coff, C.off[t], 1, 1.0));
+  }
+
+  // algorithmic flops over nonzero (A-block, B-block -> C-block) triples
+  double fl = 0.0, gf = 0.0;
+  for (auto& g : p->groups) gf += 2.0 * (double)g.M * (double)g.N * (double)g.K;
+  for (size_t t = 0; t < C.tiles.size(); ++t) {
+    int hr = tuple_irrep(dA, c_row[t]);
+    if (!ks.count(hr)) continue;
+    double mn = (double)tuple_size(dA, c_row[t]) * (double)tuple_size(dB, c_col[t]);
+    for (auto& kv : ks[hr].off) {
+      int v[kMaxDims], sd[kMaxDims];
+      double f;
+      for (size_t i = 0; i < s.extA.size(); ++i) v[s.extA[i]] = c_row[t][i];
+      for (size_t i = 0; i < s.contrA.size(); ++i) v[s.contrA[i]] = kv.first[i];
+      if (A.resolve(v, sd, &f) < 0) continue;
+      int w[kMaxDims];
+      for (size_t i = 0; i < s.extB.size(); ++i) w[s.extB[i]] = c_col[t][i];
+      for (size_t i = 0; i < s.contrB.size(); ++i) w[s.contrB[i]] = kv.first[i];
+      if (B.resolve(w, sd, &f) < 0) continue;
+      fl += 2.0 * mn * (double)tuple_size(dK, kv.first);
+    }
+  }
+  p->flops = fl;
+  p->gemm_flops = gf;
+  GBX_TRY(check_moves(p->packA, A.nelem, p->a_elems, "pack A"));
+  GBX_TRY(check_moves(p->packB, B.nelem, p->b_elems, "pack B"));
+  GBX_TRY(check_moves(p->unpackC, p->c_elems, C.nelem, "unpack C"));
+  GBX_TRY(p->build(e, nslices));
+  out = std::move(p);
+  return GBX_OK;
+}
+
+int ContractionPlan::build(Engine e, int nslices) {
+  engine = e;
+  slices = nslices;
+  GBX_TRY(packA.upload());
+  GBX_TRY(packB.upload());
+  GBX_TRY(unpackC.upload());
+  GBX_TRY(dev_alloc((void**)&d_Abig, sizeof(double) * a_elems));
+  GBX_TRY(dev_alloc((void**)&d_Bbig, sizeof(double) * b_elems));
+  GBX_TRY(dev_alloc((void**)&d_Cbig, sizeof(double) * c_elems));
+  if (e == Engine::F64) {
+    std::vector<GemmProblem> probs;
+    std::vector<int> first;
+    int total = 0;
+    for (auto& g : groups) {
+      if (g.M == 0 || g.N == 0 || g.K == 0) continue;
+      if (g.M >= (1ll << 31) || g.N >= (1ll << 31) || g.K >= (1ll << 31))
+        return fail(GBX_EUNSUPPORTED, "packed block too large");
+      GemmProblem q;
+      q.A = d_Abig + g.a_off;
+      q.B = d_Bbig + g.b_off;
+      q.C = d_Cbig + g.c_off;
+      q.a_rs = g.K;
+      q.a_cs = 1;
+      q.b_rs = g.K;
+      q.b_cs = 1;
+      q.c_rs = g.N;
+      q.m = (int)g.M;
+      q.n = (int)g.N;
+      q.k = (int)g.K;
+      q.alpha = 1.0;
+      q.accumulate = 0;
+      probs.push_back(q);
+      first.push_back(total);
+      total += f64_tiles(q.m, q.n);
+    }
+    nprob = (int)probs.size();
+    total_tiles = total;
+    if (nprob > 0) {
+      GBX_TRY(dev_alloc((void**)&d_probs, sizeof(GemmProblem) * nprob));
+      GBX_TRY(dev_alloc((void**)&d_tile_first, sizeof(int) * nprob));
+      GBX_TRY(dev_alloc((void**)&d_ticket, sizeof(int)));
+      GBX_CUDA(cudaMemcpy(d_probs, probs.data(), sizeof(GemmProblem) * nprob, cudaMemcpyHostToDevice));
+      GBX_CUDA(cudaMemcpy(d_tile_first, first.data(), sizeof(int) * nprob, cudaMemcpyHostToDevice));
+    }
+  } else {
+    std::vector<SplitProblem> sp;
+    for (auto& g : groups) {
+      if (g.M == 0 || g.N == 0 || g.K == 0) continue;
+      SplitProblem q;
+      q.A = d_Abig + g.a_off;
+      q.B = d_Bbig + g.b_off;
+      q.C = d_Cbig + g.c_off;
+      q.M = g.M;
+      q.N = g.N;
+      q.K = g.K;
+      sp.push_back(q);
+    }
+    GBX_TRY(create_split_plan(sp, nslices, &split));
+  }
+  return GBX_OK;
+}
+
+int ContractionPlan::execute(const double* dA, const double* dB, double* dC, double alpha, cudaStream_t st) {
+  if (nprob == 0 && !split) return GBX_OK;
+  bool skipA = a_static && a_ready;
+  if (!skipA) {
+    if (a_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Abig, 0, sizeof(double) * a_elems, st));
+    GBX_TRY(run_moves(packA, dA, d_Abig, st));
+  }
+  if (b_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Bbig, 0, sizeof(double) * b_elems, st));
+  GBX_TRY(run_moves(packB, dB, d_Bbig, st));
+  if (engine == Engine::F64) {
+    GBX_TRY(grouped_gemm_f64(d_probs, nprob, total_tiles, d_tile_first, d_ticket, st));
+  } else {
+    GBX_TRY(run_split_plan(split, !skipA, st));
+  }
+  if (a_static) a_ready = true;
+  return run_moves_scaled(unpackC, d_Cbig, dC, alpha, st);
+}
+
+int SumPlan::execute(const double* dA, double* dC, double alpha, cudaStream_t st) {
+  return run_moves_scaled(moves, dA, dC, alpha, st);
+}
+
+int plan_sum(const TensorLayout& A, const TensorLayout& C, const std::vector<std::string>& la,
+             const std::vector<std::string>& lc, double coef, std::unique_ptr<SumPlan>& out) {
+  if ((int)la.size() != A.rank || (int)lc.size() != C.rank || A.rank != C.rank)
+    return fail(GBX_EINVAL, "sum: index strings do not match ranks");
+  std::vector<int> a_of_c(C.rank);
+  for (int i = 0; i < C.rank; ++i) {
+    a_of_c[i] = -1;
+    for (int j = 0; j < A.rank; ++j)
+      if (la[j] == lc[i]) a_of_c[i] = j;
+    if (a_of_c[i] < 0) return fail(GBX_EINVAL, "sum: index %s of C missing in A", lc[i].c_str());
+    if (!C.dims[i]->same_as(*A.dims[a_of_c[i]])) return fail(GBX_EINVAL, "sum: blocking differs for %s", lc[i].c_str());
+  }
+  auto p = std::make_unique<SumPlan>();
+  p->A = A;
+  p->C = C;
+  for (size_t t = 0; t < C.tiles.size(); ++t) {
+    const Coords& cc = C.tiles[t];
+    int v[kMaxDims];
+    for (int i = 0; i < C.rank; ++i) v[a_of_c[i]] = cc[i];  // A's virtual coords
+    int src_dim[kMaxDims];
+    double f;
+    int id = A.resolve(v, src_dim, &f);
+    if (id < 0) continue;  // zero tile
+    const Coords& sc = A.tiles[id];
+    int64_t sst[kMaxDims];
+    sst[A.rank - 1] = 1;
+    for (int d = A.rank - 2; d >= 0; --d) sst[d] = sst[d + 1] * A.dims[d + 1]->ext[sc[d + 1]];
+    int64_t ext[kMaxDims], sstr[kMaxDims], dstr[kMaxDims];
+    dstr[C.rank - 1] = 1;
+    for (int d = C.rank - 2; d >= 0; --d) dstr[d] = dstr[d + 1] * C.dims[d + 1]->ext[cc[d + 1]];
+    for (int i = 0; i < C.rank; ++i) {
+      ext[i] = C.dims[i]->ext[cc[i]];
+      sstr[i] = sst[src_dim[a_of_c[i]]];
+    }
+    p->moves.host.push_back(make_move(C.rank, ext, sstr, dstr, A.off[id], C.off[t], 1, coef * f));
+  }
+  GBX_TRY(check_moves(p->moves, A.nelem, C.nelem, "sum"));
+  GBX_TRY(p->moves.upload());
+  out = std::move(p);
+  return GBX_OK;
+}
+
+}  // namespace gbx

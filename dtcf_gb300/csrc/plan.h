@@ -1,0 +1,153 @@
+// Block-sparse tensor layouts and contraction plans.
+//
+// A tensor is a set of stored tiles; each tile is a dense row-major block over
+// one block of every dimension.  A dimension is a list of blocks, each with an
+// extent and an irrep (spatial-symmetry label, 0 when unused).  Dimensions may
+// form permutational symmetry groups; a layout that stores only canonical
+// tiles (block coordinates non-increasing within each group, as RRR stores
+// them, tensor.cc:617-640) recovers the others by permuting the stored tile
+// and multiplying by sign^(number of transpositions).
+//
+// A contraction C[c] += alpha * sum A[a] B[b] is planned once:
+//   - A is packed, per irrep h of its external block tuple, into a row-major
+//     matrix A_h (rows: external tuples of A that C needs, columns: contracted
+//     tuples), B into B_h likewise, both with the contracted tuples in the
+//     same order -- the row/column placement of create_big_matrix
+//     (transpose_helper.cc:20-171) with lexicographic block order;
+//   - C_h = A_h * B_h^T runs as one grouped GEMM over all h;
+//   - C's stored tiles are unpacked from C_h and accumulated with alpha.
+// Packs and unpacks are tile moves (permute + place) run as one launch each.
+#pragma once
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "common.h"
+
+namespace gbx {
+
+struct BlockDim {
+  std::vector<int> ext;
+  std::vector<int> irrep;
+  std::vector<int64_t> start;  // first element of each block along the dimension
+  int64_t total = 0;
+  static std::shared_ptr<BlockDim> uniform(int nblocks, int extent);
+  static std::shared_ptr<BlockDim> make(const std::vector<int>& ext, const std::vector<int>& irrep);
+  bool same_as(const BlockDim& o) const { return ext == o.ext && irrep == o.irrep; }
+};
+
+using Coords = std::vector<int>;
+
+inline uint64_t coord_key(const int* c, int rank) {
+  uint64_t k = 0;
+  for (int d = 0; d < rank; ++d) k = k * 65536u + (uint64_t)c[d];
+  return k;
+}
+
+struct TensorLayout {
+  int rank = 0;
+  std::vector<std::shared_ptr<BlockDim>> dims;
+  std::vector<int> group;  // symmetry group per dim, -1 = none
+  int sign = 1;            // +1 symmetric, -1 antisymmetric groups
+  std::vector<Coords> tiles;
+  std::vector<int64_t> off;
+  std::unordered_map<uint64_t, int> index;
+  int64_t nelem = 0;
+
+  // Appends a stored tile (offsets assigned in order).
+  void add_tile(const Coords& c);
+  int find(const int* c) const {
+    auto it = index.find(coord_key(c, rank));
+    return it == index.end() ? -1 : it->second;
+  }
+  int64_t tile_size(const int* c) const {
+    int64_t n = 1;
+    for (int d = 0; d < rank; ++d) n *= dims[d]->ext[c[d]];
+    return n;
+  }
+  int irrep_of(const int* c) const {
+    int h = 0;
+    for (int d = 0; d < rank; ++d) h ^= dims[d]->irrep[c[d]];
+    return h;
+  }
+  // Resolves virtual tile coords v to a stored tile: returns its id (or -1
+  // when the tile is not stored), sets src_dim[d] = the stored tile's
+  // dimension that becomes virtual dimension d, and the sign factor.
+  int resolve(const int* v, int* src_dim, double* factor) const;
+  // All tiles with irrep XOR zero, optionally canonical only.
+  static TensorLayout full(const std::vector<std::shared_ptr<BlockDim>>& dims, const std::vector<int>& group,
+                           int sign, bool canonical_only);
+};
+
+// Parsed index labels of a contraction.
+struct ContractionSpec {
+  std::vector<int> extA;          // dims of A kept in C (A order)
+  std::vector<int> extB;          // dims of B kept in C (B order)
+  std::vector<int> contrA;        // contracted dims of A (A order)
+  std::vector<int> contrB;        // matching dims of B
+  std::vector<int> c_from;        // per C dim: index into extA (>=0) or -(1 + index into extB)
+};
+
+int parse_contraction(const std::vector<std::string>& la, const std::vector<std::string>& lb,
+                      const std::vector<std::string>& lc, ContractionSpec& out);
+std::vector<std::string> split_labels(const char* s);
+
+struct GroupBlock {   // one irrep block of the packed operands
+  int h;
+  int64_t M, N, K;
+  int64_t a_off, b_off, c_off;  // element offsets in the packed buffers
+};
+
+enum class Engine { F64 = 0, Split = 1 };
+
+struct SplitPlan;  // the split-precision GEMM state (gemm_split.cu)
+
+struct ContractionPlan {
+  TensorLayout A, B, C;
+  ContractionSpec spec;
+  std::vector<GroupBlock> groups;
+  int64_t a_elems = 0, b_elems = 0, c_elems = 0;
+  bool a_needs_zero = false, b_needs_zero = false;
+  MoveSet packA, packB, unpackC;
+  // F64 engine
+  GemmProblem* d_probs = nullptr;
+  int* d_tile_first = nullptr;
+  int* d_ticket = nullptr;
+  int nprob = 0, total_tiles = 0;
+  // workspace
+  double *d_Abig = nullptr, *d_Bbig = nullptr, *d_Cbig = nullptr;
+  bool own_workspace = true;
+  Engine engine = Engine::F64;
+  int slices = 0;
+  SplitPlan* split = nullptr;
+  double flops = 0.0;        // algorithmic: 2 * sum over nonzero triples m*n*k
+  double gemm_flops = 0.0;   // what the packed GEMMs execute
+  bool a_static = false;     // A's values do not change between executes (split once)
+  bool a_ready = false;
+
+  ~ContractionPlan();
+  int build(Engine e, int nslices);
+  // C += alpha * A * B.  When skip_pack_a is set the packed / split A from the
+  // previous execute is reused (the operand is constant, e.g. integrals).
+  int execute(const double* dA, const double* dB, double* dC, double alpha, cudaStream_t st);
+};
+
+int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorLayout& C,
+                     const std::vector<std::string>& la, const std::vector<std::string>& lb,
+                     const std::vector<std::string>& lc, Engine e, int nslices,
+                     std::unique_ptr<ContractionPlan>& out);
+
+// Tile moves accumulating alpha * permuted A into C: C[c] += alpha * A[a],
+// the DLTC Summation (DLTC/task.cc:51-81) over block-sparse layouts.
+struct SumPlan {
+  TensorLayout A, C;
+  MoveSet moves;
+  int execute(const double* dA, double* dC, double alpha, cudaStream_t st);
+};
+int check_moves(const MoveSet& ms, int64_t src_elems, int64_t dst_elems, const char* what);
+int plan_sum(const TensorLayout& A, const TensorLayout& C, const std::vector<std::string>& la,
+             const std::vector<std::string>& lc, double coef, std::unique_ptr<SumPlan>& out);
+
+}  // namespace gbx

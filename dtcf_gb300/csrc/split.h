@@ -1,0 +1,27 @@
+// Split-precision FP64 GEMM: FP64 operands split into exact integer slices
+// held in bf16, products on the tcgen05 tensor cores with exact FP32
+// accumulation chunks, recombined in FP64 (gemm_split.cu).
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include "common.h"
+
+namespace gbx {
+
+// C[M x N] = A[M x K] * B[N x K]^T, all row-major FP64 (ld = K for A and B,
+// N for C).
+struct SplitProblem {
+  const double* A;
+  const double* B;
+  double* C;
+  int64_t M, N, K;
+};
+
+struct SplitPlan;
+int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitPlan** out);
+// split_a: re-split A (false when A is unchanged since the last run).
+int run_split_plan(SplitPlan* sp, bool split_a, cudaStream_t st);
+void destroy_split_plan(SplitPlan* sp);
+
+}  // namespace gbx

@@ -1,0 +1,181 @@
+"""GPU parity of the leaf entry points against the reference fixtures and the
+oracle: permutes and packs bit-exact, FP64 GEMMs within 1e-12 relative."""
+import itertools
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+import oracle.rrr  # noqa: F401
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gbx():
+    import dtcf_gb300
+    dtcf_gb300.lib()
+    return dtcf_gb300
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64).reshape(-1)).cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def test_transpose_bit_exact_vs_reference(gbx, golden):
+    for n in range(int(golden["tr_count"])):
+        w, p = golden[f"tr{n}_widths"], golden[f"tr{n}_perm"]
+        x = dev(golden[f"tr{n}_in"])
+        y = torch.full_like(x, np.nan)
+        gbx.transpose(x, y, p, w)
+        assert np.array_equal(host(y), golden[f"tr{n}_out"]), (w, p)
+
+
+def test_dltc_transpose_bit_exact_vs_reference(gbx, golden):
+    for n in range(int(golden["dl_count"])):
+        name = bytes(golden[f"dl{n}_name"]).decode()
+        dims = golden[f"dl{n}_dims"]
+        x = dev(golden[f"dl{n}_in"])
+        y = torch.full_like(x, np.nan)
+        letters = "ijkl"[: len(dims)]
+        gbx.dltc_transpose(x, list(range(len(dims))), y, [letters.index(c) for c in name], dims)
+        assert np.array_equal(host(y), golden[f"dl{n}_out"]), name
+
+
+def test_dltc_identity_copies(gbx):
+    """DLTC/transp.cc:16,24 leaves y unwritten for identity; the C ABI copies."""
+    x = dev(np.arange(24.0))
+    y = torch.zeros_like(x)
+    gbx.dltc_transpose(x, [0, 1, 2, 3], y, [0, 1, 2, 3], [2, 3, 2, 2])
+    assert np.array_equal(host(y), np.arange(24.0))
+
+
+def test_big_matrix_bit_exact_vs_reference(gbx, golden):
+    for b in range(int(golden["bm_count"])):
+        pre = f"bm{b}_"
+        vg, pm = golden[pre + "vgrid"], golden[pre + "p_map"]
+        rpb, cpb, nrd = int(golden[pre + "rpb"]), int(golden[pre + "cpb"]), int(golden[pre + "nrd"])
+        tiles = dev(golden[pre + "tiles"])
+        big = torch.full_like(tiles, np.nan)
+        gbx.create_big_matrix(vg, pm, tiles, golden[pre + "perm_addr"], rpb, cpb, nrd, big)
+        assert np.array_equal(host(big), golden[pre + "big"])
+        back = torch.full_like(tiles, np.nan)
+        gbx.revert_big_matrix(vg, pm, golden[pre + "perm_addr"], rpb, cpb, nrd, dev(golden[pre + "big2"]), back)
+        assert np.array_equal(host(back).reshape(golden[pre + "back"].shape), golden[pre + "back"])
+
+
+def test_big_matrix_rejects_ragged(gbx):
+    tiles = dev(np.zeros(3 * 4))
+    big = torch.zeros_like(tiles)
+    with pytest.raises(Exception):
+        gbx.create_big_matrix([2, 2], [0, 1], tiles, [[0, 0], [0, 1], [1, 0]], 2, 2, 1, big)
+
+
+@pytest.mark.parametrize("na,nb,nk,at,bt", [(8, 8, 8, 0, 1), (3, 5, 7, 0, 1), (64, 48, 200, 0, 1), (7, 5, 9, 0, 0),
+                                            (33, 65, 17, 1, 0), (130, 70, 64, 1, 1), (1, 1, 1, 0, 1), (5, 6, 0, 0, 1)])
+def test_local_contraction_vs_oracle(gbx, na, nb, nk, at, bt):
+    rng = np.random.default_rng(na * 1000 + nb * 10 + nk)
+    A = rng.standard_normal(na * nk)
+    B = rng.standard_normal(nb * nk)
+    C = rng.standard_normal(na * nb)
+    want = C.copy()
+    oracle.local_contraction(na, nb, nk, A, B, want, at, bt, -0.75)
+    dC = dev(C)
+    gbx.local_contraction(na, nb, nk, dev(A), dev(B), dC, at, bt, -0.75)
+    got = host(dC)
+    scale = np.abs(A).max(initial=1) * np.abs(B).max(initial=1) * max(nk, 1)
+    assert np.max(np.abs(got - want)) <= 1e-13 * scale
+
+
+def test_local_contraction_vs_reference_fixtures(gbx, golden):
+    for c in range(int(golden["lc_count"])):
+        pre = f"lc{c}_"
+        na, nb, nk, at, bt = [int(v) for v in golden[pre + "shape"]]
+        dC = dev(golden[pre + "C_in"])
+        gbx.local_contraction(na, nb, nk, dev(golden[pre + "A"]), dev(golden[pre + "B"]), dC, at, bt,
+                              float(golden[pre + "alpha"]))
+        np.testing.assert_allclose(host(dC), golden[pre + "C_out"], rtol=1e-12, atol=1e-12)
+
+
+def test_grouped_gemm_triples(gbx):
+    from dtcf_gb300.leaves import Triple
+    rng = np.random.default_rng(5)
+    keep, trip, want = [], [], []
+    for _ in range(37):
+        m, n, k = [int(x) for x in rng.integers(1, 90, size=3)]
+        A, B, C = rng.standard_normal((m, k)), rng.standard_normal((n, k)), rng.standard_normal((m, n))
+        dA, dB, dC = dev(A), dev(B), dev(C)
+        keep += [dA, dB, dC]
+        trip.append(Triple(dA.data_ptr(), dB.data_ptr(), dC.data_ptr(), k, 1, k, 1, n, m, n, k, 1.5, 1))
+        want.append((dC, C + 1.5 * A @ B.T))
+    gbx.grouped_gemm_f64(trip)
+    for dC, w in want:
+        np.testing.assert_allclose(host(dC).reshape(w.shape), w, rtol=1e-12, atol=1e-12)
+
+
+def test_transpose_blocks_symmetric_unflip(gbx):
+    """Per-block permutes of transpose_and_dgemm: get_symm_permutation composed
+    with the p_map (contraction.cc:1824-1857), bit-exact."""
+    rng = np.random.default_rng(9)
+    addrs = [[1, 3, 0, 2], [3, 1, 2, 0], [2, 2, 1, 1], [0, 1, 1, 0]]
+    sg = [0, 0, 1, 1]
+    p_map = [2, 3, 0, 1]
+    w = [4, 4, 3, 3]
+    blocks = rng.standard_normal((len(addrs), int(np.prod(w))))
+    perms = [oracle.compose_p_maps(oracle.symm_permutation(a, sg), p_map) for a in addrs]
+    out = torch.full((blocks.size,), np.nan, dtype=torch.float64, device="cuda")
+    gbx.transpose_blocks(dev(blocks), out, perms, w)
+    got = host(out).reshape(blocks.shape)
+    for i in range(len(addrs)):
+        assert np.array_equal(got[i], oracle.transpose(blocks[i].reshape(w), perms[i]).reshape(-1))
+
+
+def _rrr_case(sym_a, sym_b, sym_c, sizes, vgrids, seed):
+    from dtcf_gb300.rrr import Tensor
+    rng = np.random.default_rng(seed)
+    T = [Tensor(s, z, v) for s, z, v in zip((sym_a, sym_b, sym_c), sizes, vgrids)]
+    for t in T:
+        t.tiles.copy_(torch.from_numpy(rng.uniform(-1, 1, t.tiles.numel())).cuda())
+    return T
+
+
+def _as_oracle(t):
+    return dict(tiles=host(t.tiles).reshape(t.num_tiles, -1), addrs=t.addrs, sym=t.sym, block_range=t.block_range,
+                vgrid=t.vgrid)
+
+
+@pytest.mark.parametrize("sign", [1, -1])
+def test_rrr_plan_ladder_small(gbx, sign):
+    """C[a,b,i,j] += 0.5 sum_ef V[a,b,e,f] T[e,f,i,j] with unique blocks (aabb)."""
+    from dtcf_gb300.rrr import Contraction
+    o, v, blk = 8, 12, 4
+    V, T, C = _rrr_case("aabb", "aabb", "aabb", [(v, v, v, v), (v, v, o, o), (v, v, o, o)],
+                        [(v // blk,) * 4, (v // blk, v // blk, o // blk, o // blk), (v // blk, v // blk, o // blk, o // blk)],
+                        11)
+    want = oracle.rrr.contract(_as_oracle(V), _as_oracle(T), _as_oracle(C), "a,b,e,f", "e,f,i,j", "a,b,i,j", 0.5,
+                               sign)
+    Contraction(V, T, C, sign=sign).contract("a,b,e,f", "e,f,i,j", "a,b,i,j", 0.5)
+    got = host(C.tiles).reshape(want.shape)
+    assert np.max(np.abs(got - want)) <= 1e-12 * max(1.0, np.abs(want).max())
+
+
+def test_rrr_plan_cntr4a_shape(gbx):
+    """examples/cntr4a_4D-style C[a,b,m,n] = A[a,b,k,l] * B[m,n,k,l], no symmetry,
+    block-constant initialize() values (tensor.cc:744-758)."""
+    from dtcf_gb300.rrr import Tensor, Contraction
+    n, nb = 16, 4
+    A = Tensor("cccc", (n,) * 4, (nb,) * 4).initialize()
+    B = Tensor("cccc", (n,) * 4, (nb,) * 4).initialize()
+    C = Tensor("cccc", (n,) * 4, (nb,) * 4)
+    want = oracle.rrr.contract(_as_oracle(A), _as_oracle(B), _as_oracle(C), "a,b,k,l", "m,n,k,l", "a,b,m,n", 1.0)
+    ctr = Contraction(A, B, C)
+    ctr.contract("a,b,k,l", "m,n,k,l", "a,b,m,n")
+    got = host(C.tiles).reshape(want.shape)
+    assert np.max(np.abs(got - want)) <= 1e-12 * np.abs(want).max()
+    assert ctr.plan("a,b,k,l", "m,n,k,l", "a,b,m,n").flops == 2.0 * n ** 6
