@@ -27,6 +27,15 @@ SIGNATURES = {
     "gbx_plan_flops": (_d, [_p]),
     "gbx_plan_destroy": (_i, [_p]),
     "gbx_grouped_gemm_f64": (_i, [_p, _i, _p]),
+    "gbx_cc_default_config": (None, [_p]),
+    "gbx_cc_create": (_i, [_p, _p, ctypes.POINTER(_p)]),
+    "gbx_cc_enqueue": (_i, [_p, _i, _p]),
+    "gbx_cc_iterate": (_i, [_p, _i, _p, _p]),
+    "gbx_cc_energies": (_i, [_p, _p, _ip]),
+    "gbx_cc_stats_get": (_i, [_p, _p]),
+    "gbx_cc_get_orbitals": (_i, [_p, _p, _p]),
+    "gbx_cc_get_amplitudes": (_i, [_p, _p, _p, _p]),
+    "gbx_cc_destroy": (_i, [_p]),
 }
 
 _lib = None

@@ -1,0 +1,638 @@
+// Coupled-cluster iteration driver (see cc.h): builds the synthetic system on
+// the device, plans every contraction of one CCD / CCSD iteration once, and
+// replays the iteration (optionally as one CUDA graph).
+#include "cc.h"
+#include "split.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace gbx {
+
+uint64_t cc_mix64(uint64_t z) {
+  z ^= z >> 30;
+  z *= 0xBF58476D1CE4E5B9ull;
+  z ^= z >> 27;
+  z *= 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return z;
+}
+
+CCStream::CCStream(uint64_t seed, int k) : state(cc_mix64(seed ^ (0x9E3779B97F4A7C15ull * (uint64_t)(k + 1)))) {}
+
+uint64_t CCStream::next() {
+  state += 0x9E3779B97F4A7C15ull;
+  return cc_mix64(state);
+}
+
+double CCStream::uniform() { return (double)(next() >> 11) * 0x1.0p-53; }
+
+namespace {
+
+// irrep occupation counts of one space
+std::vector<int> draw_counts(int n, int nirrep, int min_block, uint64_t seed, int stream) {
+  CCStream rng(seed, stream);
+  int need = std::min(min_block, nirrep > 0 ? n / nirrep : 0);
+  for (;;) {
+    std::vector<int> c(nirrep, 0);
+    for (int i = 0; i < n; ++i) {
+      int h = (int)(rng.uniform() * nirrep);
+      if (h >= nirrep) h = nirrep - 1;
+      ++c[h];
+    }
+    if (nirrep == 1 || *std::min_element(c.begin(), c.end()) >= need) return c;
+  }
+}
+
+void blocks_of(const std::vector<int>& counts, int max_block, std::vector<int>& ext, std::vector<int>& irr) {
+  for (size_t h = 0; h < counts.size(); ++h) {
+    int c = counts[h];
+    if (c == 0) continue;
+    int nb = (c + max_block - 1) / max_block;
+    for (int k = 0; k < nb; ++k) {
+      ext.push_back(c / nb + (k < c % nb ? 1 : 0));
+      irr.push_back((int)h);
+    }
+  }
+}
+
+}  // namespace
+
+struct CCTensor {
+  std::string spaces;
+  TensorLayout L;
+  double* d = nullptr;
+  ~CCTensor() { dev_free(d); }
+};
+
+}  // namespace gbx
+
+using namespace gbx;
+
+struct gbx_cc_job {
+  gbx_cc_config cfg;
+  int o = 0, v = 0, n = 0;
+  std::shared_ptr<BlockDim> occ, vir;
+  std::vector<int> irrep;
+  std::vector<double> eps;
+  int* d_irrep = nullptr;
+  double* d_eps = nullptr;
+  double* d_mag = nullptr;
+  CCDeviceTables tab;
+  std::map<std::string, std::unique_ptr<CCTensor>> T;
+  std::vector<std::unique_ptr<ContractionPlan>> cplans;
+  std::vector<std::unique_ptr<SumPlan>> splans;
+  std::vector<std::function<int(cudaStream_t)>> steps;  // one iteration
+  std::vector<std::unique_ptr<CCTileSet>> tilesets;
+  CCTileSet *den1 = nullptr, *den2 = nullptr;
+  double* d_partial = nullptr;
+  double* d_hist = nullptr;
+  int* d_count = nullptr;
+  int hist_cap = 4096;
+  int nenergies = 0;  // host view of the history length
+  int npartial = 608;
+  double flops = 0.0, gemm_flops = 0.0;
+  int launches = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+
+  ~gbx_cc_job() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    cplans.clear();
+    splans.clear();
+    T.clear();
+    tilesets.clear();
+    dev_free(d_irrep);
+    dev_free(d_eps);
+    dev_free(d_mag);
+    dev_free(d_partial);
+    dev_free(d_hist);
+    dev_free(d_count);
+  }
+
+  std::shared_ptr<BlockDim> dim_of(char s) { return s == 'o' ? occ : vir; }
+  int gstart(char s, int b) { return s == 'o' ? (int)occ->start[b] : o + (int)vir->start[b]; }
+
+  int tensor(const std::string& name, const std::string& spaces) {
+    auto t = std::make_unique<CCTensor>();
+    t->spaces = spaces;
+    std::vector<std::shared_ptr<BlockDim>> dims;
+    for (char c : spaces) dims.push_back(dim_of(c));
+    t->L = TensorLayout::full(dims, {}, 1, false);
+    GBX_TRY(dev_alloc((void**)&t->d, sizeof(double) * std::max<int64_t>(1, t->L.nelem)));
+    GBX_CUDA(cudaMemset(t->d, 0, sizeof(double) * std::max<int64_t>(1, t->L.nelem)));
+    T[name] = std::move(t);
+    return GBX_OK;
+  }
+
+  CCTensor* get(const std::string& name) { return T.at(name).get(); }
+
+  static std::vector<std::string> labels(const char* s) {
+    std::vector<std::string> out;
+    for (const char* p = s; *p; ++p) out.push_back(std::string(1, *p));
+    return out;
+  }
+
+  int check_labels(const CCTensor* t, const char* lab, const char* name) {
+    if (std::strlen(lab) != t->spaces.size()) return fail(GBX_EINVAL, "%s: label %s vs spaces %s", name, lab, t->spaces.c_str());
+    for (size_t i = 0; i < t->spaces.size(); ++i) {
+      char want = std::strchr("ijklmn", lab[i]) ? 'o' : 'v';
+      if (want != t->spaces[i]) return fail(GBX_EINVAL, "%s: label %s does not fit spaces %s", name, lab, t->spaces.c_str());
+    }
+    return GBX_OK;
+  }
+
+  // C[lc] += alpha * A[la] * B[lb]
+  int contract(const char* c, const char* lc, const char* a, const char* la, const char* b, const char* lb,
+               double alpha, bool a_static = false) {
+    CCTensor *C = get(c), *A = get(a), *B = get(b);
+    GBX_TRY(check_labels(C, lc, c));
+    GBX_TRY(check_labels(A, la, a));
+    GBX_TRY(check_labels(B, lb, b));
+    std::unique_ptr<ContractionPlan> p;
+    Engine e = cfg.engine == GBX_MODE_SPLIT ? Engine::Split : Engine::F64;
+    GBX_TRY(plan_contraction(A->L, B->L, C->L, labels(la), labels(lb), labels(lc), e, cfg.slices, p));
+    p->a_static = a_static;
+    flops += p->flops;
+    gemm_flops += p->gemm_flops;
+    ContractionPlan* pp = p.get();
+    double *dA = A->d, *dB = B->d, *dC = C->d;
+    steps.push_back([=](cudaStream_t st) { return pp->execute(dA, dB, dC, alpha, st); });
+    launches += 4;
+    cplans.push_back(std::move(p));
+    return GBX_OK;
+  }
+
+  // C[lc] += coef * A[la]
+  int sum(const char* c, const char* lc, const char* a, const char* la, double coef) {
+    CCTensor *C = get(c), *A = get(a);
+    GBX_TRY(check_labels(C, lc, c));
+    GBX_TRY(check_labels(A, la, a));
+    std::unique_ptr<SumPlan> p;
+    GBX_TRY(plan_sum(A->L, C->L, labels(la), labels(lc), coef, p));
+    SumPlan* pp = p.get();
+    double *dA = A->d, *dC = C->d;
+    steps.push_back([=](cudaStream_t st) { return pp->execute(dA, dC, 1.0, st); });
+    launches += 1;
+    splans.push_back(std::move(p));
+    return GBX_OK;
+  }
+
+  int zero(const char* c) {
+    CCTensor* C = get(c);
+    double* d = C->d;
+    size_t bytes = sizeof(double) * C->L.nelem;
+    steps.push_back([=](cudaStream_t st) {
+      GBX_CUDA(cudaMemsetAsync(d, 0, bytes, st));
+      return GBX_OK;
+    });
+    launches += 1;
+    return GBX_OK;
+  }
+
+  CCTileSet* tileset(const CCTensor* t) {
+    std::vector<CCTile> h;
+    for (size_t i = 0; i < t->L.tiles.size(); ++i) {
+      CCTile ct;
+      std::memset(&ct, 0, sizeof(ct));
+      ct.off = t->L.off[i];
+      ct.rank = t->L.rank;
+      int64_t nn = 1;
+      for (int d = 0; d < t->L.rank; ++d) {
+        int b = t->L.tiles[i][d];
+        ct.ext[d] = (uint32_t)t->L.dims[d]->ext[b];
+        ct.gstart[d] = gstart(t->spaces[d], b);
+        nn *= ct.ext[d];
+      }
+      ct.n = (uint32_t)nn;
+      h.push_back(ct);
+    }
+    auto ts = std::make_unique<CCTileSet>();
+    if (ts->upload(h) != GBX_OK) return nullptr;
+    tilesets.push_back(std::move(ts));
+    return tilesets.back().get();
+  }
+
+  int denom(const char* out, const char* in, CCTileSet* ts) {
+    double* dout = get(out)->d;
+    const double* din = get(in)->d;
+    CCDeviceTables tb = tab;
+    steps.push_back([=](cudaStream_t st) { return run_cc_tiles(*ts, CC_OP_DENOM, tb, din, dout, st); });
+    launches += 1;
+    return GBX_OK;
+  }
+
+  int energy_step() {
+    const double* V = get("OOVV")->d;
+    const double* tau = get(cfg.method == GBX_CC_CCSD ? "tau" : "t2")->d;
+    int64_t n = get("OOVV")->L.nelem;
+    double* part = d_partial;
+    double* hist = d_hist;
+    int* cnt = d_count;
+    int np = npartial, cap = hist_cap;
+    steps.push_back([=](cudaStream_t st) { return gbx::run_energy(V, tau, n, part, np, hist, cnt, cap, st); });
+    launches += 2;
+    return GBX_OK;
+  }
+
+  int build();
+  int tau_steps();
+};
+
+// tau = t2 + t1 t1 - t1 t1 (i<->j), taut = t2 + (t1 t1 - t1 t1) / 2
+int gbx_cc_job::tau_steps() {
+  GBX_TRY(zero("tau"));
+  GBX_TRY(sum("tau", "ijab", "t2", "ijab", 1.0));
+  GBX_TRY(contract("tau", "ijab", "t1", "ia", "t1", "jb", 1.0));
+  GBX_TRY(contract("tau", "ijab", "t1", "ib", "t1", "ja", -1.0));
+  GBX_TRY(zero("taut"));
+  GBX_TRY(sum("taut", "ijab", "t2", "ijab", 1.0));
+  GBX_TRY(contract("taut", "ijab", "t1", "ia", "t1", "jb", 0.5));
+  GBX_TRY(contract("taut", "ijab", "t1", "ib", "t1", "ja", -0.5));
+  return GBX_OK;
+}
+
+int gbx_cc_job::build() {
+  const bool sd = cfg.method == GBX_CC_CCSD;
+  // amplitudes, residuals, intermediates
+  GBX_TRY(tensor("t2", "oovv"));
+  GBX_TRY(tensor("R2", "oovv"));
+  GBX_TRY(tensor("Xa", "oovv"));
+  GBX_TRY(tensor("Fae", "vv"));
+  GBX_TRY(tensor("Fmi", "oo"));
+  GBX_TRY(tensor("Wmnij", "oooo"));
+  GBX_TRY(tensor("Wmbej", "ovvo"));
+  GBX_TRY(tensor("Q", "oovv"));
+  for (const char* nm : {"OOOO", "OOVV", "OVVO", "VVVV"}) {
+    std::string sp;
+    for (const char* c = nm; *c; ++c) sp += (char)(*c == 'O' ? 'o' : 'v');
+    GBX_TRY(tensor(nm, sp));
+  }
+  if (sd) {
+    GBX_TRY(tensor("t1", "ov"));
+    GBX_TRY(tensor("R1", "ov"));
+    GBX_TRY(tensor("tau", "oovv"));
+    GBX_TRY(tensor("taut", "oovv"));
+    GBX_TRY(tensor("Fme", "ov"));
+    GBX_TRY(tensor("Fbe", "vv"));
+    GBX_TRY(tensor("Fmj", "oo"));
+    GBX_TRY(tensor("Xoooo", "oooo"));
+    GBX_TRY(tensor("Zp", "ooov"));
+    GBX_TRY(tensor("V3", "oovo"));
+    for (const char* nm : {"OOOV", "OVVV", "OOVO", "OVOV", "VVVO", "OVOO"}) {
+      std::string sp;
+      for (const char* c = nm; *c; ++c) sp += (char)(*c == 'O' ? 'o' : 'v');
+      GBX_TRY(tensor(nm, sp));
+    }
+  }
+  // integrals on the device
+  cudaStream_t st0 = 0;
+  for (auto& kv : T) {
+    const std::string& nm = kv.first;
+    bool integ = nm.size() == 4 && std::all_of(nm.begin(), nm.end(), [](char c) { return c == 'O' || c == 'V'; });
+    if (!integ) continue;
+    CCTileSet* ts = tileset(kv.second.get());
+    if (!ts) return fail(GBX_ENOMEM, "tile set upload failed");
+    GBX_TRY(run_cc_tiles(*ts, CC_OP_INTEGRAL, tab, nullptr, kv.second->d, st0));
+  }
+  den2 = tileset(get("t2"));
+  if (sd) den1 = tileset(get("t1"));
+  if (!den2 || (sd && !den1)) return fail(GBX_ENOMEM, "tile set upload failed");
+  // MP2 guess t2 = <ij||ab> / D, t1 = 0, energy 0
+  GBX_TRY(run_cc_tiles(*den2, CC_OP_DENOM, tab, get("OOVV")->d, get("t2")->d, st0));
+  const char* TAU = sd ? "tau" : "t2";
+  const char* TAUT = sd ? "taut" : "t2";
+  if (sd) {
+    // initial tau / taut from the guess, run once outside the iteration
+    size_t first = steps.size();
+    GBX_TRY(tau_steps());
+    for (size_t i = first; i < steps.size(); ++i) GBX_TRY(steps[i](st0));
+    steps.resize(first);
+  }
+  GBX_TRY(gbx::run_energy(get("OOVV")->d, get(TAU)->d, get("OOVV")->L.nelem, d_partial, npartial, d_hist, d_count,
+                          hist_cap, st0));
+  launches = 0;
+
+  // ---- one iteration --------------------------------------------------------
+  // F_ae, F_mi, F_me
+  GBX_TRY(zero("Fae"));
+  if (sd) GBX_TRY(contract("Fae", "ae", "t1", "mf", "OVVV", "mafe", 1.0));
+  GBX_TRY(contract("Fae", "ae", TAUT, "mnaf", "OOVV", "mnef", -0.5));
+  GBX_TRY(zero("Fmi"));
+  if (sd) GBX_TRY(contract("Fmi", "mi", "t1", "ne", "OOOV", "mnie", 1.0));
+  GBX_TRY(contract("Fmi", "mi", TAUT, "inef", "OOVV", "mnef", 0.5));
+  if (sd) {
+    GBX_TRY(zero("Fme"));
+    GBX_TRY(contract("Fme", "me", "t1", "nf", "OOVV", "mnef", 1.0));
+  }
+  // W_mnij (with the ladder's 1/8 tau <mn||ef> tau term folded in: 1/2 instead of 1/4)
+  GBX_TRY(zero("Wmnij"));
+  GBX_TRY(sum("Wmnij", "mnij", "OOOO", "mnij", 1.0));
+  if (sd) {
+    GBX_TRY(zero("Xoooo"));
+    GBX_TRY(contract("Xoooo", "mnij", "t1", "je", "OOOV", "mnie", 1.0));
+    GBX_TRY(sum("Wmnij", "mnij", "Xoooo", "mnij", 1.0));
+    GBX_TRY(sum("Wmnij", "mnij", "Xoooo", "mnji", -1.0));
+  }
+  GBX_TRY(contract("Wmnij", "mnij", TAU, "ijef", "OOVV", "mnef", 0.5));
+  // W_mbej
+  GBX_TRY(zero("Wmbej"));
+  GBX_TRY(sum("Wmbej", "mbej", "OVVO", "mbej", 1.0));
+  if (sd) {
+    GBX_TRY(contract("Wmbej", "mbej", "t1", "jf", "OVVV", "mbef", 1.0));
+    GBX_TRY(contract("Wmbej", "mbej", "t1", "nb", "OOVO", "mnej", -1.0));
+  }
+  GBX_TRY(zero("Q"));
+  GBX_TRY(sum("Q", "jnfb", "t2", "jnfb", 0.5));
+  if (sd) GBX_TRY(contract("Q", "jnfb", "t1", "jf", "t1", "nb", 1.0));
+  GBX_TRY(contract("Wmbej", "mbej", "Q", "jnfb", "OOVV", "mnef", -1.0));
+  // T1 residual
+  if (sd) {
+    GBX_TRY(zero("R1"));
+    GBX_TRY(contract("R1", "ia", "t1", "ie", "Fae", "ae", 1.0));
+    GBX_TRY(contract("R1", "ia", "t1", "ma", "Fmi", "mi", -1.0));
+    GBX_TRY(contract("R1", "ia", "t2", "imae", "Fme", "me", 1.0));
+    GBX_TRY(contract("R1", "ia", "t1", "nf", "OVOV", "naif", -1.0));
+    GBX_TRY(contract("R1", "ia", "t2", "imef", "OVVV", "maef", -0.5));
+    GBX_TRY(contract("R1", "ia", "t2", "mnae", "OOVO", "nmei", -0.5));
+  }
+  // T2 residual
+  GBX_TRY(zero("R2"));
+  GBX_TRY(sum("R2", "ijab", "OOVV", "ijab", 1.0));
+  const char* FBE = "Fae";
+  const char* FMJ = "Fmi";
+  if (sd) {
+    GBX_TRY(zero("Fbe"));
+    GBX_TRY(sum("Fbe", "be", "Fae", "be", 1.0));
+    GBX_TRY(contract("Fbe", "be", "t1", "mb", "Fme", "me", -0.5));
+    GBX_TRY(zero("Fmj"));
+    GBX_TRY(sum("Fmj", "mj", "Fmi", "mj", 1.0));
+    GBX_TRY(contract("Fmj", "mj", "t1", "je", "Fme", "me", 0.5));
+    FBE = "Fbe";
+    FMJ = "Fmj";
+  }
+  // P(ab) t_ij^ae F'_be
+  GBX_TRY(zero("Xa"));
+  GBX_TRY(contract("Xa", "ijab", "t2", "ijae", FBE, "be", 1.0));
+  GBX_TRY(sum("R2", "ijab", "Xa", "ijab", 1.0));
+  GBX_TRY(sum("R2", "ijab", "Xa", "ijba", -1.0));
+  // -P(ij) t_im^ab F'_mj
+  GBX_TRY(zero("Xa"));
+  GBX_TRY(contract("Xa", "ijab", "t2", "imab", FMJ, "mj", 1.0));
+  GBX_TRY(sum("R2", "ijab", "Xa", "ijab", -1.0));
+  GBX_TRY(sum("R2", "ijab", "Xa", "jiab", 1.0));
+  // 1/2 tau_mn^ab W_mnij
+  GBX_TRY(contract("R2", "ijab", TAU, "mnab", "Wmnij", "mnij", 0.5));
+  // 1/2 tau_ij^ef <ab||ef>: the ladder, integrals as the (static) A operand
+  GBX_TRY(contract("R2", "ijab", "VVVV", "abef", TAU, "ijef", 0.5, true));
+  if (sd) {
+    // -1/2 P(ab) t_m^b sum_ef tau_ij^ef <am||ef> = +1/2 P(ab) sum_m t_m^b Z'_ijma
+    GBX_TRY(zero("Zp"));
+    GBX_TRY(contract("Zp", "ijma", TAU, "ijef", "OVVV", "maef", 1.0));
+    GBX_TRY(zero("Xa"));
+    GBX_TRY(contract("Xa", "ijab", "Zp", "ijma", "t1", "mb", 1.0));
+    GBX_TRY(sum("R2", "ijab", "Xa", "ijab", 0.5));
+    GBX_TRY(sum("R2", "ijab", "Xa", "ijba", -0.5));
+  }
+  // P(ij)P(ab) (t_im^ae W_mbej - t_i^e t_m^a <mb||ej>)
+  GBX_TRY(zero("Xa"));
+  GBX_TRY(contract("Xa", "ijab", "t2", "imae", "Wmbej", "mbej", 1.0));
+  if (sd) {
+    GBX_TRY(zero("V3"));
+    GBX_TRY(contract("V3", "imbj", "t1", "ie", "OVVO", "mbej", 1.0));
+    GBX_TRY(contract("Xa", "ijab", "t1", "ma", "V3", "imbj", -1.0));
+  }
+  GBX_TRY(sum("R2", "ijab", "Xa", "ijab", 1.0));
+  GBX_TRY(sum("R2", "ijab", "Xa", "jiab", -1.0));
+  GBX_TRY(sum("R2", "ijab", "Xa", "ijba", -1.0));
+  GBX_TRY(sum("R2", "ijab", "Xa", "jiba", 1.0));
+  if (sd) {
+    // P(ij) t_i^e <ab||ej>
+    GBX_TRY(zero("Xa"));
+    GBX_TRY(contract("Xa", "ijab", "t1", "ie", "VVVO", "abej", 1.0));
+    GBX_TRY(sum("R2", "ijab", "Xa", "ijab", 1.0));
+    GBX_TRY(sum("R2", "ijab", "Xa", "jiab", -1.0));
+    // -P(ab) t_m^a <mb||ij>
+    GBX_TRY(zero("Xa"));
+    GBX_TRY(contract("Xa", "ijab", "t1", "ma", "OVOO", "mbij", 1.0));
+    GBX_TRY(sum("R2", "ijab", "Xa", "ijab", -1.0));
+    GBX_TRY(sum("R2", "ijab", "Xa", "ijba", 1.0));
+  }
+  // Jacobi update and energy
+  GBX_TRY(denom("t2", "R2", den2));
+  if (sd) {
+    GBX_TRY(denom("t1", "R1", den1));
+    GBX_TRY(tau_steps());
+  }
+  GBX_TRY(energy_step());
+  return GBX_OK;
+}
+
+extern "C" {
+
+void gbx_cc_default_config(gbx_cc_config* c) {
+  std::memset(c, 0, sizeof(*c));
+  c->nocc = 8;
+  c->nvir = 24;
+  c->nirrep = 1;
+  c->max_block = 16;
+  c->min_block = 1;
+  c->method = GBX_CC_CCSD;
+  c->engine = GBX_MODE_FP64;
+  c->slices = 0;
+  c->use_graph = 1;
+  c->seed = 1;
+  c->eps_occ_lo = -2.0;
+  c->eps_occ_hi = -0.5;
+  c->eps_vir_lo = 0.2;
+  c->eps_vir_hi = 3.0;
+  c->v_scale = 1e-2;
+  c->v_decay = 8.0;
+}
+
+int gbx_cc_create(const gbx_cc_config* cfg, void* stream, gbx_cc_job** out) {
+  if (!cfg || !out) return fail(GBX_EINVAL, "null argument");
+  *out = nullptr;
+  if (cfg->nocc < 1 || cfg->nvir < 1 || cfg->max_block < 1 ||
+      !(cfg->nirrep == 1 || cfg->nirrep == 2 || cfg->nirrep == 4 || cfg->nirrep == 8) ||
+      (cfg->method != GBX_CC_CCD && cfg->method != GBX_CC_CCSD) ||
+      (cfg->engine != GBX_MODE_FP64 && cfg->engine != GBX_MODE_SPLIT) || cfg->v_decay <= 0)
+    return fail(GBX_EINVAL, "bad CC configuration");
+  auto job = std::make_unique<gbx_cc_job>();
+  job->cfg = *cfg;
+  job->o = cfg->nocc;
+  job->v = cfg->nvir;
+  job->n = cfg->nocc + cfg->nvir;
+  // orbitals
+  std::vector<int> ext_o, irr_o, ext_v, irr_v;
+  blocks_of(draw_counts(job->o, cfg->nirrep, cfg->min_block, cfg->seed, 1), cfg->max_block, ext_o, irr_o);
+  blocks_of(draw_counts(job->v, cfg->nirrep, cfg->min_block, cfg->seed, 2), cfg->max_block, ext_v, irr_v);
+  job->occ = BlockDim::make(ext_o, irr_o);
+  job->vir = BlockDim::make(ext_v, irr_v);
+  for (size_t b = 0; b < ext_o.size(); ++b)
+    for (int k = 0; k < ext_o[b]; ++k) job->irrep.push_back(irr_o[b]);
+  for (size_t b = 0; b < ext_v.size(); ++b)
+    for (int k = 0; k < ext_v[b]; ++k) job->irrep.push_back(irr_v[b]);
+  CCStream eo(cfg->seed, 3), ev(cfg->seed, 4), ei(cfg->seed, 5);
+  for (int i = 0; i < job->o; ++i) job->eps.push_back(cfg->eps_occ_lo + (cfg->eps_occ_hi - cfg->eps_occ_lo) * eo.uniform());
+  for (int a = 0; a < job->v; ++a) job->eps.push_back(cfg->eps_vir_lo + (cfg->eps_vir_hi - cfg->eps_vir_lo) * ev.uniform());
+  std::vector<double> mag(2 * job->n + 1);
+  for (size_t d = 0; d < mag.size(); ++d) mag[d] = cfg->v_scale * std::exp(-(double)d / cfg->v_decay);
+  GBX_TRY(dev_alloc((void**)&job->d_irrep, sizeof(int) * job->n));
+  GBX_TRY(dev_alloc((void**)&job->d_eps, sizeof(double) * job->n));
+  GBX_TRY(dev_alloc((void**)&job->d_mag, sizeof(double) * mag.size()));
+  GBX_CUDA(cudaMemcpy(job->d_irrep, job->irrep.data(), sizeof(int) * job->n, cudaMemcpyHostToDevice));
+  GBX_CUDA(cudaMemcpy(job->d_eps, job->eps.data(), sizeof(double) * job->n, cudaMemcpyHostToDevice));
+  GBX_CUDA(cudaMemcpy(job->d_mag, mag.data(), sizeof(double) * mag.size(), cudaMemcpyHostToDevice));
+  job->tab.irrep = job->d_irrep;
+  job->tab.eps = job->d_eps;
+  job->tab.mag = job->d_mag;
+  job->tab.norb = job->n;
+  job->tab.nocc = job->o;
+  job->tab.seed_int = ei.next();
+  GBX_TRY(dev_alloc((void**)&job->d_partial, sizeof(double) * job->npartial));
+  GBX_TRY(dev_alloc((void**)&job->d_hist, sizeof(double) * job->hist_cap));
+  GBX_TRY(dev_alloc((void**)&job->d_count, sizeof(int)));
+  GBX_CUDA(cudaMemset(job->d_count, 0, sizeof(int)));
+  GBX_TRY(job->build());
+  GBX_CUDA(cudaDeviceSynchronize());
+  job->nenergies = 1;
+  (void)stream;
+  *out = job.release();
+  return GBX_OK;
+}
+
+int gbx_cc_enqueue(gbx_cc_job* job, int niter, void* stream) {
+  if (!job || niter < 0) return fail(GBX_EINVAL, "bad arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (job->cfg.use_graph && !job->exec && niter > 0) {
+    cudaStream_t cap;
+    GBX_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    GBX_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    int rc = GBX_OK;
+    for (auto& s : job->steps) {
+      rc = s(cap);
+      if (rc != GBX_OK) break;
+    }
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    if (rc != GBX_OK) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+    job->graph = g;
+    GBX_CUDA(cudaGraphInstantiate(&job->exec, g, 0));
+  }
+  for (int it = 0; it < niter; ++it) {
+    if (job->exec) {
+      GBX_CUDA(cudaGraphLaunch(job->exec, st));
+    } else {
+      for (auto& s : job->steps) GBX_TRY(s(st));
+    }
+  }
+  job->nenergies += niter;
+  return GBX_OK;
+}
+
+int gbx_cc_iterate(gbx_cc_job* job, int niter, double* energies, void* stream) {
+  GBX_TRY(gbx_cc_enqueue(job, niter, stream));
+  GBX_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  if (energies && niter > 0) {
+    int first = job->nenergies - niter;
+    if (first + niter > job->hist_cap) return fail(GBX_EUNSUPPORTED, "energy history full");
+    GBX_CUDA(cudaMemcpy(energies, job->d_hist + first, sizeof(double) * niter, cudaMemcpyDeviceToHost));
+  }
+  return GBX_OK;
+}
+
+int gbx_cc_energies(gbx_cc_job* job, double* energies, int* count) {
+  if (!job || !count) return fail(GBX_EINVAL, "bad arguments");
+  int n = std::min(std::min(*count, job->nenergies), job->hist_cap);
+  GBX_CUDA(cudaDeviceSynchronize());
+  if (n > 0) GBX_CUDA(cudaMemcpy(energies, job->d_hist, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  *count = n;
+  return GBX_OK;
+}
+
+int gbx_cc_stats_get(const gbx_cc_job* job, gbx_cc_stats* s) {
+  if (!job || !s) return fail(GBX_EINVAL, "bad arguments");
+  std::memset(s, 0, sizeof(*s));
+  s->flops_per_iter = job->flops;
+  s->gemm_flops_per_iter = job->gemm_flops;
+  double bytes = 0;
+  for (auto& kv : job->T) bytes += 8.0 * kv.second->L.nelem;
+  for (auto& p : job->cplans) bytes += 8.0 * (p->a_elems + p->b_elems + p->c_elems) + split_plan_bytes(p->split);
+  s->resident_bytes = bytes;
+  s->ncontractions = (int)job->cplans.size();
+  s->nsums = (int)job->splans.size();
+  s->nblocks_occ = (int)job->occ->ext.size();
+  s->nblocks_vir = (int)job->vir->ext.size();
+  s->launches_per_iter = job->launches;
+  return GBX_OK;
+}
+
+int gbx_cc_get_orbitals(const gbx_cc_job* job, int* irrep, double* eps) {
+  if (!job) return fail(GBX_EINVAL, "null job");
+  if (irrep) std::memcpy(irrep, job->irrep.data(), sizeof(int) * job->n);
+  if (eps) std::memcpy(eps, job->eps.data(), sizeof(double) * job->n);
+  return GBX_OK;
+}
+
+int gbx_cc_get_amplitudes(gbx_cc_job* job, double* t1, double* t2, void* stream) {
+  if (!job) return fail(GBX_EINVAL, "null job");
+  GBX_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  const int o = job->o, v = job->v;
+  auto dump = [&](const char* name, double* out, int rank) -> int {
+    CCTensor* t = job->get(name);
+    std::vector<double> h(t->L.nelem);
+    GBX_CUDA(cudaMemcpy(h.data(), t->d, sizeof(double) * t->L.nelem, cudaMemcpyDeviceToHost));
+    int full[4] = {o, o, v, v};
+    if (rank == 2) {
+      full[0] = o;
+      full[1] = v;
+    }
+    int64_t total = 1;
+    for (int d = 0; d < rank; ++d) total *= full[d];
+    std::fill(out, out + total, 0.0);
+    for (size_t ti = 0; ti < t->L.tiles.size(); ++ti) {
+      const Coords& c = t->L.tiles[ti];
+      int ext[4], st[4];
+      for (int d = 0; d < rank; ++d) {
+        ext[d] = t->L.dims[d]->ext[c[d]];
+        st[d] = (int)t->L.dims[d]->start[c[d]];
+      }
+      int64_t e = 0;
+      int idx[4] = {0, 0, 0, 0};
+      for (;;) {
+        int64_t off = 0;
+        for (int d = 0; d < rank; ++d) off = off * full[d] + st[d] + idx[d];
+        out[off] = h[t->L.off[ti] + e];
+        ++e;
+        int d = rank - 1;
+        for (; d >= 0; --d) {
+          if (++idx[d] < ext[d]) break;
+          idx[d] = 0;
+        }
+        if (d < 0) break;
+      }
+    }
+    return GBX_OK;
+  };
+  if (t2) GBX_TRY(dump("t2", t2, 4));
+  if (t1) {
+    if (job->cfg.method == GBX_CC_CCSD) GBX_TRY(dump("t1", t1, 2));
+    else std::fill(t1, t1 + (int64_t)o * v, 0.0);
+  }
+  return GBX_OK;
+}
+
+int gbx_cc_destroy(gbx_cc_job* job) {
+  delete job;
+  return GBX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,180 @@
+// Element-wise kernels of the coupled-cluster driver: synthetic integral
+// generation, orbital-energy denominators (MP2 guess, Jacobi update) and the
+// deterministic FP64 dot product behind the correlation energy.
+//
+// All of them walk a list of tiles; a tile carries its element offset, rank,
+// extents and the global orbital index of the first orbital of each block.
+#include <algorithm>
+
+#include "cc.h"
+
+namespace gbx {
+
+namespace {
+constexpr int kThreads = 256;
+constexpr int kChunk = 2048;
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z ^= z >> 30;
+  z *= 0xBF58476D1CE4E5B9ull;
+  z ^= z >> 27;
+  z *= 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return z;
+}
+
+// <pq||rs> of the synthetic Hamiltonian (see cc.h for the definition).
+__device__ __forceinline__ double integral(int p, int q, int r, int s, const CCDeviceTables& t) {
+  if (p == q || r == s) return 0.0;
+  if ((t.irrep[p] ^ t.irrep[q] ^ t.irrep[r] ^ t.irrep[s]) != 0) return 0.0;
+  double sg = 1.0;
+  if (p > q) {
+    int x = p; p = q; q = x;
+    sg = -sg;
+  }
+  if (r > s) {
+    int x = r; r = s; s = x;
+    sg = -sg;
+  }
+  uint64_t P = (uint64_t)p * (uint64_t)t.norb + (uint64_t)q;
+  uint64_t R = (uint64_t)r * (uint64_t)t.norb + (uint64_t)s;
+  if (P > R) {
+    uint64_t x = P; P = R; R = x;
+  }
+  uint64_t h = mix64(t.seed_int ^ (P * 0x9E3779B97F4A7C15ull + R * 0xC2B2AE3D27D4EB4Full));
+  double v = t.mag[(q - p) + (s - r)];
+  return ((h >> 63) ? -v : v) * sg;
+}
+}  // namespace
+
+__global__ void __launch_bounds__(kThreads) cc_tile_kernel(const CCTile* __restrict__ tiles,
+                                                           const uint32_t* __restrict__ first, int ntiles,
+                                                           uint32_t nchunks, int op, CCDeviceTables tab,
+                                                           const double* __restrict__ in, double* __restrict__ out) {
+  for (uint32_t chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
+    int lo = 0, hi = ntiles - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (__ldg(first + mid) <= chunk) lo = mid; else hi = mid - 1;
+    }
+    const CCTile& t = tiles[lo];
+    const uint32_t base = (chunk - __ldg(first + lo)) * kChunk;
+    for (int k = 0; k < kChunk / kThreads; ++k) {
+      uint32_t e = base + (uint32_t)(k * kThreads) + threadIdx.x;
+      if (e >= t.n) break;
+      int g[4];
+      uint32_t rem = e;
+      for (int d = t.rank - 1; d >= 0; --d) {
+        uint32_t q = rem / t.ext[d];
+        g[d] = t.gstart[d] + (int)(rem - q * t.ext[d]);
+        rem = q;
+      }
+      const int64_t o = t.off + e;
+      if (op == CC_OP_INTEGRAL) {
+        out[o] = integral(g[0], g[1], g[2], g[3], tab);
+      } else {
+        // denominator: sum over occupied indices of eps minus over virtual ones
+        double dnm = 0.0;
+        for (int d = 0; d < t.rank; ++d) {
+          double ev = tab.eps[g[d]];
+          dnm = (g[d] < tab.nocc) ? __dadd_rn(dnm, ev) : __dsub_rn(dnm, ev);
+        }
+        out[o] = __ddiv_rn(in[o], dnm);
+      }
+    }
+  }
+}
+
+// Per-CTA partial sums of x*y over n elements, in a fixed order.
+__global__ void __launch_bounds__(kThreads) dot_partial_kernel(const double* __restrict__ x,
+                                                               const double* __restrict__ y, int64_t n,
+                                                               double* __restrict__ partial) {
+  __shared__ double red[kThreads];
+  double s = 0.0;
+  int64_t per = (n + gridDim.x - 1) / gridDim.x;
+  int64_t lo = per * blockIdx.x, hi = min(n, lo + per);
+  for (int64_t i = lo + threadIdx.x; i < hi; i += kThreads) s = fma(x[i], y[i], s);
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = kThreads / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+__global__ void dot_final_kernel(const double* __restrict__ partial, int np, double scale, double* __restrict__ out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < np; ++i) s += partial[i];
+    *out = s * scale;
+  }
+}
+
+__global__ void energy_final_kernel(const double* __restrict__ partial, int np, double scale, double* __restrict__ hist,
+                                    int* __restrict__ count, int cap) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < np; ++i) s += partial[i];
+    int k = *count;
+    if (k < cap) hist[k] = s * scale;
+    *count = k + 1;
+  }
+}
+
+int run_energy(const double* V, const double* tau, int64_t n, double* partial, int npartial, double* hist, int* count,
+               int cap, cudaStream_t st) {
+  dot_partial_kernel<<<npartial, kThreads, 0, st>>>(V, tau, n, partial);
+  GBX_CUDA(cudaGetLastError());
+  energy_final_kernel<<<1, 32, 0, st>>>(partial, npartial, 0.25, hist, count, cap);
+  GBX_CUDA(cudaGetLastError());
+  return GBX_OK;
+}
+
+int CCTileSet::upload(const std::vector<CCTile>& h) {
+  release();
+  ntiles = (int)h.size();
+  if (!ntiles) return GBX_OK;
+  std::vector<uint32_t> f(ntiles + 1);
+  uint64_t c = 0;
+  for (int i = 0; i < ntiles; ++i) {
+    f[i] = (uint32_t)c;
+    c += (h[i].n + kChunk - 1) / kChunk;
+  }
+  f[ntiles] = (uint32_t)c;
+  nchunks = (uint32_t)c;
+  GBX_TRY(dev_alloc((void**)&d_tiles, sizeof(CCTile) * ntiles));
+  GBX_TRY(dev_alloc((void**)&d_first, sizeof(uint32_t) * (ntiles + 1)));
+  GBX_CUDA(cudaMemcpy(d_tiles, h.data(), sizeof(CCTile) * ntiles, cudaMemcpyHostToDevice));
+  GBX_CUDA(cudaMemcpy(d_first, f.data(), sizeof(uint32_t) * (ntiles + 1), cudaMemcpyHostToDevice));
+  return GBX_OK;
+}
+
+void CCTileSet::release() {
+  dev_free(d_tiles);
+  dev_free(d_first);
+  d_tiles = nullptr;
+  d_first = nullptr;
+  ntiles = 0;
+  nchunks = 0;
+}
+
+int run_cc_tiles(const CCTileSet& ts, int op, const CCDeviceTables& tab, const double* in, double* out,
+                 cudaStream_t st) {
+  if (ts.ntiles == 0 || ts.nchunks == 0) return GBX_OK;
+  int grid = (int)std::min<uint32_t>(ts.nchunks, 152u * 16u);
+  cc_tile_kernel<<<grid, kThreads, 0, st>>>(ts.d_tiles, ts.d_first, ts.ntiles, ts.nchunks, op, tab, in, out);
+  GBX_CUDA(cudaGetLastError());
+  return GBX_OK;
+}
+
+int run_dot(const double* x, const double* y, int64_t n, double scale, double* partial, int npartial, double* out,
+            cudaStream_t st) {
+  dot_partial_kernel<<<npartial, kThreads, 0, st>>>(x, y, n, partial);
+  GBX_CUDA(cudaGetLastError());
+  dot_final_kernel<<<1, 32, 0, st>>>(partial, npartial, scale, out);
+  GBX_CUDA(cudaGetLastError());
+  return GBX_OK;
+}
+
+}  // namespace gbx

@@ -23,5 +23,6 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
 // split_a: re-split A (false when A is unchanged since the last run).
 int run_split_plan(SplitPlan* sp, bool split_a, cudaStream_t st);
 void destroy_split_plan(SplitPlan* sp);
+double split_plan_bytes(const SplitPlan* sp);
 
 }  // namespace gbx

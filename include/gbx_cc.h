@@ -1,0 +1,73 @@
+/*
+ * gbx_cc.h -- C ABI of the coupled-cluster iteration driver and the
+ * continuous-batching request loop built on the gbx contraction path.
+ *
+ * The reference has no CC iteration of its own: its DLTC residual tables
+ * (DLTC/ccd-t2.cc:45-95, DLTC/ccsd-t1.cc:40-109, DLTC/ccsd-t2.cc:55-216) are
+ * the workload definitions this driver executes, completed with the
+ * permutation operators, coefficients and the Jacobi update a converging
+ * spin-orbital CCSD needs.  Conventions as in gbx.h: int status, messages via
+ * gbx_last_error(), streams as void*.
+ */
+#ifndef GBX_CC_H
+#define GBX_CC_H
+#include <stdint.h>
+
+#include "gbx.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBX_CC_CCD 0
+#define GBX_CC_CCSD 1
+
+typedef struct {
+    int nocc, nvir;      /* spin orbitals */
+    int nirrep;          /* 1, 2, 4 or 8 (XOR product rule) */
+    int max_block;       /* an irrep's orbitals are cut into blocks of at most this size */
+    int min_block;       /* irrep occupation draws repeat until each irrep has this many */
+    int method;          /* GBX_CC_CCD or GBX_CC_CCSD */
+    int engine;          /* GBX_MODE_FP64 or GBX_MODE_SPLIT */
+    int slices;          /* split engine: bf16 slices per operand (0 = default) */
+    int use_graph;       /* capture one iteration as a CUDA graph */
+    uint64_t seed;
+    double eps_occ_lo, eps_occ_hi, eps_vir_lo, eps_vir_hi;
+    double v_scale, v_decay; /* |<pq||rs>| = v_scale * exp(-(|p-q| + |r-s|) / v_decay) */
+} gbx_cc_config;
+
+typedef struct {
+    double flops_per_iter;       /* algorithmic FP64 flops of one iteration (nonzero block triples) */
+    double gemm_flops_per_iter;  /* flops the packed GEMMs execute */
+    double resident_bytes;       /* device bytes held by the job (tensors + plans) */
+    int ncontractions, nsums, nblocks_occ, nblocks_vir;
+    int launches_per_iter;       /* kernels launched by one iteration */
+} gbx_cc_stats;
+
+typedef struct gbx_cc_job gbx_cc_job;
+
+/* Fill cfg with the defaults of the synthetic system (seed 1, eps ranges
+ * [-2,-0.5] / [0.2,3.0], v_scale 1e-2, v_decay 8, block 16, CCSD, FP64). */
+GBX_API void gbx_cc_default_config(gbx_cc_config* cfg);
+/* Build the job: orbitals, integrals (on the device), plans, MP2 guess. */
+GBX_API int gbx_cc_create(const gbx_cc_config* cfg, void* stream, gbx_cc_job** job);
+/* Enqueue niter Jacobi iterations on stream without waiting; the energy of
+ * each lands in the job's device history. */
+GBX_API int gbx_cc_enqueue(gbx_cc_job* job, int niter, void* stream);
+/* Run niter iterations and return their correlation energies (host array of
+ * niter); waits for the stream. */
+GBX_API int gbx_cc_iterate(gbx_cc_job* job, int niter, double* energies, void* stream);
+/* Energy history: all energies so far (index 0 = MP2 guess); *count in/out. */
+GBX_API int gbx_cc_energies(gbx_cc_job* job, double* energies, int* count);
+GBX_API int gbx_cc_stats_get(const gbx_cc_job* job, gbx_cc_stats* out);
+/* Orbital irreps and energies in orbital order (nocc + nvir entries each). */
+GBX_API int gbx_cc_get_orbitals(const gbx_cc_job* job, int* irrep, double* eps);
+/* Dense amplitudes (t1: nocc x nvir, t2: nocc^2 x nvir^2, row-major);
+ * either may be NULL.  Waits for the stream. */
+GBX_API int gbx_cc_get_amplitudes(gbx_cc_job* job, double* t1, double* t2, void* stream);
+GBX_API int gbx_cc_destroy(gbx_cc_job* job);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBX_CC_H */

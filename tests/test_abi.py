@@ -14,7 +14,7 @@ def declared_symbols():
     for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
         text = open(h).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(gbx_\w+)\s*\(", text, flags=re.M):
+        for m in re.finditer(r"^\s*(?:GBX_API\s+)?(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(gbx_\w+)\s*\(", text, flags=re.M):
             names.add(m.group(1))
     return sorted(names)
 
