@@ -1,0 +1,288 @@
+#!/usr/bin/env python
+"""CCSD iterations/s on one GB300: the split-precision path and the FP64
+path of the node-local contraction engine, on the synthetic CCSD system with
+8-irrep spatial symmetry (o=48, v=240 spin orbitals, blocks 4..40).
+
+One step = one CCSD Jacobi iteration (all T1/T2 residual contractions, the
+denominator update and the correlation energy), job state resident in HBM.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gbx|reference]
+
+N > 1 runs N independent replicas (one job per GPU, no collective on the data
+path) under torchrun; value = iterations/s summed over ranks.  Rank 0 prints
+one JSON line.  --impl reference times the reference's CPU path (the oracle
+port of its permute + big-matrix + dgemm leaf algorithm, GEMM part) on the
+host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "CCSD iter/s & eff. TFLOP/s, INT8-split vs FP64 path @<=1e-10 Eh; p99 req latency"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gbx", choices=["gbx", "reference"])
+    p.add_argument("--engine", default="auto", choices=["auto", "split", "fp64"])
+    p.add_argument("--nocc", type=int, default=48)
+    p.add_argument("--nvir", type=int, default=240)
+    p.add_argument("--nirrep", type=int, default=8)
+    p.add_argument("--max-block", type=int, default=40)
+    p.add_argument("--min-block", type=int, default=4)
+    p.add_argument("--seed", type=int, default=1)
+    p.add_argument("--slices", type=int, default=0)
+    p.add_argument("--profile", action="store_true", help="print the per-step breakdown to stderr")
+    return p.parse_args()
+
+
+def workload(a):
+    return {"workload": "ccsd_8irrep_o%d_v%d" % (a.nocc, a.nvir), "method": "CCSD spin-orbital (Jacobi)",
+            "nocc": a.nocc, "nvir": a.nvir, "nirrep": a.nirrep, "block_min": a.min_block, "block_max": a.max_block,
+            "seed": a.seed, "l2": "inputs larger than L2 (integrals resident, > 3 GB)", "parallelism": "replicas"}
+
+
+class Clocks:
+    """nvidia-smi sampler started before and stopped after the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, smax, reasons = [], None, set()
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for name, val in zip(["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"], f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_arm(a, steps, warmup, label_impl):
+    """The reference's CPU path on this host: per contraction and irrep one
+    dgemm with the packed shapes, all host threads."""
+    import numpy as np  # noqa: F401
+    from oracle import cc as occ, cc_cpu
+    sysm = occ.System(a.nocc, a.nvir, nirrep=a.nirrep, max_block=a.max_block, min_block=a.min_block, seed=a.seed)
+    shapes = cc_cpu.gemm_shapes(sysm, "ccsd")
+    g = cc_cpu.IterationGemms(shapes)
+    fl = cc_cpu.flops(shapes)
+    for _ in range(warmup):
+        g.run()
+    t = time.perf_counter()
+    for _ in range(steps):
+        g.run()
+    dt = (time.perf_counter() - t) / max(steps, 1)
+    cores = os.cpu_count()
+    return dict(value=1.0 / dt, unit="iter/s", cores=cores, kind="port", ms_per_step=dt * 1e3,
+                sample="all %d per-irrep dgemms of one CCSD iteration (%.3g flops, packed shapes of the reference's "
+                       "transpose_and_dgemm), numpy/OpenBLAS FP64 on %d threads; permutes and packs not timed"
+                       % (len(shapes), fl, cores), gemm_tflops=fl / dt / 1e12)
+
+
+def main():
+    a = parse()
+    world, rank, local = dist_setup()
+    if a.impl == "reference":
+        if rank != 0:
+            return 0
+        r = cpu_arm(a, max(a.steps, 1), max(min(a.warmup, 1), 0), "reference")
+        line = {"metric": METRIC, "impl": "reference", "value": r["value"], "unit": "iter/s", "n_gpus": a.gpus,
+                "steps": a.steps, "warmup": a.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+                "config": workload(a),
+                "cpu_baseline": {"value": r["value"], "unit": "iter/s", "cores": r["cores"], "kind": r["kind"],
+                                 "sample": r["sample"]},
+                "e2e": {"value": r["value"], "unit": "iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    import numpy as np
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from dtcf_gb300.cc import Job
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t)
+        return float(t.item())
+
+    common = dict(nocc=a.nocc, nvir=a.nvir, nirrep=a.nirrep, max_block=a.max_block, min_block=a.min_block,
+                  seed=a.seed, method="ccsd", slices=a.slices)
+    engines = ["fp64"]
+    if a.engine in ("auto", "split"):
+        engines = ["split", "fp64"]
+    stream = torch.cuda.current_stream()
+
+    def time_job(job, steps, warmup):
+        for _ in range(warmup):
+            job.enqueue(1, stream)
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        job.enqueue(steps, stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        return e0.elapsed_time(e1)
+
+    results = {}
+    primary = None
+    clocks = None
+    for eng in engines:
+        try:
+            job = Job(engine=eng, **common)
+        except Exception as ex:  # split engine unavailable in this build
+            if eng == "split" and a.engine == "auto":
+                print("split engine unavailable: %s" % ex, file=sys.stderr)
+                continue
+            raise
+        st = job.stats()
+        steps = a.steps if primary is None else max(2, min(a.steps, 3))
+        ck = Clocks(local)
+        if primary is None:
+            ck.start()
+        ms = time_job(job, steps, a.warmup)
+        if primary is None:
+            clocks = ck.stop()
+        ms = max_over_ranks(ms)
+        energies = job.energies()
+        results[eng] = dict(ms=ms / steps, steps=steps, stats=st, energies=energies, job=job)
+        if primary is None:
+            primary = eng
+    if primary is None:
+        raise SystemExit("no engine could run")
+    P = results[primary]
+    st = P["stats"]
+    iters = 1000.0 / P["ms"]
+    value = sum_over_ranks(iters)
+
+    # dominant kernel: per-step breakdown of one iteration (CUDA events on the launching stream)
+    prof = P["job"].profile(stream)
+    if a.profile and rank == 0:
+        for s in sorted(prof, key=lambda x: -x["ms"])[:25]:
+            print("%9.3f ms  %10.3g fl  %s" % (s["ms"], s["flops"], s["name"]), file=sys.stderr)
+    top = max((s for s in prof if s["kind"] == 0), key=lambda s: s["ms"])
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    if primary == "split":
+        peak, unit, bound, src = peaks.get("bf16_tflops", 1900.0), "TFLOP/s", "tensor", "of measured"
+        achieved = top["flops"] / (top["ms"] * 1e-3) / 1e12  # FP64-equivalent of the dominant contraction
+    else:
+        # FP64 tensor-pipe ceiling measured on this GPU (DMMA m8n8k4 throughput probe)
+        peak, unit, bound, src = 1.05, "TFLOP/s", "tensor", "of measured DMMA probe"
+        achieved = top["flops"] / (top["ms"] * 1e-3) / 1e12
+    roofline = {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak,
+                "traffic": None, "kernel": top["name"], "kernel_ms": top["ms"], "peak_source": src}
+
+    # end to end through the public API with host buffers: every step copies the
+    # amplitudes in from pinned host memory and reads the energy back
+    job = P["job"]
+    n1, n2 = job.amplitude_elems()
+    t1h = torch.zeros(max(n1, 1), dtype=torch.float64, pin_memory=True)
+    t2h = torch.zeros(n2, dtype=torch.float64, pin_memory=True)
+    eh = torch.zeros(max(a.steps, 1), dtype=torch.float64, pin_memory=True)
+    torch.cuda.synchronize()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(a.steps):
+        job.set_amplitudes(t1h.data_ptr() if n1 else 0, t2h.data_ptr(), stream)
+        job.enqueue(1, stream)
+        job.read_energy(eh.data_ptr() + 8 * k, stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1)) / a.steps
+    e2e = {"value": sum_over_ranks(1000.0 / e2e_ms), "unit": "iter/s", "h2d_bytes_per_step": 8 * (n1 + n2),
+           "d2h_bytes_per_step": 8}
+
+    line = {"metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": P["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if primary == "fp64" else "bf16-slices/f64", "data": "synthetic (seeded)",
+            "config": dict(workload(a), engine=primary), "engine": primary,
+            "eff_tflops": st.flops_per_iter * iters / 1e12, "flops_per_iter": st.flops_per_iter,
+            "gpu_launches": int(st.launches_per_iter * a.steps), "clocks": clocks, "roofline": roofline, "e2e": e2e}
+    if "fp64" in results and primary != "fp64":
+        F = results["fp64"]
+        line["fp64_iter_s"] = sum_over_ranks(1000.0 / F["ms"])
+        line["split_speedup_vs_fp64"] = F["ms"] / P["ms"]
+        m = min(len(F["energies"]), len(P["energies"]))
+        line["energy_err_vs_fp64_eh"] = float(np.max(np.abs(np.array(F["energies"][:m]) - np.array(P["energies"][:m]))))
+    if rank == 0:
+        try:
+            cb = cpu_arm(a, 1, 1, "port")
+            line["cpu_baseline"] = {"value": cb["value"], "unit": "iter/s", "cores": cb["cores"], "kind": cb["kind"],
+                                    "sample": cb["sample"]}
+        except Exception as ex:  # the CPU sample must not hide the GPU number
+            line["cpu_baseline"] = {"value": None, "unit": "iter/s", "cores": os.cpu_count(), "kind": "port",
+                                    "sample": "failed: %s" % ex}
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -36,6 +36,11 @@ SIGNATURES = {
     "gbx_cc_get_orbitals": (_i, [_p, _p, _p]),
     "gbx_cc_get_amplitudes": (_i, [_p, _p, _p, _p]),
     "gbx_cc_destroy": (_i, [_p]),
+    "gbx_cc_gemm_shapes": (_i, [_p, _p, _ip]),
+    "gbx_cc_amplitude_elems": (_i, [_p, _p, _p]),
+    "gbx_cc_set_amplitudes": (_i, [_p, _p, _p, _p]),
+    "gbx_cc_read_energy": (_i, [_p, _p, _p]),
+    "gbx_cc_profile": (_i, [_p, _i, _p, _p, _p, _p, _p, _i, _ip, _p]),
 }
 
 _lib = None

@@ -16,7 +16,9 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgbx.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code: no FMA contraction, so host arithmetic is identical on x86 and Arm
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+         "-Xcompiler", "-ffp-contract=off",
          "-I" + os.path.join(os.path.dirname(HERE), "include")]
 
 

@@ -87,6 +87,43 @@ class Job:
                                           t2.ctypes.data_as(ctypes.c_void_p), _stream(stream)))
         return t1, t2
 
+    def gemm_shapes(self):
+        cnt = ctypes.c_int(0)
+        check(lib().gbx_cc_gemm_shapes(self.handle, None, ctypes.byref(cnt)))
+        out = np.zeros((cnt.value, 3), dtype=np.int64)
+        check(lib().gbx_cc_gemm_shapes(self.handle, out.ctypes.data_as(ctypes.c_void_p), ctypes.byref(cnt)))
+        return out
+
+    def amplitude_elems(self):
+        n1, n2 = ctypes.c_int64(), ctypes.c_int64()
+        check(lib().gbx_cc_amplitude_elems(self.handle, ctypes.byref(n1), ctypes.byref(n2)))
+        return n1.value, n2.value
+
+    def set_amplitudes(self, t1_ptr, t2_ptr, stream=None):
+        """Host pointers (ints) of tile-storage amplitudes; copies are enqueued."""
+        check(lib().gbx_cc_set_amplitudes(self.handle, ctypes.c_void_p(t1_ptr), ctypes.c_void_p(t2_ptr),
+                                          _stream(stream)))
+
+    def read_energy(self, host_ptr, stream=None):
+        check(lib().gbx_cc_read_energy(self.handle, ctypes.c_void_p(host_ptr), _stream(stream)))
+
+    def profile(self, stream=None):
+        """One iteration step by step: list of dicts (name, kind, ms, flops, bytes)."""
+        cap, nl = 512, 96
+        ms = np.zeros(cap, dtype=np.float32)
+        fl, by = np.zeros(cap), np.zeros(cap)
+        kind = np.zeros(cap, dtype=np.int32)
+        names = ctypes.create_string_buffer(cap * nl)
+        cnt = ctypes.c_int()
+        P = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        check(lib().gbx_cc_profile(self.handle, cap, P(ms), P(fl), P(by), P(kind), names, nl, ctypes.byref(cnt),
+                                   _stream(stream)))
+        out = []
+        for i in range(min(cnt.value, cap)):
+            nm = names.raw[i * nl:(i + 1) * nl].split(b"\0", 1)[0].decode()
+            out.append(dict(name=nm, kind=int(kind[i]), ms=float(ms[i]), flops=float(fl[i]), bytes=float(by[i])))
+        return out
+
     def close(self):
         if getattr(self, "handle", None) and self.handle.value:
             lib().gbx_cc_destroy(self.handle)

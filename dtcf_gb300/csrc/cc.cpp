@@ -84,6 +84,12 @@ struct gbx_cc_job {
   std::vector<std::unique_ptr<ContractionPlan>> cplans;
   std::vector<std::unique_ptr<SumPlan>> splans;
   std::vector<std::function<int(cudaStream_t)>> steps;  // one iteration
+  struct StepInfo {
+    std::string name;
+    int kind;  // 0 contraction, 1 sum, 2 zero, 3 denominator, 4 energy
+    double flops, bytes;
+  };
+  std::vector<StepInfo> info;
   std::vector<std::unique_ptr<CCTileSet>> tilesets;
   CCTileSet *den1 = nullptr, *den2 = nullptr;
   double* d_partial = nullptr;
@@ -160,6 +166,8 @@ struct gbx_cc_job {
     ContractionPlan* pp = p.get();
     double *dA = A->d, *dB = B->d, *dC = C->d;
     steps.push_back([=](cudaStream_t st) { return pp->execute(dA, dB, dC, alpha, st); });
+    info.push_back({std::string(c) + "[" + lc + "]+=" + a + "[" + la + "]*" + b + "[" + lb + "]", 0, pp->flops,
+                    8.0 * (double)(A->L.nelem + B->L.nelem + 2 * C->L.nelem)});
     launches += 4;
     cplans.push_back(std::move(p));
     return GBX_OK;
@@ -175,6 +183,8 @@ struct gbx_cc_job {
     SumPlan* pp = p.get();
     double *dA = A->d, *dC = C->d;
     steps.push_back([=](cudaStream_t st) { return pp->execute(dA, dC, 1.0, st); });
+    info.push_back({std::string(c) + "[" + lc + "]+=" + a + "[" + la + "]", 1, 0.0,
+                    8.0 * (double)(A->L.nelem + 2 * C->L.nelem)});
     launches += 1;
     splans.push_back(std::move(p));
     return GBX_OK;
@@ -188,6 +198,7 @@ struct gbx_cc_job {
       GBX_CUDA(cudaMemsetAsync(d, 0, bytes, st));
       return GBX_OK;
     });
+    info.push_back({std::string("zero ") + c, 2, 0.0, (double)bytes});
     launches += 1;
     return GBX_OK;
   }
@@ -220,6 +231,7 @@ struct gbx_cc_job {
     const double* din = get(in)->d;
     CCDeviceTables tb = tab;
     steps.push_back([=](cudaStream_t st) { return run_cc_tiles(*ts, CC_OP_DENOM, tb, din, dout, st); });
+    info.push_back({std::string(out) + "=" + in + "/D", 3, 0.0, 16.0 * (double)get(out)->L.nelem});
     launches += 1;
     return GBX_OK;
   }
@@ -233,6 +245,7 @@ struct gbx_cc_job {
     int* cnt = d_count;
     int np = npartial, cap = hist_cap;
     steps.push_back([=](cudaStream_t st) { return gbx::run_energy(V, tau, n, part, np, hist, cnt, cap, st); });
+    info.push_back({"energy", 4, 2.0 * (double)n, 16.0 * (double)n});
     launches += 2;
     return GBX_OK;
   }
@@ -310,12 +323,14 @@ int gbx_cc_job::build() {
     GBX_TRY(tau_steps());
     for (size_t i = first; i < steps.size(); ++i) GBX_TRY(steps[i](st0));
     steps.resize(first);
+    info.resize(first);
   }
   GBX_TRY(gbx::run_energy(get("OOVV")->d, get(TAU)->d, get("OOVV")->L.nelem, d_partial, npartial, d_hist, d_count,
                           hist_cap, st0));
   launches = 0;
 
   // ---- one iteration --------------------------------------------------------
+  if (sd) GBX_TRY(tau_steps());
   // F_ae, F_mi, F_me
   GBX_TRY(zero("Fae"));
   if (sd) GBX_TRY(contract("Fae", "ae", "t1", "mf", "OVVV", "mafe", 1.0));
@@ -627,6 +642,81 @@ int gbx_cc_get_amplitudes(gbx_cc_job* job, double* t1, double* t2, void* stream)
     if (job->cfg.method == GBX_CC_CCSD) GBX_TRY(dump("t1", t1, 2));
     else std::fill(t1, t1 + (int64_t)o * v, 0.0);
   }
+  return GBX_OK;
+}
+
+int gbx_cc_gemm_shapes(const gbx_cc_job* job, int64_t* mnk, int* count) {
+  if (!job || !count) return fail(GBX_EINVAL, "bad arguments");
+  int n = 0;
+  for (auto& p : job->cplans)
+    for (auto& g : p->groups) {
+      if (g.M == 0 || g.N == 0 || g.K == 0) continue;
+      if (mnk && n < *count) {
+        mnk[3 * n] = g.M;
+        mnk[3 * n + 1] = g.N;
+        mnk[3 * n + 2] = g.K;
+      }
+      ++n;
+    }
+  *count = n;
+  return GBX_OK;
+}
+
+int gbx_cc_amplitude_elems(const gbx_cc_job* job, int64_t* n1, int64_t* n2) {
+  if (!job) return fail(GBX_EINVAL, "null job");
+  auto& T = const_cast<gbx_cc_job*>(job)->T;
+  if (n1) *n1 = T.count("t1") ? T.at("t1")->L.nelem : 0;
+  if (n2) *n2 = T.at("t2")->L.nelem;
+  return GBX_OK;
+}
+
+int gbx_cc_set_amplitudes(gbx_cc_job* job, const double* t1, const double* t2, void* stream) {
+  if (!job) return fail(GBX_EINVAL, "null job");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (t2) GBX_CUDA(cudaMemcpyAsync(job->get("t2")->d, t2, sizeof(double) * job->get("t2")->L.nelem,
+                                   cudaMemcpyHostToDevice, st));
+  if (t1 && job->T.count("t1"))
+    GBX_CUDA(cudaMemcpyAsync(job->get("t1")->d, t1, sizeof(double) * job->get("t1")->L.nelem, cudaMemcpyHostToDevice,
+                             st));
+  return GBX_OK;
+}
+
+int gbx_cc_read_energy(gbx_cc_job* job, double* energy, void* stream) {
+  if (!job || !energy) return fail(GBX_EINVAL, "bad arguments");
+  int k = job->nenergies - 1;
+  if (k < 0 || k >= job->hist_cap) return fail(GBX_EUNSUPPORTED, "energy history full");
+  GBX_CUDA(cudaMemcpyAsync(energy, job->d_hist + k, sizeof(double), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  return GBX_OK;
+}
+
+int gbx_cc_profile(gbx_cc_job* job, int cap, float* ms, double* flops, double* bytes, int* kind, char* names,
+                   int name_len, int* count, void* stream) {
+  if (!job || !count) return fail(GBX_EINVAL, "bad arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  int n = (int)job->steps.size();
+  std::vector<cudaEvent_t> ev(n + 1);
+  for (auto& e : ev) GBX_CUDA(cudaEventCreate(&e));
+  GBX_CUDA(cudaEventRecord(ev[0], st));
+  for (int i = 0; i < n; ++i) {
+    GBX_TRY(job->steps[i](st));
+    GBX_CUDA(cudaEventRecord(ev[i + 1], st));
+  }
+  GBX_CUDA(cudaEventSynchronize(ev[n]));
+  job->nenergies += 1;
+  for (int i = 0; i < n && i < cap; ++i) {
+    float t = 0.f;
+    GBX_CUDA(cudaEventElapsedTime(&t, ev[i], ev[i + 1]));
+    if (ms) ms[i] = t;
+    if (flops) flops[i] = job->info[i].flops;
+    if (bytes) bytes[i] = job->info[i].bytes;
+    if (kind) kind[i] = job->info[i].kind;
+    if (names && name_len > 0) {
+      std::strncpy(names + (size_t)i * name_len, job->info[i].name.c_str(), name_len - 1);
+      names[(size_t)i * name_len + name_len - 1] = 0;
+    }
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  *count = n;
   return GBX_OK;
 }
 

@@ -102,14 +102,31 @@ struct GemmProblem {
   int m, n, k;
   double alpha;
   int accumulate;
+  // split-K (filled by F64Gemm::build)
+  int ksplit, kchunk, pad_;
+  double* partial;
 };
 
 // Grouped FP64 GEMM: C_p (+)= alpha_p * A_p * B_p^T for all problems in one
-// persistent launch.  d_problems is device memory.
-// d_ticket: a device int used as the work-queue counter (reset by the call),
-// or nullptr for a static round-robin schedule.
-int grouped_gemm_f64(const GemmProblem* d_problems, int nprob, int total_tiles, const int* d_tile_first,
-                     int* d_ticket, cudaStream_t st);
+// persistent launch (plus a fixed-order split-K reduction when needed).
+struct F64Gemm {
+  GemmProblem* d_probs = nullptr;
+  int* d_first = nullptr;
+  int* d_ticket = nullptr;
+  double* d_partial = nullptr;
+  int* d_red_prob = nullptr;
+  uint32_t* d_red_first = nullptr;
+  int nprob = 0, total_tiles = 0, nred = 0;
+  uint32_t red_chunks = 0;
+  double workspace_bytes = 0.0;
+  bool async_stream_set = false;
+  cudaStream_t async_stream = nullptr;
+  // async: allocate / upload stream-ordered on st (for one-shot leaf calls)
+  int build(const std::vector<GemmProblem>& probs, bool async = false, cudaStream_t st = nullptr);
+  int run(cudaStream_t st) const;
+  void release();
+  ~F64Gemm() { release(); }
+};
 // Tile decomposition shared by the host planner and the kernel.
 constexpr int kF64TileM = 64;
 constexpr int kF64TileN = 64;

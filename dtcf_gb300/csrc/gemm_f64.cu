@@ -1,12 +1,16 @@
 // Grouped FP64 GEMM on the FP64 tensor pipe (DMMA, mma.sync m8n8k4 f64).
 //
 // C_p (+)= alpha_p * A_p * B_p^T for every problem p of a launch.  One
-// persistent grid walks a device-side queue of 64x64 output tiles over all
-// problems (an atomic ticket per CTA), so a whole contraction -- every block
-// triple, every irrep -- is one launch.  Operands are read through generic
-// element strides, which covers the transposed forms of local_contraction.
+// persistent grid walks a device-side queue of work items (an atomic ticket
+// per CTA) over all problems, so a whole contraction -- every block triple,
+// every irrep -- is one launch.  A work item is a 64x64 output tile and, for
+// problems whose output is too small to fill the GPU, one K range of it
+// (split-K): those write raw partial sums to a workspace that a second
+// kernel reduces in a fixed order, so results are deterministic.  Operands
+// are read through generic element strides, which covers the transposed
+// forms of local_contraction.
 //
-// On GB300 the FP64 pipe runs near 1 TFLOP/s (DMMA and FFMA alike), so this
+// On GB300 the FP64 pipe runs near 1 TFLOP/s (DMMA and FFMA alike), so the
 // kernel is FP64-issue bound at any reasonable occupancy; the data path is
 // kept simple (register-staged shared-memory tiles, double buffered).
 #include <algorithm>
@@ -18,7 +22,11 @@ namespace gbx {
 namespace {
 constexpr int BM = kF64TileM, BN = kF64TileN, BK = 16;
 constexpr int kThreads = 128;
-constexpr int kPad = 1;  // pad rows to spread shared-memory banks
+constexpr int kPad = 1;               // pad rows to spread shared-memory banks
+constexpr int kFillTiles = 152 * 3;   // work items that keep every SM busy
+constexpr int kMinChunk = 256;        // smallest K range of a split
+constexpr int kRedThreads = 256;
+constexpr int kRedChunk = 2048;
 }  // namespace
 
 int f64_tiles(int m, int n) { return ((m + BM - 1) / BM) * ((n + BN - 1) / BN); }
@@ -32,8 +40,8 @@ __device__ __forceinline__ void dmma884(double (&c)[2], double a, double b) {
 __global__ void __launch_bounds__(kThreads) grouped_gemm_f64_kernel(const GemmProblem* __restrict__ probs, int nprob,
                                                                     const int* __restrict__ tile_first,
                                                                     int total_tiles, int* __restrict__ ticket) {
-  // ticket == nullptr: static round-robin over tiles; otherwise a device
-  // work queue (one atomic ticket per tile) balances uneven problem sizes.
+  // ticket == nullptr: static round-robin over work items; otherwise a device
+  // work queue (one atomic ticket per item) balances uneven problem sizes.
   __shared__ double As[2][BM][BK + kPad];
   __shared__ double Bs[2][BN][BK + kPad];
   __shared__ int s_tile;
@@ -55,9 +63,13 @@ __global__ void __launch_bounds__(kThreads) grouped_gemm_f64_kernel(const GemmPr
       if (tile_first[mid] <= tile) lo = mid; else hi = mid - 1;
     }
     const GemmProblem p = probs[lo];
-    const int local = tile - tile_first[lo];
-    const int ntn = (p.n + BN - 1) / BN;
+    int local = tile - tile_first[lo];
+    const int ntn = (p.n + BN - 1) / BN, ntm = (p.m + BM - 1) / BM;
+    const int kc = local / (ntm * ntn);
+    local -= kc * ntm * ntn;
     const int m0 = (local / ntn) * BM, n0 = (local % ntn) * BN;
+    const int kbeg = kc * p.kchunk;
+    const int kend = min(p.k, kbeg + p.kchunk);
 
     double acc[4][4][2];
 #pragma unroll
@@ -73,8 +85,8 @@ __global__ void __launch_bounds__(kThreads) grouped_gemm_f64_kernel(const GemmPr
         int e = tid + r * kThreads;  // 0..1023 over a 64 x 16 tile
         int row = e / BK, col = e % BK;
         int gm = m0 + row, gk = k0 + col, gn = n0 + row;
-        ra[r] = (gm < p.m && gk < p.k) ? __ldg(p.A + (int64_t)gm * p.a_rs + (int64_t)gk * p.a_cs) : 0.0;
-        rb[r] = (gn < p.n && gk < p.k) ? __ldg(p.B + (int64_t)gn * p.b_rs + (int64_t)gk * p.b_cs) : 0.0;
+        ra[r] = (gm < p.m && gk < kend) ? __ldg(p.A + (int64_t)gm * p.a_rs + (int64_t)gk * p.a_cs) : 0.0;
+        rb[r] = (gn < p.n && gk < kend) ? __ldg(p.B + (int64_t)gn * p.b_rs + (int64_t)gk * p.b_cs) : 0.0;
       }
     };
     auto store_regs = [&](int buf) {
@@ -87,15 +99,15 @@ __global__ void __launch_bounds__(kThreads) grouped_gemm_f64_kernel(const GemmPr
       }
     };
 
-    const int nk = (p.k + BK - 1) / BK;
+    const int nk = kend > kbeg ? (kend - kbeg + BK - 1) / BK : 0;
     if (nk > 0) {
-      load_regs(0);
+      load_regs(kbeg);
       store_regs(0);
     }
     __syncthreads();
     for (int kt = 0; kt < nk; ++kt) {
       const int buf = kt & 1;
-      if (kt + 1 < nk) load_regs((kt + 1) * BK);
+      if (kt + 1 < nk) load_regs(kbeg + (kt + 1) * BK);
 #pragma unroll
       for (int k4 = 0; k4 < BK; k4 += 4) {
         double af[4], bf[4];
@@ -112,7 +124,8 @@ __global__ void __launch_bounds__(kThreads) grouped_gemm_f64_kernel(const GemmPr
       __syncthreads();
     }
 
-    // epilogue: C (+)= alpha * acc
+    // epilogue: C (+)= alpha * acc, or the raw partial of this K range
+    double* part = p.partial ? p.partial + (int64_t)kc * p.m * p.n : nullptr;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int gm = m0 + wm * 32 + i * 8 + (lane >> 2);
@@ -123,22 +136,160 @@ __global__ void __launch_bounds__(kThreads) grouped_gemm_f64_kernel(const GemmPr
         for (int h = 0; h < 2; ++h) {
           const int gn = n0 + wn * 32 + j * 8 + (lane & 3) * 2 + h;
           if (gn >= p.n) continue;
-          double* c = p.C + (int64_t)gm * p.c_rs + gn;
-          double v = __dmul_rn(p.alpha, acc[i][j][h]);
-          *c = p.accumulate ? __dadd_rn(*c, v) : v;
+          if (part) {
+            part[(int64_t)gm * p.n + gn] = acc[i][j][h];
+          } else {
+            double* c = p.C + (int64_t)gm * p.c_rs + gn;
+            double v = __dmul_rn(p.alpha, acc[i][j][h]);
+            *c = p.accumulate ? __dadd_rn(*c, v) : v;
+          }
         }
       }
     }
   }
 }
 
-int grouped_gemm_f64(const GemmProblem* d_problems, int nprob, int total_tiles, const int* d_tile_first,
-                     int* d_ticket, cudaStream_t st) {
-  if (nprob <= 0 || total_tiles <= 0) return GBX_OK;
-  if (d_ticket) GBX_CUDA(cudaMemsetAsync(d_ticket, 0, sizeof(int), st));
+// Fixed-order reduction of split-K partials into C.
+__global__ void __launch_bounds__(kRedThreads) splitk_reduce_kernel(const GemmProblem* __restrict__ probs,
+                                                                    const int* __restrict__ red_prob,
+                                                                    const uint32_t* __restrict__ red_first, int nred,
+                                                                    uint32_t nchunks) {
+  for (uint32_t chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
+    int lo = 0, hi = nred - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (red_first[mid] <= chunk) lo = mid; else hi = mid - 1;
+    }
+    const GemmProblem& p = probs[red_prob[lo]];
+    const int64_t mn = (int64_t)p.m * p.n;
+    const int64_t base = (int64_t)(chunk - red_first[lo]) * kRedChunk;
+    for (int k = 0; k < kRedChunk / kRedThreads; ++k) {
+      int64_t e = base + k * kRedThreads + threadIdx.x;
+      if (e >= mn) break;
+      double s = 0.0;
+      for (int c = 0; c < p.ksplit; ++c) s = __dadd_rn(s, p.partial[(int64_t)c * mn + e]);
+      int64_t row = e / p.n, col = e - row * p.n;
+      double* cp = p.C + row * p.c_rs + col;
+      double v = __dmul_rn(p.alpha, s);
+      *cp = p.accumulate ? __dadd_rn(*cp, v) : v;
+    }
+  }
+}
+
+void F64Gemm::release() {
+  auto fr = [&](void* q) {
+    if (!q) return;
+    if (async_stream_set) cudaFreeAsync(q, async_stream); else cudaFree(q);
+  };
+  fr(d_probs);
+  fr(d_first);
+  fr(d_ticket);
+  fr(d_partial);
+  fr(d_red_prob);
+  fr(d_red_first);
+  d_probs = nullptr;
+  d_first = nullptr;
+  d_ticket = nullptr;
+  d_partial = nullptr;
+  d_red_prob = nullptr;
+  d_red_first = nullptr;
+  total_tiles = nprob = nred = 0;
+  red_chunks = 0;
+}
+
+int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t st) {
+  release();
+  async_stream_set = async;
+  async_stream = st;
+  std::vector<GemmProblem> probs;
+  for (const GemmProblem& q : in)
+    if (q.m > 0 && q.n > 0) probs.push_back(q);
+  nprob = (int)probs.size();
+  if (nprob == 0) return GBX_OK;
+  // total output tiles decide how much K splitting the small problems get
+  int64_t out_tiles = 0;
+  for (auto& q : probs) out_tiles += f64_tiles(q.m, q.n);
+  int64_t part_elems = 0;
+  std::vector<int> first(nprob);
+  std::vector<int> red;
+  std::vector<uint32_t> red_first;
+  int64_t tiles = 0;
+  uint64_t rc = 0;
+  for (int i = 0; i < nprob; ++i) {
+    GemmProblem& q = probs[i];
+    int t = f64_tiles(q.m, q.n);
+    int ks = 1;
+    if (out_tiles < kFillTiles && q.k > 2 * kMinChunk) {
+      int want = (int)((kFillTiles + out_tiles - 1) / out_tiles);
+      ks = std::max(1, std::min(want, (q.k + kMinChunk - 1) / kMinChunk));
+    }
+    int chunk = (q.k + ks - 1) / ks;
+    chunk = ((chunk + BK - 1) / BK) * BK;
+    ks = std::max(1, (q.k + chunk - 1) / chunk);
+    q.ksplit = ks;
+    q.kchunk = std::max(chunk, BK);
+    q.partial = nullptr;
+    q.pad_ = 0;
+    if (ks > 1) {
+      q.partial = (double*)(intptr_t)(part_elems + 1);  // offset + 1, patched below
+      part_elems += (int64_t)ks * q.m * q.n;
+      red.push_back(i);
+      red_first.push_back((uint32_t)rc);
+      rc += ((uint64_t)q.m * q.n + kRedChunk - 1) / kRedChunk;
+    }
+    first[i] = (int)tiles;
+    tiles += (int64_t)t * ks;
+  }
+  if (tiles >= (1ll << 31)) return fail(GBX_EUNSUPPORTED, "grouped GEMM has too many work items");
+  total_tiles = (int)tiles;
+  nred = (int)red.size();
+  red_chunks = (uint32_t)rc;
+  auto alloc = [&](void** q, size_t bytes) -> int {
+    if (bytes == 0) {
+      *q = nullptr;
+      return GBX_OK;
+    }
+    if (async) {
+      GBX_CUDA(cudaMallocAsync(q, bytes, st));
+      return GBX_OK;
+    }
+    return dev_alloc(q, bytes);
+  };
+  auto copy = [&](void* dst, const void* src, size_t bytes) -> int {
+    if (bytes == 0) return GBX_OK;
+    if (async) GBX_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+    else GBX_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+    return GBX_OK;
+  };
+  GBX_TRY(alloc((void**)&d_partial, sizeof(double) * part_elems));
+  for (auto& q : probs)
+    if (q.partial) q.partial = d_partial + ((intptr_t)q.partial - 1);
+  GBX_TRY(alloc((void**)&d_probs, sizeof(GemmProblem) * nprob));
+  GBX_TRY(alloc((void**)&d_first, sizeof(int) * nprob));
+  GBX_TRY(alloc((void**)&d_ticket, sizeof(int)));
+  GBX_TRY(copy(d_probs, probs.data(), sizeof(GemmProblem) * nprob));
+  GBX_TRY(copy(d_first, first.data(), sizeof(int) * nprob));
+  if (nred) {
+    GBX_TRY(alloc((void**)&d_red_prob, sizeof(int) * nred));
+    GBX_TRY(alloc((void**)&d_red_first, sizeof(uint32_t) * nred));
+    GBX_TRY(copy(d_red_prob, red.data(), sizeof(int) * nred));
+    GBX_TRY(copy(d_red_first, red_first.data(), sizeof(uint32_t) * nred));
+  }
+  workspace_bytes = (double)part_elems * 8.0;
+  return GBX_OK;
+}
+
+int F64Gemm::run(cudaStream_t st) const {
+  if (nprob == 0 || total_tiles == 0) return GBX_OK;
+  GBX_CUDA(cudaMemsetAsync(d_ticket, 0, sizeof(int), st));
   int grid = std::min(total_tiles, 152 * 4);
-  grouped_gemm_f64_kernel<<<grid, kThreads, 0, st>>>(d_problems, nprob, d_tile_first, total_tiles, d_ticket);
+  grouped_gemm_f64_kernel<<<grid, kThreads, 0, st>>>(d_probs, nprob, d_first, total_tiles, d_ticket);
   GBX_CUDA(cudaGetLastError());
+  if (nred) {
+    int rg = (int)std::min<uint32_t>(red_chunks, 152u * 8u);
+    splitk_reduce_kernel<<<rg, kRedThreads, 0, st>>>(d_probs, d_red_prob, d_red_first, nred, red_chunks);
+    GBX_CUDA(cudaGetLastError());
+  }
   return GBX_OK;
 }
 

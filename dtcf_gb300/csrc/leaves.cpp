@@ -275,6 +275,7 @@ int gbx_local_contraction(int n_a, int n_b, int n_k, const double* d_A, const do
   if (n_a < 0 || n_b < 0 || n_k < 0) return fail(GBX_EINVAL, "negative extent");
   if (n_a == 0 || n_b == 0) return GBX_OK;
   GemmProblem p;
+  std::memset(&p, 0, sizeof(p));
   p.A = d_A;
   p.B = d_B;
   p.C = d_C;
@@ -289,14 +290,9 @@ int gbx_local_contraction(int n_a, int n_b, int n_k, const double* d_A, const do
   p.alpha = alpha;
   p.accumulate = 1;
   cudaStream_t st = (cudaStream_t)stream;
-  int first = 0;
-  void *dp = nullptr, *df = nullptr;
-  GBX_TRY(upload_async(&p, sizeof(p), st, &dp));
-  GBX_TRY(upload_async(&first, sizeof(int), st, &df));
-  int rc = grouped_gemm_f64((const GemmProblem*)dp, 1, f64_tiles(n_a, n_b), (const int*)df, nullptr, st);
-  cudaFreeAsync(dp, st);
-  cudaFreeAsync(df, st);
-  return rc;
+  F64Gemm g;
+  GBX_TRY(g.build({p}, true, st));
+  return g.run(st);
 }
 
 int gbx_dltc_compute(double* d_c, const double* d_a, const double* d_b, int m, int n, int k, void* stream) {
@@ -322,26 +318,32 @@ int gbx_revert_big_matrix(int dims, const int* vgrid, const int* p_map, int num_
 }
 
 int gbx_grouped_gemm_f64(const gbx_triple* triples, int num_triples, void* stream) {
-  static_assert(sizeof(gbx_triple) == sizeof(GemmProblem), "gbx_triple and GemmProblem layouts differ");
   if (num_triples < 0) return fail(GBX_EINVAL, "num_triples < 0");
   if (num_triples == 0) return GBX_OK;
-  std::vector<int> first(num_triples);
-  int total = 0;
+  std::vector<GemmProblem> probs(num_triples);
   for (int i = 0; i < num_triples; ++i) {
-    if (triples[i].m < 0 || triples[i].n < 0 || triples[i].k < 0) return fail(GBX_EINVAL, "negative extent");
-    first[i] = total;
-    total += f64_tiles(triples[i].m, triples[i].n);
+    const gbx_triple& t = triples[i];
+    if (t.m < 0 || t.n < 0 || t.k < 0) return fail(GBX_EINVAL, "negative extent");
+    GemmProblem& p = probs[i];
+    std::memset(&p, 0, sizeof(p));
+    p.A = t.A;
+    p.B = t.B;
+    p.C = t.C;
+    p.a_rs = t.a_rs;
+    p.a_cs = t.a_cs;
+    p.b_rs = t.b_rs;
+    p.b_cs = t.b_cs;
+    p.c_rs = t.c_rs;
+    p.m = t.m;
+    p.n = t.n;
+    p.k = t.k;
+    p.alpha = t.alpha;
+    p.accumulate = t.accumulate;
   }
   cudaStream_t st = (cudaStream_t)stream;
-  void *dp = nullptr, *df = nullptr, *dt = nullptr;
-  GBX_TRY(upload_async(triples, sizeof(gbx_triple) * num_triples, st, &dp));
-  GBX_TRY(upload_async(first.data(), sizeof(int) * num_triples, st, &df));
-  GBX_CUDA(cudaMallocAsync(&dt, sizeof(int), st));
-  int rc = grouped_gemm_f64((const GemmProblem*)dp, num_triples, total, (const int*)df, (int*)dt, st);
-  cudaFreeAsync(dp, st);
-  cudaFreeAsync(df, st);
-  cudaFreeAsync(dt, st);
-  return rc;
+  F64Gemm g;
+  GBX_TRY(g.build(probs, true, st));
+  return g.run(st);
 }
 
 }  // extern "C"

@@ -240,9 +240,6 @@ void sub_strides(const std::vector<int64_t>& ext, int64_t base, std::vector<int6
 }  // namespace
 
 ContractionPlan::~ContractionPlan() {
-  dev_free(d_probs);
-  dev_free(d_tile_first);
-  dev_free(d_ticket);
   if (own_workspace) {
     dev_free(d_Abig);
     dev_free(d_Bbig);
@@ -445,13 +442,12 @@ int ContractionPlan::build(Engine e, int nslices) {
   GBX_TRY(dev_alloc((void**)&d_Cbig, sizeof(double) * c_elems));
   if (e == Engine::F64) {
     std::vector<GemmProblem> probs;
-    std::vector<int> first;
-    int total = 0;
     for (auto& g : groups) {
       if (g.M == 0 || g.N == 0 || g.K == 0) continue;
       if (g.M >= (1ll << 31) || g.N >= (1ll << 31) || g.K >= (1ll << 31))
         return fail(GBX_EUNSUPPORTED, "packed block too large");
       GemmProblem q;
+      std::memset(&q, 0, sizeof(q));
       q.A = d_Abig + g.a_off;
       q.B = d_Bbig + g.b_off;
       q.C = d_Cbig + g.c_off;
@@ -466,18 +462,8 @@ int ContractionPlan::build(Engine e, int nslices) {
       q.alpha = 1.0;
       q.accumulate = 0;
       probs.push_back(q);
-      first.push_back(total);
-      total += f64_tiles(q.m, q.n);
     }
-    nprob = (int)probs.size();
-    total_tiles = total;
-    if (nprob > 0) {
-      GBX_TRY(dev_alloc((void**)&d_probs, sizeof(GemmProblem) * nprob));
-      GBX_TRY(dev_alloc((void**)&d_tile_first, sizeof(int) * nprob));
-      GBX_TRY(dev_alloc((void**)&d_ticket, sizeof(int)));
-      GBX_CUDA(cudaMemcpy(d_probs, probs.data(), sizeof(GemmProblem) * nprob, cudaMemcpyHostToDevice));
-      GBX_CUDA(cudaMemcpy(d_tile_first, first.data(), sizeof(int) * nprob, cudaMemcpyHostToDevice));
-    }
+    GBX_TRY(f64.build(probs));
   } else {
     std::vector<SplitProblem> sp;
     for (auto& g : groups) {
@@ -497,7 +483,7 @@ int ContractionPlan::build(Engine e, int nslices) {
 }
 
 int ContractionPlan::execute(const double* dA, const double* dB, double* dC, double alpha, cudaStream_t st) {
-  if (nprob == 0 && !split) return GBX_OK;
+  if (f64.nprob == 0 && !split) return GBX_OK;
   bool skipA = a_static && a_ready;
   if (!skipA) {
     if (a_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Abig, 0, sizeof(double) * a_elems, st));
@@ -506,7 +492,7 @@ int ContractionPlan::execute(const double* dA, const double* dB, double* dC, dou
   if (b_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Bbig, 0, sizeof(double) * b_elems, st));
   GBX_TRY(run_moves(packB, dB, d_Bbig, st));
   if (engine == Engine::F64) {
-    GBX_TRY(grouped_gemm_f64(d_probs, nprob, total_tiles, d_tile_first, d_ticket, st));
+    GBX_TRY(f64.run(st));
   } else {
     GBX_TRY(run_split_plan(split, !skipA, st));
   }

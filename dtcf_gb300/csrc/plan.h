@@ -112,10 +112,7 @@ struct ContractionPlan {
   bool a_needs_zero = false, b_needs_zero = false;
   MoveSet packA, packB, unpackC;
   // F64 engine
-  GemmProblem* d_probs = nullptr;
-  int* d_tile_first = nullptr;
-  int* d_ticket = nullptr;
-  int nprob = 0, total_tiles = 0;
+  F64Gemm f64;
   // workspace
   double *d_Abig = nullptr, *d_Bbig = nullptr, *d_Cbig = nullptr;
   bool own_workspace = true;

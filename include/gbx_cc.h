@@ -65,6 +65,23 @@ GBX_API int gbx_cc_get_orbitals(const gbx_cc_job* job, int* irrep, double* eps);
 /* Dense amplitudes (t1: nocc x nvir, t2: nocc^2 x nvir^2, row-major);
  * either may be NULL.  Waits for the stream. */
 GBX_API int gbx_cc_get_amplitudes(gbx_cc_job* job, double* t1, double* t2, void* stream);
+/* Shapes (M, N, K triples) of every packed GEMM of one iteration; *count in
+ * = capacity of mnk (3 int64 per GEMM), out = number of GEMMs. */
+GBX_API int gbx_cc_gemm_shapes(const gbx_cc_job* job, int64_t* mnk, int* count);
+/* Element counts of the amplitude tensors in their tile storage. */
+GBX_API int gbx_cc_amplitude_elems(const gbx_cc_job* job, int64_t* n1, int64_t* n2);
+/* Enqueue host -> device copies of the amplitudes (tile storage order) on
+ * stream; the next iteration starts from them.  Pinned host memory keeps the
+ * copies asynchronous. */
+GBX_API int gbx_cc_set_amplitudes(gbx_cc_job* job, const double* t1, const double* t2, void* stream);
+/* Enqueue a device -> host copy of the latest energy on stream. */
+GBX_API int gbx_cc_read_energy(gbx_cc_job* job, double* energy, void* stream);
+/* Run one iteration step by step with CUDA events between the steps and
+ * report per step: time (ms), algorithmic flops, bytes, kind (0 contraction,
+ * 1 permuted sum, 2 zero, 3 denominator, 4 energy) and a name of name_len
+ * chars.  Counts as one iteration of the job. */
+GBX_API int gbx_cc_profile(gbx_cc_job* job, int cap, float* ms, double* flops, double* bytes, int* kind, char* names,
+                           int name_len, int* count, void* stream);
 GBX_API int gbx_cc_destroy(gbx_cc_job* job);
 
 #ifdef __cplusplus
