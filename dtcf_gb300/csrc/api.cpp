@@ -3,6 +3,7 @@
 #include <memory>
 
 #include "plan.h"
+#include "split.h"
 
 using namespace gbx;
 
@@ -62,6 +63,30 @@ int gbx_execute(gbx_plan* plan, const double* d_A, const double* d_B, double* d_
 }
 
 double gbx_plan_flops(const gbx_plan* plan) { return (plan && plan->p) ? plan->p->flops : 0.0; }
+
+int gbx_split_gemm(const double* d_A, const double* d_B, double* d_C, int64_t M, int64_t N, int64_t K, int slices,
+                   void* stream) {
+  if (M < 0 || N < 0 || K < 0) return fail(GBX_EINVAL, "negative extent");
+  if (M == 0 || N == 0) return GBX_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (K == 0) {
+    for (int64_t i = 0; i < M; ++i) GBX_CUDA(cudaMemsetAsync(d_C + i * N, 0, sizeof(double) * N, st));
+    return GBX_OK;
+  }
+  SplitPlan* sp = nullptr;
+  GBX_TRY(create_split_plan({SplitProblem{d_A, d_B, d_C, M, N, K}}, slices, &sp));
+  int rc = run_split_plan(sp, true, st);
+  if (rc == GBX_OK) {
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cuda_fail(e, "split gemm", __FILE__, __LINE__);
+  }
+  if (rc == GBX_OK) {
+    int err = split_plan_error(sp);
+    if (err != 0) rc = fail(GBX_ETIMEOUT, "split GEMM: a bounded device wait ran out (stage %d)", err);
+  }
+  destroy_split_plan(sp);
+  return rc;
+}
 
 int gbx_plan_destroy(gbx_plan* plan) {
   delete plan;

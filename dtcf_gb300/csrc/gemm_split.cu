@@ -1,13 +1,641 @@
-// Split-precision FP64 GEMM (placeholder until the tcgen05 engine lands).
+// Split-precision FP64 GEMM on the tcgen05 tensor cores.
+//
+// C = A * B^T with A (M x K) and B (N x K) row-major FP64.
+//
+// Split.  Row i of A is scaled by 2^-e_i, e_i the smallest exponent with
+// max_k |A_ik| < 2^e_i, and the scaled row is rounded to a fixed-point
+// integer X = round(A_ik 2^(F - e_i)), F = 7 + 8 (S - 1).  X is cut into S
+// balanced base-256 digits d_1..d_S (d_1 in [-128, 128], the rest in
+// [-128, 127]) so that A_ik ~ 2^e_i sum_s d_s 2^-(7 + 8 (s - 1)).  Every digit
+// is an integer that bf16 holds exactly.  The split is pure integer
+// arithmetic on the FP64 bit pattern (no FP64 instructions); subnormal
+// inputs count as zero.  B is split by rows the same way (exponents f_j).
+//
+// Products.  C_ij = 2^(e_i + f_j - 14) sum_l 2^(-8 l) X_l with
+// X_l = sum_{s + t - 2 = l} (D^A_s D^B_t^T)_ij, kept for levels l <= S - 1
+// (S (S + 1) / 2 slice products).  Each product runs on tcgen05.mma
+// (kind::f16, bf16 operands from TMA-loaded 128B-swizzled shared memory,
+// FP32 accumulator in TMEM).  |d_A d_B| <= 2^14, so a TMEM accumulation over
+// at most 1024 K-elements stays below 2^24 and is exact; the kernel drains
+// the accumulator after every such chunk into int32 registers (exact), folds
+// the int32 sums into an FP64 Horner accumulator at each level change
+// (acc = acc * 2^-8 + X, levels from S - 1 down to 0), and writes
+// 2^(e_i + f_j - 14) * acc.  Only the fold and the final scale are FP64.
+//
+// Kernel roles (one CTA per SM, persistent over 128 x BN output tiles of
+// all problems): warp 0 issues TMA loads into a ring of shared-memory stages,
+// warp 1 allocates TMEM and issues the MMAs (one elected lane), warps 2..5
+// drain the accumulators (each owns one 32-lane TMEM quarter, i.e. 32 rows).
+// Two TMEM accumulator buffers let the drain of one chunk overlap the MMAs of
+// the next.  Every mbarrier wait is bounded (about a second); on timeout the
+// kernel records an error, stops issuing work, waits (bounded) for its own
+// TMA copies and MMAs in flight, frees its TMEM and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+
 #include "split.h"
 
 namespace gbx {
-struct SplitPlan {};
-int create_split_plan(const std::vector<SplitProblem>&, int, SplitPlan** out) {
-  *out = nullptr;
-  return fail(GBX_EUNSUPPORTED, "split engine not built yet");
+
+namespace {
+
+constexpr int BM = 128;
+constexpr int BK = 64;             // bf16 elements per 128-byte swizzled row
+constexpr int kStages = 5;
+constexpr int kAcc = 2;            // TMEM accumulator buffers
+constexpr int kChunkKb = 16;       // k-blocks per exact FP32 chunk (16 * 64 = 1024)
+constexpr int kFoldChunks = 127;   // int32 drain sums fold into FP64 before overflow
+constexpr int kThreads = 192;
+constexpr long long kWaitCycles = 2000000000ll;  // ~1 s at 2 GHz
+
+struct SplitRowSet {   // one operand of one problem for the split kernel
+  const double* src;
+  int64_t rows, K;     // source rows (M or N) and row length
+  __nv_bfloat16* dst;  // slice 0, row 0
+  int64_t slice_stride, Kp;
+  int* exps;
+  int64_t first_row;   // prefix over all row sets
+};
+
+struct DevProblem {
+  int M, N, K, nkb;
+  int tiles_m, tiles_n;
+  const int* eA;
+  const int* eB;
+  double* C;
+  int64_t ldc;
+};
+
+struct GemmParams {
+  const DevProblem* probs;
+  const int* tile_first;
+  const CUtensorMap* maps;  // 2 per problem: A, B
+  int nprob, total_tiles, S, L;
+  int* err;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
 }
-int run_split_plan(SplitPlan*, bool, cudaStream_t) { return fail(GBX_EUNSUPPORTED, "split engine not built yet"); }
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait; false (and the error word set) when it ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+  if (mbar_try_wait(bar, parity)) return true;
+  long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (clock64() - t0 > kWaitCycles) {
+      atomicCAS(err, 0, code);
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], "
+      "[%2];" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms of
+// 1024 bytes stacked along M/N (stride byte offset 1024).
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)1 << 16;              // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;    // stride byte offset
+  d |= (uint64_t)1 << 46;              // descriptor version
+  d |= (uint64_t)2 << 61;              // 128-byte swizzle
+  return d;
+}
+
+template <int BN>
+__device__ __forceinline__ constexpr uint32_t idesc_bf16() {
+  return (1u << 4)                  // D: f32
+         | (1u << 7)                // A: bf16
+         | (1u << 10)               // B: bf16
+         | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Number of slice pairs (s, t), 1 <= s, t <= S, on level l = s + t - 2.
+__device__ __forceinline__ int level_pairs(int l, int S) {
+  int lo = max(1, l + 2 - S), hi = min(S, l + 1);
+  return hi >= lo ? hi - lo + 1 : 0;
+}
+
+template <int BN>
+struct Smem {
+  alignas(1024) __nv_bfloat16 a[kStages][BM * BK];
+  alignas(1024) __nv_bfloat16 b[kStages][BN * BK];
+  uint64_t full[kStages], empty[kStages], accfull[kAcc], accempty[kAcc], done;
+  uint32_t tmem_base;
+};
+
+template <int BN>
+__global__ void __launch_bounds__(kThreads, 1) split_gemm_kernel(const GemmParams P) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  Smem<BN>& sm = *reinterpret_cast<Smem<BN>*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr uint32_t kTxBytes = (BM + BN) * BK * 2;
+  constexpr uint32_t kTmemCols = (kAcc * BN < 32) ? 32 : kAcc * BN;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&sm.full[s], 1);
+      mbar_init(&sm.empty[s], 1);
+    }
+    for (int b = 0; b < kAcc; ++b) {
+      mbar_init(&sm.accfull[b], 1);
+      mbar_init(&sm.accempty[b], 4);
+    }
+    mbar_init(&sm.done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm.tmem_base)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = sm.tmem_base;
+  const int S = P.S, L = P.L;
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < P.total_tiles && ok; tile += gridDim.x) {
+        int p = 0;
+        while (p + 1 < P.nprob && P.tile_first[p + 1] <= tile) ++p;
+        const DevProblem& pr = P.probs[p];
+        const int local = tile - P.tile_first[p];
+        const int m0 = (local / pr.tiles_n) * BM, n0 = (local % pr.tiles_n) * BN;
+        const CUtensorMap* ma = P.maps + 2 * p;
+        const CUtensorMap* mb = P.maps + 2 * p + 1;
+        for (int l = L; l >= 0 && ok; --l)
+          for (int s = max(1, l + 2 - S); s <= min(S, l + 1) && ok; ++s) {
+            const int t = l + 2 - s;
+            for (int kb = 0; kb < pr.nkb; ++kb) {
+              if (!mbar_wait(&sm.empty[stage], phase ^ 1, P.err, 1)) {
+                ok = false;
+                break;
+              }
+              mbar_expect_tx(&sm.full[stage], kTxBytes);
+              tma_load_3d(sm.a[stage], ma, &sm.full[stage], kb * BK, m0, s - 1);
+              tma_load_3d(sm.b[stage], mb, &sm.full[stage], kb * BK, n0, t - 1);
+              if (++stage == kStages) {
+                stage = 0;
+                phase ^= 1;
+              }
+            }
+          }
+      }
+      // wait (bounded) for the copies this warp issued to land before leaving
+      for (int i = 0; i < kStages; ++i) {
+        if (--stage < 0) {
+          stage = kStages - 1;
+          phase ^= 1;
+        }
+        // stage was last filled with parity `phase`; completion flips it
+        long long t0 = clock64();
+        while (!mbar_try_wait(&sm.full[stage], phase) && !mbar_try_wait(&sm.empty[stage], phase)) {
+          if (clock64() - t0 > kWaitCycles) {
+            atomicCAS(P.err, 0, 5);
+            break;
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      int stage = 0, buf = 0;
+      uint32_t phase = 0, aphase = 0;
+      bool ok = true;
+      constexpr uint32_t idesc = idesc_bf16<BN>();
+      for (int tile = blockIdx.x; tile < P.total_tiles && ok; tile += gridDim.x) {
+        int p = 0;
+        while (p + 1 < P.nprob && P.tile_first[p + 1] <= tile) ++p;
+        const int nkb = P.probs[p].nkb;
+        for (int l = L; l >= 0 && ok; --l) {
+          const int items = level_pairs(l, S) * nkb;
+          int item = 0;
+          for (int s = max(1, l + 2 - S); s <= min(S, l + 1) && ok; ++s) {
+            for (int kb = 0; kb < nkb && ok; ++kb, ++item) {
+              const int in_chunk = item % kChunkKb;
+              if (in_chunk == 0 && !mbar_wait(&sm.accempty[buf], aphase ^ 1, P.err, 2)) {
+                ok = false;
+                break;
+              }
+              if (!mbar_wait(&sm.full[stage], phase, P.err, 3)) {
+                ok = false;
+                break;
+              }
+              tc_fence_after();
+              const uint32_t d = tmem + (uint32_t)(buf * BN);
+              const uint64_t a0 = sdesc(smem_u32(sm.a[stage]));
+              const uint64_t b0 = sdesc(smem_u32(sm.b[stage]));
+#pragma unroll
+              for (int k = 0; k < BK / 16; ++k)
+                umma(d, a0 + (uint64_t)(k * 2), b0 + (uint64_t)(k * 2), idesc, (in_chunk > 0 || k > 0) ? 1u : 0u);
+              umma_commit(&sm.empty[stage]);
+              if (++stage == kStages) {
+                stage = 0;
+                phase ^= 1;
+              }
+              if (in_chunk == kChunkKb - 1 || item == items - 1) {
+                umma_commit(&sm.accfull[buf]);
+                if (++buf == kAcc) {
+                  buf = 0;
+                  aphase ^= 1;
+                }
+              }
+            }
+          }
+        }
+      }
+      // all MMAs issued by this thread complete before TMEM is released
+      umma_commit(&sm.done);
+      mbar_wait(&sm.done, 0, P.err, 6);
+    }
+  } else {
+    // ---------------- drain / epilogue (warps 2..5) ----------------
+    const int quarter = warp & 3;
+    const int row_in_tile = quarter * 32 + lane;
+    const uint32_t lane_addr = (uint32_t)(quarter * 32) << 16;
+    int buf = 0;
+    uint32_t aphase = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < P.total_tiles && ok; tile += gridDim.x) {
+      int p = 0;
+      while (p + 1 < P.nprob && P.tile_first[p + 1] <= tile) ++p;
+      const DevProblem& pr = P.probs[p];
+      const int local = tile - P.tile_first[p];
+      const int m0 = (local / pr.tiles_n) * BM, n0 = (local % pr.tiles_n) * BN;
+      double acc[BN];
+      int32_t X[BN];
+#pragma unroll
+      for (int j = 0; j < BN; ++j) {
+        acc[j] = 0.0;
+        X[j] = 0;
+      }
+      for (int l = L; l >= 0 && ok; --l) {
+        if (l != L) {
+#pragma unroll
+          for (int j = 0; j < BN; ++j) acc[j] *= 0x1.0p-8;  // exact
+        }
+        const int items = level_pairs(l, S) * pr.nkb;
+        const int chunks = (items + kChunkKb - 1) / kChunkKb;
+        int since_fold = 0;
+        for (int c = 0; c < chunks; ++c) {
+          // one lane waits, the warp follows (tcgen05.ld must stay warp-uniform)
+          int w_ok = lane == 0 ? (int)mbar_wait(&sm.accfull[buf], aphase, P.err, 4) : 1;
+          w_ok = __shfl_sync(0xffffffffu, w_ok, 0);
+          if (!w_ok) {
+            ok = false;
+            break;
+          }
+          __syncwarp();
+          tc_fence_after();
+#pragma unroll
+          for (int j0 = 0; j0 < BN; j0 += 16) {
+            uint32_t r[16];
+            tmem_ld16(tmem + lane_addr + (uint32_t)(buf * BN + j0), r);
+            tmem_wait_ld();
+#pragma unroll
+            for (int q = 0; q < 16; ++q) X[j0 + q] += __float2int_rn(__uint_as_float(r[q]));
+          }
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&sm.accempty[buf]);
+          if (++buf == kAcc) {
+            buf = 0;
+            aphase ^= 1;
+          }
+          if (++since_fold == kFoldChunks || c == chunks - 1) {
+#pragma unroll
+            for (int j = 0; j < BN; ++j) {
+              acc[j] += (double)X[j];
+              X[j] = 0;
+            }
+            since_fold = 0;
+          }
+        }
+      }
+      if (!ok) break;
+      const int row = m0 + row_in_tile;
+      if (row < pr.M) {
+        const int ea = pr.eA[row];
+        double* crow = pr.C + (int64_t)row * pr.ldc;
+#pragma unroll
+        for (int j = 0; j < BN; ++j) {
+          const int col = n0 + j;
+          if (col < pr.N) {
+            int ex = ea + pr.eB[col] - 14 + 1023;
+            ex = ex < 1 ? 1 : (ex > 2046 ? 2046 : ex);
+            crow[col] = acc[j] * __longlong_as_double((long long)ex << 52);
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+  }
+}
+
+// FP64 rows -> S bf16 digit slices + row exponents (integer arithmetic only).
+__global__ void __launch_bounds__(256) split_rows_kernel(const SplitRowSet* __restrict__ sets, int nsets,
+                                                         int64_t total_rows, int S) {
+  const int64_t row_g = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row_g >= total_rows) return;
+  int lo = 0, hi = nsets - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (sets[mid].first_row <= row_g) lo = mid; else hi = mid - 1;
+  }
+  const SplitRowSet& rs = sets[lo];
+  const int64_t row = row_g - rs.first_row;
+  const double* src = rs.src + row * rs.K;
+  // row maximum of |x| as the largest biased exponent of a normal number
+  uint32_t emax = 0;
+  for (int64_t k = lane; k < rs.K; k += 32) {
+    uint32_t e = (uint32_t)((__double_as_longlong(__ldg(src + k)) >> 52) & 0x7FF);
+    emax = max(emax, e);
+  }
+  for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+  if (lane == 0) rs.exps[row] = emax == 0 ? 0 : (int)emax - 1022;
+  const int F = 7 + 8 * (S - 1);
+  __nv_bfloat16* dst = rs.dst + row * rs.Kp;
+  for (int64_t k = lane; k < rs.K; k += 32) {
+    const long long bits = __double_as_longlong(__ldg(src + k));
+    const uint32_t e = (uint32_t)((bits >> 52) & 0x7FF);
+    long long X = 0;
+    if (e != 0 && emax != 0) {
+      const long long mant = (bits & 0xFFFFFFFFFFFFFll) | (1ll << 52);
+      const int sh = 53 + (int)(emax - e) - F;  // X = mant * 2^-sh, rounded
+      if (sh <= 0) X = mant << (-sh);
+      else if (sh < 63) X = (mant + (1ll << (sh - 1))) >> sh;
+      if (bits < 0) X = -X;
+    }
+    // balanced base-256 digits, least significant first
+    for (int s = S - 1; s >= 1; --s) {
+      const long long d = ((X + 128) & 255) - 128;
+      X = (X - d) >> 8;
+      dst[s * rs.slice_stride + k] = __int2bfloat16_rn((int)d);
+    }
+    dst[k] = __int2bfloat16_rn((int)X);
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }
+  return fn;
+}
+
+int encode_slices(CUtensorMap* map, const __nv_bfloat16* base, int64_t S, int64_t rows_p, int64_t Kp, int box_rows) {
+  auto enc = get_encode();
+  if (!enc) return fail(GBX_ECUDA, "cuTensorMapEncodeTiled unavailable");
+  cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows_p, (cuuint64_t)S};
+  cuuint64_t strides[2] = {(cuuint64_t)(Kp * 2), (cuuint64_t)(rows_p * Kp * 2)};
+  cuuint32_t box[3] = {(cuuint32_t)BK, (cuuint32_t)box_rows, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, (void*)base, dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(GBX_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return GBX_OK;
+}
+
+}  // namespace
+
+constexpr int kBN = 64;
+
+struct SplitPlan {
+  int S = 0, L = 0;
+  std::vector<SplitProblem> host;
+  __nv_bfloat16* d_slices = nullptr;  // all A and B slices
+  int* d_exps = nullptr;
+  SplitRowSet* d_sets_a = nullptr;
+  SplitRowSet* d_sets_b = nullptr;
+  int nsets = 0;
+  int64_t rows_a = 0, rows_b = 0;
+  DevProblem* d_probs = nullptr;
+  int* d_tile_first = nullptr;
+  CUtensorMap* d_maps = nullptr;
+  int* d_err = nullptr;
+  int total_tiles = 0;
+  double bytes = 0.0;
+  ~SplitPlan() {
+    dev_free(d_slices);
+    dev_free(d_exps);
+    dev_free(d_sets_a);
+    dev_free(d_sets_b);
+    dev_free(d_probs);
+    dev_free(d_tile_first);
+    dev_free(d_maps);
+    dev_free(d_err);
+  }
+};
+
+int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitPlan** out) {
+  *out = nullptr;
+  auto sp = std::make_unique<SplitPlan>();
+  sp->S = slices > 0 ? slices : 6;
+  if (sp->S < 2 || sp->S > 7) return fail(GBX_EINVAL, "split slices must be in [2, 7]");
+  sp->L = sp->S - 1;
+  sp->host = probs;
+  const int S = sp->S;
+  int64_t slice_elems = 0, exp_elems = 0;
+  struct Off {
+    int64_t a, b, ea, eb, Mp, Np, Kp;
+  };
+  std::vector<Off> offs;
+  for (auto& p : probs) {
+    if (p.M <= 0 || p.N <= 0 || p.K <= 0) return fail(GBX_EINVAL, "empty split problem");
+    if (p.M >= (1ll << 30) || p.N >= (1ll << 30) || p.K >= (1ll << 30)) return fail(GBX_EUNSUPPORTED, "split problem too large");
+    Off o;
+    o.Mp = (p.M + BM - 1) / BM * BM;
+    o.Np = (p.N + kBN - 1) / kBN * kBN;
+    o.Kp = (p.K + BK - 1) / BK * BK;
+    o.a = slice_elems;
+    slice_elems += S * o.Mp * o.Kp;
+    o.b = slice_elems;
+    slice_elems += S * o.Np * o.Kp;
+    o.ea = exp_elems;
+    exp_elems += o.Mp;
+    o.eb = exp_elems;
+    exp_elems += o.Np;
+    offs.push_back(o);
+  }
+  GBX_TRY(dev_alloc((void**)&sp->d_slices, sizeof(__nv_bfloat16) * std::max<int64_t>(slice_elems, 1)));
+  GBX_TRY(dev_alloc((void**)&sp->d_exps, sizeof(int) * std::max<int64_t>(exp_elems, 1)));
+  GBX_CUDA(cudaMemset(sp->d_slices, 0, sizeof(__nv_bfloat16) * std::max<int64_t>(slice_elems, 1)));
+  GBX_CUDA(cudaMemset(sp->d_exps, 0, sizeof(int) * std::max<int64_t>(exp_elems, 1)));
+  sp->bytes = 2.0 * slice_elems + 4.0 * exp_elems;
+  std::vector<SplitRowSet> sa, sb;
+  std::vector<DevProblem> dp;
+  std::vector<int> first;
+  std::vector<CUtensorMap> maps;
+  int64_t ra = 0, rb = 0;
+  int tiles = 0;
+  for (size_t i = 0; i < probs.size(); ++i) {
+    const SplitProblem& p = probs[i];
+    const Off& o = offs[i];
+    SplitRowSet a{p.A, p.M, p.K, sp->d_slices + o.a, o.Mp * o.Kp, o.Kp, sp->d_exps + o.ea, ra};
+    SplitRowSet b{p.B, p.N, p.K, sp->d_slices + o.b, o.Np * o.Kp, o.Kp, sp->d_exps + o.eb, rb};
+    ra += p.M;
+    rb += p.N;
+    sa.push_back(a);
+    sb.push_back(b);
+    DevProblem d;
+    d.M = (int)p.M;
+    d.N = (int)p.N;
+    d.K = (int)p.K;
+    d.nkb = (int)(o.Kp / BK);
+    d.tiles_m = (int)(o.Mp / BM);
+    d.tiles_n = (int)(o.Np / kBN);
+    d.eA = sp->d_exps + o.ea;
+    d.eB = sp->d_exps + o.eb;
+    d.C = p.C;
+    d.ldc = p.N;
+    dp.push_back(d);
+    first.push_back(tiles);
+    tiles += d.tiles_m * d.tiles_n;
+    CUtensorMap ma, mb;
+    GBX_TRY(encode_slices(&ma, sp->d_slices + o.a, S, o.Mp, o.Kp, BM));
+    GBX_TRY(encode_slices(&mb, sp->d_slices + o.b, S, o.Np, o.Kp, kBN));
+    maps.push_back(ma);
+    maps.push_back(mb);
+  }
+  sp->nsets = (int)probs.size();
+  sp->rows_a = ra;
+  sp->rows_b = rb;
+  sp->total_tiles = tiles;
+  GBX_TRY(dev_alloc((void**)&sp->d_sets_a, sizeof(SplitRowSet) * sp->nsets));
+  GBX_TRY(dev_alloc((void**)&sp->d_sets_b, sizeof(SplitRowSet) * sp->nsets));
+  GBX_TRY(dev_alloc((void**)&sp->d_probs, sizeof(DevProblem) * sp->nsets));
+  GBX_TRY(dev_alloc((void**)&sp->d_tile_first, sizeof(int) * sp->nsets));
+  GBX_TRY(dev_alloc((void**)&sp->d_maps, sizeof(CUtensorMap) * maps.size()));
+  GBX_TRY(dev_alloc((void**)&sp->d_err, sizeof(int)));
+  GBX_CUDA(cudaMemcpy(sp->d_sets_a, sa.data(), sizeof(SplitRowSet) * sp->nsets, cudaMemcpyHostToDevice));
+  GBX_CUDA(cudaMemcpy(sp->d_sets_b, sb.data(), sizeof(SplitRowSet) * sp->nsets, cudaMemcpyHostToDevice));
+  GBX_CUDA(cudaMemcpy(sp->d_probs, dp.data(), sizeof(DevProblem) * sp->nsets, cudaMemcpyHostToDevice));
+  GBX_CUDA(cudaMemcpy(sp->d_tile_first, first.data(), sizeof(int) * sp->nsets, cudaMemcpyHostToDevice));
+  GBX_CUDA(cudaMemcpy(sp->d_maps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice));
+  GBX_CUDA(cudaMemset(sp->d_err, 0, sizeof(int)));
+  size_t smem = sizeof(Smem<kBN>) + 1024;
+  GBX_CUDA(cudaFuncSetAttribute(split_gemm_kernel<kBN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  *out = sp.release();
+  return GBX_OK;
+}
+
+int run_split_plan(SplitPlan* sp, bool split_a, cudaStream_t st) {
+  if (!sp || sp->nsets == 0) return GBX_OK;
+  if (split_a && sp->rows_a > 0) {
+    split_rows_kernel<<<(unsigned)((sp->rows_a + 7) / 8), 256, 0, st>>>(sp->d_sets_a, sp->nsets, sp->rows_a, sp->S);
+    GBX_CUDA(cudaGetLastError());
+  }
+  if (sp->rows_b > 0) {
+    split_rows_kernel<<<(unsigned)((sp->rows_b + 7) / 8), 256, 0, st>>>(sp->d_sets_b, sp->nsets, sp->rows_b, sp->S);
+    GBX_CUDA(cudaGetLastError());
+  }
+  if (sp->total_tiles == 0) return GBX_OK;
+  GemmParams P;
+  P.probs = sp->d_probs;
+  P.tile_first = sp->d_tile_first;
+  P.maps = sp->d_maps;
+  P.nprob = sp->nsets;
+  P.total_tiles = sp->total_tiles;
+  P.S = sp->S;
+  P.L = sp->L;
+  P.err = sp->d_err;
+  int dev = 0, nsm = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  int grid = std::min(sp->total_tiles, nsm);
+  size_t smem = sizeof(Smem<kBN>) + 1024;
+  split_gemm_kernel<kBN><<<grid, kThreads, smem, st>>>(P);
+  GBX_CUDA(cudaGetLastError());
+  return GBX_OK;
+}
+
+int split_plan_error(SplitPlan* sp) {
+  if (!sp) return 0;
+  int e = 0;
+  if (cudaMemcpy(&e, sp->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  return e;
+}
+
 void destroy_split_plan(SplitPlan* sp) { delete sp; }
-double split_plan_bytes(const SplitPlan*) { return 0.0; }
+
+double split_plan_bytes(const SplitPlan* sp) { return sp ? sp->bytes : 0.0; }
+
 }  // namespace gbx

@@ -24,5 +24,7 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
 int run_split_plan(SplitPlan* sp, bool split_a, cudaStream_t st);
 void destroy_split_plan(SplitPlan* sp);
 double split_plan_bytes(const SplitPlan* sp);
+// Error word of the GEMM kernel (0 = ok, else the wait that ran out); syncs.
+int split_plan_error(SplitPlan* sp);
 
 }  // namespace gbx

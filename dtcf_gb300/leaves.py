@@ -102,3 +102,11 @@ def grouped_gemm_f64(triples, stream=None):
     """All triples (Triple structs with device pointers) in one persistent launch."""
     arr = (Triple * len(triples))(*triples)
     check(lib().gbx_grouped_gemm_f64(ctypes.cast(arr, ctypes.c_void_p), len(triples), _stream(stream)))
+
+
+def split_gemm(A, B, C, slices=0, stream=None):
+    """C = A B^T (row-major FP64) on the split-precision tcgen05 engine."""
+    M, K = A.shape
+    N = B.shape[0]
+    check(lib().gbx_split_gemm(_ptr(A), _ptr(B), _ptr(C), M, N, K, slices, _stream(stream)))
+    return C

@@ -140,6 +140,17 @@ GBX_API int gbx_execute(gbx_plan* plan, const double* d_A, const double* d_B, do
 GBX_API double gbx_plan_flops(const gbx_plan* plan);
 GBX_API int gbx_plan_destroy(gbx_plan* plan);
 
+/* C[M x N] = A[M x K] * B[N x K]^T, row-major FP64, computed with the
+ * split-precision engine: each operand row is split into `slices` exact
+ * integer bf16 slices (0 = default 6; 2..7), the slice products run on the
+ * tcgen05 tensor cores with exact FP32 accumulation chunks and are recombined
+ * in FP64.  Relative error about 2^(-8*slices+1) of the row/column scale.
+ * Allocates its workspace and waits for the stream (a one-shot call; plans
+ * keep the workspace).  The FP64-emulating counterpart of local_contraction
+ * (localcontract.cc:3-20) with at=0, bt=1, alpha=1, beta=0. */
+GBX_API int gbx_split_gemm(const double* d_A, const double* d_B, double* d_C, int64_t M, int64_t N, int64_t K,
+                           int slices, void* stream);
+
 /* ---- grouped block GEMM ------------------------------------------------- */
 
 /* One block triple: C[m x n] (+)= alpha * A[m x k] * B[n x k]^T with element
