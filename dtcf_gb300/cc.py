@@ -14,7 +14,8 @@ class Config(ctypes.Structure):
     """gbx_cc_config."""
     _fields_ = [("nocc", ctypes.c_int), ("nvir", ctypes.c_int), ("nirrep", ctypes.c_int), ("max_block", ctypes.c_int),
                 ("min_block", ctypes.c_int), ("method", ctypes.c_int), ("engine", ctypes.c_int),
-                ("slices", ctypes.c_int), ("use_graph", ctypes.c_int), ("seed", ctypes.c_uint64),
+                ("slices", ctypes.c_int), ("use_graph", ctypes.c_int), ("split_all", ctypes.c_int),
+                ("seed", ctypes.c_uint64),
                 ("eps_occ_lo", ctypes.c_double), ("eps_occ_hi", ctypes.c_double), ("eps_vir_lo", ctypes.c_double),
                 ("eps_vir_hi", ctypes.c_double), ("v_scale", ctypes.c_double), ("v_decay", ctypes.c_double)]
 
@@ -113,16 +114,27 @@ class Job:
         ms = np.zeros(cap, dtype=np.float32)
         fl, by = np.zeros(cap), np.zeros(cap)
         kind = np.zeros(cap, dtype=np.int32)
+        plan = np.zeros(cap, dtype=np.int32)
         names = ctypes.create_string_buffer(cap * nl)
         cnt = ctypes.c_int()
         P = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
-        check(lib().gbx_cc_profile(self.handle, cap, P(ms), P(fl), P(by), P(kind), names, nl, ctypes.byref(cnt),
-                                   _stream(stream)))
+        check(lib().gbx_cc_profile(self.handle, cap, P(ms), P(fl), P(by), P(kind), P(plan), names, nl,
+                                   ctypes.byref(cnt), _stream(stream)))
         out = []
         for i in range(min(cnt.value, cap)):
             nm = names.raw[i * nl:(i + 1) * nl].split(b"\0", 1)[0].decode()
-            out.append(dict(name=nm, kind=int(kind[i]), ms=float(ms[i]), flops=float(fl[i]), bytes=float(by[i])))
+            out.append(dict(name=nm, kind=int(kind[i]), ms=float(ms[i]), flops=float(fl[i]), bytes=float(by[i]),
+                            plan=int(plan[i])))
         return out
+
+    def time_gemm(self, contraction, reps=5, stream=None):
+        """GEMM launches of one contraction alone: dict(ms, fp64_flops, tensor_flops, engine)."""
+        ms = ctypes.c_float()
+        f64, ten = ctypes.c_double(), ctypes.c_double()
+        eng = ctypes.c_int()
+        check(lib().gbx_cc_time_gemm(self.handle, contraction, reps, ctypes.byref(ms), ctypes.byref(f64),
+                                     ctypes.byref(ten), ctypes.byref(eng), _stream(stream)))
+        return dict(ms=ms.value, fp64_flops=f64.value, tensor_flops=ten.value, engine=eng.value)
 
     def close(self):
         if getattr(self, "handle", None) and self.handle.value:

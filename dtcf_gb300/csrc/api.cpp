@@ -75,7 +75,7 @@ int gbx_split_gemm(const double* d_A, const double* d_B, double* d_C, int64_t M,
   }
   SplitPlan* sp = nullptr;
   GBX_TRY(create_split_plan({SplitProblem{d_A, d_B, d_C, M, N, K}}, slices, &sp));
-  int rc = run_split_plan(sp, true, st);
+  int rc = run_split_plan(sp, true, true, st);
   if (rc == GBX_OK) {
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) rc = cuda_fail(e, "split gemm", __FILE__, __LINE__);

@@ -88,6 +88,7 @@ struct gbx_cc_job {
     std::string name;
     int kind;  // 0 contraction, 1 sum, 2 zero, 3 denominator, 4 energy
     double flops, bytes;
+    int plan = -1;  // index into cplans for contractions
   };
   std::vector<StepInfo> info;
   std::vector<std::unique_ptr<CCTileSet>> tilesets;
@@ -151,23 +152,35 @@ struct gbx_cc_job {
   }
 
   // C[lc] += alpha * A[la] * B[lb]
+  static bool is_integral(const char* name) {
+    size_t n = std::strlen(name);
+    if (n != 2 && n != 4) return false;
+    for (size_t i = 0; i < n; ++i)
+      if (name[i] != 'O' && name[i] != 'V') return false;
+    return true;
+  }
+
   int contract(const char* c, const char* lc, const char* a, const char* la, const char* b, const char* lb,
-               double alpha, bool a_static = false) {
+               double alpha) {
     CCTensor *C = get(c), *A = get(a), *B = get(b);
     GBX_TRY(check_labels(C, lc, c));
     GBX_TRY(check_labels(A, la, a));
     GBX_TRY(check_labels(B, lb, b));
     std::unique_ptr<ContractionPlan> p;
     Engine e = cfg.engine == GBX_MODE_SPLIT ? Engine::Split : Engine::F64;
-    GBX_TRY(plan_contraction(A->L, B->L, C->L, labels(la), labels(lb), labels(lc), e, cfg.slices, p));
-    p->a_static = a_static;
+    GBX_TRY(plan_contraction(A->L, B->L, C->L, labels(la), labels(lb), labels(lc), e, cfg.slices, p,
+                             cfg.split_all != 0));
+    // integrals never change: pack and split them once, here
+    p->a_static = is_integral(a);
+    p->b_static = is_integral(b);
+    if (p->a_static || p->b_static) GBX_TRY(p->prepare_static(A->d, B->d, 0));
     flops += p->flops;
     gemm_flops += p->gemm_flops;
     ContractionPlan* pp = p.get();
     double *dA = A->d, *dB = B->d, *dC = C->d;
     steps.push_back([=](cudaStream_t st) { return pp->execute(dA, dB, dC, alpha, st); });
     info.push_back({std::string(c) + "[" + lc + "]+=" + a + "[" + la + "]*" + b + "[" + lb + "]", 0, pp->flops,
-                    8.0 * (double)(A->L.nelem + B->L.nelem + 2 * C->L.nelem)});
+                    8.0 * (double)(A->L.nelem + B->L.nelem + 2 * C->L.nelem), (int)cplans.size()});
     launches += 4;
     cplans.push_back(std::move(p));
     return GBX_OK;
@@ -401,7 +414,7 @@ int gbx_cc_job::build() {
   // 1/2 tau_mn^ab W_mnij
   GBX_TRY(contract("R2", "ijab", TAU, "mnab", "Wmnij", "mnij", 0.5));
   // 1/2 tau_ij^ef <ab||ef>: the ladder, integrals as the (static) A operand
-  GBX_TRY(contract("R2", "ijab", "VVVV", "abef", TAU, "ijef", 0.5, true));
+  GBX_TRY(contract("R2", "ijab", "VVVV", "abef", TAU, "ijef", 0.5));
   if (sd) {
     // -1/2 P(ab) t_m^b sum_ef tau_ij^ef <am||ef> = +1/2 P(ab) sum_m t_m^b Z'_ijma
     GBX_TRY(zero("Zp"));
@@ -556,6 +569,10 @@ int gbx_cc_enqueue(gbx_cc_job* job, int niter, void* stream) {
 int gbx_cc_iterate(gbx_cc_job* job, int niter, double* energies, void* stream) {
   GBX_TRY(gbx_cc_enqueue(job, niter, stream));
   GBX_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  for (auto& p : job->cplans) {
+    int err = split_plan_error(p->split);
+    if (err != 0) return fail(GBX_ETIMEOUT, "split GEMM: a bounded device wait ran out (stage %d)", err);
+  }
   if (energies && niter > 0) {
     int first = job->nenergies - niter;
     if (first + niter > job->hist_cap) return fail(GBX_EUNSUPPORTED, "energy history full");
@@ -689,8 +706,8 @@ int gbx_cc_read_energy(gbx_cc_job* job, double* energy, void* stream) {
   return GBX_OK;
 }
 
-int gbx_cc_profile(gbx_cc_job* job, int cap, float* ms, double* flops, double* bytes, int* kind, char* names,
-                   int name_len, int* count, void* stream) {
+int gbx_cc_profile(gbx_cc_job* job, int cap, float* ms, double* flops, double* bytes, int* kind, int* plan,
+                   char* names, int name_len, int* count, void* stream) {
   if (!job || !count) return fail(GBX_EINVAL, "bad arguments");
   cudaStream_t st = (cudaStream_t)stream;
   int n = (int)job->steps.size();
@@ -710,6 +727,7 @@ int gbx_cc_profile(gbx_cc_job* job, int cap, float* ms, double* flops, double* b
     if (flops) flops[i] = job->info[i].flops;
     if (bytes) bytes[i] = job->info[i].bytes;
     if (kind) kind[i] = job->info[i].kind;
+    if (plan) plan[i] = job->info[i].plan;
     if (names && name_len > 0) {
       std::strncpy(names + (size_t)i * name_len, job->info[i].name.c_str(), name_len - 1);
       names[(size_t)i * name_len + name_len - 1] = 0;
@@ -717,6 +735,34 @@ int gbx_cc_profile(gbx_cc_job* job, int cap, float* ms, double* flops, double* b
   }
   for (auto& e : ev) cudaEventDestroy(e);
   *count = n;
+  return GBX_OK;
+}
+
+int gbx_cc_time_gemm(gbx_cc_job* job, int contraction, int reps, float* ms, double* fp64_flops,
+                     double* tensor_flops, int* engine, void* stream) {
+  if (!job || contraction < 0 || contraction >= (int)job->cplans.size() || reps < 1)
+    return fail(GBX_EINVAL, "bad arguments");
+  ContractionPlan* p = job->cplans[contraction].get();
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t e0, e1;
+  GBX_CUDA(cudaEventCreate(&e0));
+  GBX_CUDA(cudaEventCreate(&e1));
+  // operands are already packed and split by the last iteration: time only the GEMM launches
+  GBX_CUDA(cudaEventRecord(e0, st));
+  for (int r = 0; r < reps; ++r) {
+    if (p->split) GBX_TRY(run_split_plan(p->split, false, false, st));
+    GBX_TRY(p->f64.run(st));
+  }
+  GBX_CUDA(cudaEventRecord(e1, st));
+  GBX_CUDA(cudaEventSynchronize(e1));
+  float t = 0.f;
+  GBX_CUDA(cudaEventElapsedTime(&t, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (ms) *ms = t / reps;
+  if (fp64_flops) *fp64_flops = p->gemm_flops;
+  if (tensor_flops) *tensor_flops = split_plan_tensor_flops(p->split);
+  if (engine) *engine = p->split ? (p->f64.nprob ? 2 : 1) : 0;
   return GBX_OK;
 }
 

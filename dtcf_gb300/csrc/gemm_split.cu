@@ -52,6 +52,7 @@ constexpr int kChunkKb = 16;       // k-blocks per exact FP32 chunk (16 * 64 = 1
 constexpr int kFoldChunks = 127;   // int32 drain sums fold into FP64 before overflow
 constexpr int kThreads = 192;
 constexpr long long kWaitCycles = 2000000000ll;  // ~1 s at 2 GHz
+constexpr int kSplitFill = 152 * 2;  // work items that keep every SM busy
 
 struct SplitRowSet {   // one operand of one problem for the split kernel
   const double* src;
@@ -65,9 +66,11 @@ struct SplitRowSet {   // one operand of one problem for the split kernel
 struct DevProblem {
   int M, N, K, nkb;
   int tiles_m, tiles_n;
+  int ksplit, kb_per_split;  // K split into ranges of kb_per_split k-blocks
   const int* eA;
   const int* eB;
-  double* C;
+  double* C;        // ksplit == 1: output
+  double* partial;  // ksplit > 1: ksplit x M x N raw contributions
   int64_t ldc;
 };
 
@@ -168,6 +171,28 @@ __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
+struct TileInfo {
+  int p, m0, n0, kb0, nkb, kc;
+};
+
+template <int BN>
+__device__ __forceinline__ TileInfo decode_tile(const GemmParams& P, int tile) {
+  TileInfo t;
+  int p = 0;
+  while (p + 1 < P.nprob && P.tile_first[p + 1] <= tile) ++p;
+  const DevProblem& pr = P.probs[p];
+  int local = tile - P.tile_first[p];
+  const int per_k = pr.tiles_m * pr.tiles_n;
+  t.kc = local / per_k;
+  local -= t.kc * per_k;
+  t.p = p;
+  t.m0 = (local / pr.tiles_n) * BM;
+  t.n0 = (local % pr.tiles_n) * BN;
+  t.kb0 = t.kc * pr.kb_per_split;
+  t.nkb = min(pr.nkb, t.kb0 + pr.kb_per_split) - t.kb0;
+  return t;
+}
+
 // Number of slice pairs (s, t), 1 <= s, t <= S, on level l = s + t - 2.
 __device__ __forceinline__ int level_pairs(int l, int S) {
   int lo = max(1, l + 2 - S), hi = min(S, l + 1);
@@ -220,17 +245,14 @@ __global__ void __launch_bounds__(kThreads, 1) split_gemm_kernel(const GemmParam
       uint32_t phase = 0;
       bool ok = true;
       for (int tile = blockIdx.x; tile < P.total_tiles && ok; tile += gridDim.x) {
-        int p = 0;
-        while (p + 1 < P.nprob && P.tile_first[p + 1] <= tile) ++p;
-        const DevProblem& pr = P.probs[p];
-        const int local = tile - P.tile_first[p];
-        const int m0 = (local / pr.tiles_n) * BM, n0 = (local % pr.tiles_n) * BN;
-        const CUtensorMap* ma = P.maps + 2 * p;
-        const CUtensorMap* mb = P.maps + 2 * p + 1;
+        const TileInfo ti = decode_tile<BN>(P, tile);
+        const int m0 = ti.m0, n0 = ti.n0;
+        const CUtensorMap* ma = P.maps + 2 * ti.p;
+        const CUtensorMap* mb = P.maps + 2 * ti.p + 1;
         for (int l = L; l >= 0 && ok; --l)
           for (int s = max(1, l + 2 - S); s <= min(S, l + 1) && ok; ++s) {
             const int t = l + 2 - s;
-            for (int kb = 0; kb < pr.nkb; ++kb) {
+            for (int kb = ti.kb0; kb < ti.kb0 + ti.nkb; ++kb) {
               if (!mbar_wait(&sm.empty[stage], phase ^ 1, P.err, 1)) {
                 ok = false;
                 break;
@@ -269,9 +291,7 @@ __global__ void __launch_bounds__(kThreads, 1) split_gemm_kernel(const GemmParam
       bool ok = true;
       constexpr uint32_t idesc = idesc_bf16<BN>();
       for (int tile = blockIdx.x; tile < P.total_tiles && ok; tile += gridDim.x) {
-        int p = 0;
-        while (p + 1 < P.nprob && P.tile_first[p + 1] <= tile) ++p;
-        const int nkb = P.probs[p].nkb;
+        const int nkb = decode_tile<BN>(P, tile).nkb;
         for (int l = L; l >= 0 && ok; --l) {
           const int items = level_pairs(l, S) * nkb;
           int item = 0;
@@ -322,11 +342,9 @@ __global__ void __launch_bounds__(kThreads, 1) split_gemm_kernel(const GemmParam
     uint32_t aphase = 0;
     bool ok = true;
     for (int tile = blockIdx.x; tile < P.total_tiles && ok; tile += gridDim.x) {
-      int p = 0;
-      while (p + 1 < P.nprob && P.tile_first[p + 1] <= tile) ++p;
-      const DevProblem& pr = P.probs[p];
-      const int local = tile - P.tile_first[p];
-      const int m0 = (local / pr.tiles_n) * BM, n0 = (local % pr.tiles_n) * BN;
+      const TileInfo ti = decode_tile<BN>(P, tile);
+      const DevProblem& pr = P.probs[ti.p];
+      const int m0 = ti.m0, n0 = ti.n0;
       double acc[BN];
       int32_t X[BN];
 #pragma unroll
@@ -339,7 +357,7 @@ __global__ void __launch_bounds__(kThreads, 1) split_gemm_kernel(const GemmParam
 #pragma unroll
           for (int j = 0; j < BN; ++j) acc[j] *= 0x1.0p-8;  // exact
         }
-        const int items = level_pairs(l, S) * pr.nkb;
+        const int items = level_pairs(l, S) * ti.nkb;
         const int chunks = (items + kChunkKb - 1) / kChunkKb;
         int since_fold = 0;
         for (int c = 0; c < chunks; ++c) {
@@ -381,7 +399,7 @@ __global__ void __launch_bounds__(kThreads, 1) split_gemm_kernel(const GemmParam
       const int row = m0 + row_in_tile;
       if (row < pr.M) {
         const int ea = pr.eA[row];
-        double* crow = pr.C + (int64_t)row * pr.ldc;
+        double* crow = pr.ksplit > 1 ? pr.partial + ((int64_t)ti.kc * pr.M + row) * pr.N : pr.C + (int64_t)row * pr.ldc;
 #pragma unroll
         for (int j = 0; j < BN; ++j) {
           const int col = n0 + j;
@@ -400,6 +418,27 @@ __global__ void __launch_bounds__(kThreads, 1) split_gemm_kernel(const GemmParam
     __syncwarp();
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+  }
+}
+
+// Fixed-order sum of the split-K partial contributions into C.
+__global__ void __launch_bounds__(256) split_reduce_kernel(const DevProblem* __restrict__ probs,
+                                                           const int* __restrict__ red_prob,
+                                                           const int64_t* __restrict__ red_first, int nred,
+                                                           int64_t total) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    int lo = 0, hi = nred - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (red_first[mid] <= e) lo = mid; else hi = mid - 1;
+    }
+    const DevProblem& p = probs[red_prob[lo]];
+    const int64_t i = e - red_first[lo];
+    const int64_t mn = (int64_t)p.M * p.N;
+    double acc = 0.0;
+    for (int c = 0; c < p.ksplit; ++c) acc += p.partial[c * mn + i];
+    const int64_t row = i / p.N, col = i - row * p.N;
+    p.C[row * p.ldc + col] = acc;
   }
 }
 
@@ -491,9 +530,17 @@ struct SplitPlan {
   int* d_tile_first = nullptr;
   CUtensorMap* d_maps = nullptr;
   int* d_err = nullptr;
+  double* d_partial = nullptr;
+  int* d_red_prob = nullptr;
+  int64_t* d_red_first = nullptr;
+  int nred = 0;
+  int64_t red_total = 0;
   int total_tiles = 0;
   double bytes = 0.0;
   ~SplitPlan() {
+    dev_free(d_partial);
+    dev_free(d_red_prob);
+    dev_free(d_red_first);
     dev_free(d_slices);
     dev_free(d_exps);
     dev_free(d_sets_a);
@@ -546,6 +593,12 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
   std::vector<CUtensorMap> maps;
   int64_t ra = 0, rb = 0;
   int tiles = 0;
+  int64_t out_tiles = 0;
+  for (size_t i = 0; i < probs.size(); ++i) out_tiles += (offs[i].Mp / BM) * (offs[i].Np / kBN);
+  int64_t part_elems = 0;
+  std::vector<int> red;
+  std::vector<int64_t> red_first;
+  int64_t red_total = 0;
   for (size_t i = 0; i < probs.size(); ++i) {
     const SplitProblem& p = probs[i];
     const Off& o = offs[i];
@@ -562,18 +615,50 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
     d.nkb = (int)(o.Kp / BK);
     d.tiles_m = (int)(o.Mp / BM);
     d.tiles_n = (int)(o.Np / kBN);
+    // split K when the output tiles of all problems leave SMs idle; ranges are
+    // whole exact-accumulation chunks
+    int ks = 1;
+    if (out_tiles < kSplitFill && d.nkb > 2 * kChunkKb) {
+      int want = (int)((kSplitFill + out_tiles - 1) / out_tiles);
+      ks = std::max(1, std::min(want, d.nkb / kChunkKb));
+    }
+    int per = (d.nkb + ks - 1) / ks;
+    per = (per + kChunkKb - 1) / kChunkKb * kChunkKb;
+    ks = (d.nkb + per - 1) / per;
+    d.ksplit = ks;
+    d.kb_per_split = per;
     d.eA = sp->d_exps + o.ea;
     d.eB = sp->d_exps + o.eb;
     d.C = p.C;
+    d.partial = nullptr;
+    if (ks > 1) {
+      d.partial = (double*)(intptr_t)(part_elems + 1);
+      part_elems += (int64_t)ks * p.M * p.N;
+      red.push_back((int)i);
+      red_first.push_back(red_total);
+      red_total += p.M * p.N;
+    }
     d.ldc = p.N;
     dp.push_back(d);
     first.push_back(tiles);
-    tiles += d.tiles_m * d.tiles_n;
+    tiles += d.tiles_m * d.tiles_n * ks;
     CUtensorMap ma, mb;
     GBX_TRY(encode_slices(&ma, sp->d_slices + o.a, S, o.Mp, o.Kp, BM));
     GBX_TRY(encode_slices(&mb, sp->d_slices + o.b, S, o.Np, o.Kp, kBN));
     maps.push_back(ma);
     maps.push_back(mb);
+  }
+  if (part_elems > 0) {
+    GBX_TRY(dev_alloc((void**)&sp->d_partial, sizeof(double) * part_elems));
+    for (auto& d : dp)
+      if (d.partial) d.partial = sp->d_partial + ((intptr_t)d.partial - 1);
+    GBX_TRY(dev_alloc((void**)&sp->d_red_prob, sizeof(int) * red.size()));
+    GBX_TRY(dev_alloc((void**)&sp->d_red_first, sizeof(int64_t) * red.size()));
+    GBX_CUDA(cudaMemcpy(sp->d_red_prob, red.data(), sizeof(int) * red.size(), cudaMemcpyHostToDevice));
+    GBX_CUDA(cudaMemcpy(sp->d_red_first, red_first.data(), sizeof(int64_t) * red.size(), cudaMemcpyHostToDevice));
+    sp->nred = (int)red.size();
+    sp->red_total = red_total;
+    sp->bytes += 8.0 * part_elems;
   }
   sp->nsets = (int)probs.size();
   sp->rows_a = ra;
@@ -597,16 +682,22 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
   return GBX_OK;
 }
 
-int run_split_plan(SplitPlan* sp, bool split_a, cudaStream_t st) {
+int split_operands(SplitPlan* sp, bool split_a, bool split_b, cudaStream_t st) {
   if (!sp || sp->nsets == 0) return GBX_OK;
   if (split_a && sp->rows_a > 0) {
     split_rows_kernel<<<(unsigned)((sp->rows_a + 7) / 8), 256, 0, st>>>(sp->d_sets_a, sp->nsets, sp->rows_a, sp->S);
     GBX_CUDA(cudaGetLastError());
   }
-  if (sp->rows_b > 0) {
+  if (split_b && sp->rows_b > 0) {
     split_rows_kernel<<<(unsigned)((sp->rows_b + 7) / 8), 256, 0, st>>>(sp->d_sets_b, sp->nsets, sp->rows_b, sp->S);
     GBX_CUDA(cudaGetLastError());
   }
+  return GBX_OK;
+}
+
+int run_split_plan(SplitPlan* sp, bool split_a, bool split_b, cudaStream_t st) {
+  if (!sp || sp->nsets == 0) return GBX_OK;
+  GBX_TRY(split_operands(sp, split_a, split_b, st));
   if (sp->total_tiles == 0) return GBX_OK;
   GemmParams P;
   P.probs = sp->d_probs;
@@ -624,6 +715,11 @@ int run_split_plan(SplitPlan* sp, bool split_a, cudaStream_t st) {
   size_t smem = sizeof(Smem<kBN>) + 1024;
   split_gemm_kernel<kBN><<<grid, kThreads, smem, st>>>(P);
   GBX_CUDA(cudaGetLastError());
+  if (sp->nred > 0) {
+    int rg = (int)std::min<int64_t>((sp->red_total + 255) / 256, 152 * 8);
+    split_reduce_kernel<<<rg, 256, 0, st>>>(sp->d_probs, sp->d_red_prob, sp->d_red_first, sp->nred, sp->red_total);
+    GBX_CUDA(cudaGetLastError());
+  }
   return GBX_OK;
 }
 
@@ -632,6 +728,18 @@ int split_plan_error(SplitPlan* sp) {
   int e = 0;
   if (cudaMemcpy(&e, sp->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
   return e;
+}
+
+double split_plan_tensor_flops(const SplitPlan* sp) {
+  if (!sp) return 0.0;
+  double f = 0.0;
+  const double pairs = sp->S * (sp->S + 1) / 2.0;
+  for (auto& p : sp->host) {
+    double Mp = (double)((p.M + BM - 1) / BM * BM), Np = (double)((p.N + kBN - 1) / kBN * kBN);
+    double Kp = (double)((p.K + BK - 1) / BK * BK);
+    f += 2.0 * pairs * Mp * Np * Kp;
+  }
+  return f;
 }
 
 void destroy_split_plan(SplitPlan* sp) { delete sp; }

@@ -251,7 +251,7 @@ ContractionPlan::~ContractionPlan() {
 int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorLayout& C,
                      const std::vector<std::string>& la, const std::vector<std::string>& lb,
                      const std::vector<std::string>& lc, Engine e, int nslices,
-                     std::unique_ptr<ContractionPlan>& out) {
+                     std::unique_ptr<ContractionPlan>& out, bool split_all) {
   if ((int)la.size() != A.rank || (int)lb.size() != B.rank || (int)lc.size() != C.rank)
     return fail(GBX_EINVAL, "index strings do not match tensor ranks (%d/%d, %d/%d, %d/%d)", (int)la.size(), A.rank,
                 (int)lb.size(), B.rank, (int)lc.size(), C.rank);
@@ -426,6 +426,7 @@ int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorL
   GBX_TRY(check_moves(p->packA, A.nelem, p->a_elems, "pack A"));
   GBX_TRY(check_moves(p->packB, B.nelem, p->b_elems, "pack B"));
   GBX_TRY(check_moves(p->unpackC, p->c_elems, C.nelem, "unpack C"));
+  p->split_all = split_all;
   GBX_TRY(p->build(e, nslices));
   out = std::move(p);
   return GBX_OK;
@@ -440,34 +441,16 @@ int ContractionPlan::build(Engine e, int nslices) {
   GBX_TRY(dev_alloc((void**)&d_Abig, sizeof(double) * a_elems));
   GBX_TRY(dev_alloc((void**)&d_Bbig, sizeof(double) * b_elems));
   GBX_TRY(dev_alloc((void**)&d_Cbig, sizeof(double) * c_elems));
-  if (e == Engine::F64) {
-    std::vector<GemmProblem> probs;
-    for (auto& g : groups) {
-      if (g.M == 0 || g.N == 0 || g.K == 0) continue;
-      if (g.M >= (1ll << 31) || g.N >= (1ll << 31) || g.K >= (1ll << 31))
-        return fail(GBX_EUNSUPPORTED, "packed block too large");
-      GemmProblem q;
-      std::memset(&q, 0, sizeof(q));
-      q.A = d_Abig + g.a_off;
-      q.B = d_Bbig + g.b_off;
-      q.C = d_Cbig + g.c_off;
-      q.a_rs = g.K;
-      q.a_cs = 1;
-      q.b_rs = g.K;
-      q.b_cs = 1;
-      q.c_rs = g.N;
-      q.m = (int)g.M;
-      q.n = (int)g.N;
-      q.k = (int)g.K;
-      q.alpha = 1.0;
-      q.accumulate = 0;
-      probs.push_back(q);
-    }
-    GBX_TRY(f64.build(probs));
-  } else {
-    std::vector<SplitProblem> sp;
-    for (auto& g : groups) {
-      if (g.M == 0 || g.N == 0 || g.K == 0) continue;
+  std::vector<GemmProblem> probs;
+  std::vector<SplitProblem> sp;
+  for (auto& g : groups) {
+    if (g.M == 0 || g.N == 0 || g.K == 0) continue;
+    if (g.M >= (1ll << 31) || g.N >= (1ll << 31) || g.K >= (1ll << 31))
+      return fail(GBX_EUNSUPPORTED, "packed block too large");
+    const bool use_split =
+        e == Engine::Split &&
+        (split_all || (g.K >= kSplitMinK && 2.0 * (double)g.M * (double)g.N * (double)g.K >= kSplitMinFlops));
+    if (use_split) {
       SplitProblem q;
       q.A = d_Abig + g.a_off;
       q.B = d_Bbig + g.b_off;
@@ -476,27 +459,59 @@ int ContractionPlan::build(Engine e, int nslices) {
       q.N = g.N;
       q.K = g.K;
       sp.push_back(q);
+      continue;
     }
-    GBX_TRY(create_split_plan(sp, nslices, &split));
+    GemmProblem q;
+    std::memset(&q, 0, sizeof(q));
+    q.A = d_Abig + g.a_off;
+    q.B = d_Bbig + g.b_off;
+    q.C = d_Cbig + g.c_off;
+    q.a_rs = g.K;
+    q.a_cs = 1;
+    q.b_rs = g.K;
+    q.b_cs = 1;
+    q.c_rs = g.N;
+    q.m = (int)g.M;
+    q.n = (int)g.N;
+    q.k = (int)g.K;
+    q.alpha = 1.0;
+    q.accumulate = 0;
+    probs.push_back(q);
   }
+  n_f64_groups = (int)probs.size();
+  n_split_groups = (int)sp.size();
+  GBX_TRY(f64.build(probs));
+  if (!sp.empty()) GBX_TRY(create_split_plan(sp, nslices, &split));
+  return GBX_OK;
+}
+
+int ContractionPlan::prepare_static(const double* dA, const double* dB, cudaStream_t st) {
+  if (a_static) {
+    if (a_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Abig, 0, sizeof(double) * a_elems, st));
+    GBX_TRY(run_moves(packA, dA, d_Abig, st));
+  }
+  if (b_static) {
+    if (b_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Bbig, 0, sizeof(double) * b_elems, st));
+    GBX_TRY(run_moves(packB, dB, d_Bbig, st));
+  }
+  if (split) GBX_TRY(split_operands(split, a_static, b_static, st));
+  static_ready = a_static || b_static;
   return GBX_OK;
 }
 
 int ContractionPlan::execute(const double* dA, const double* dB, double* dC, double alpha, cudaStream_t st) {
   if (f64.nprob == 0 && !split) return GBX_OK;
-  bool skipA = a_static && a_ready;
+  const bool skipA = a_static && static_ready, skipB = b_static && static_ready;
   if (!skipA) {
     if (a_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Abig, 0, sizeof(double) * a_elems, st));
     GBX_TRY(run_moves(packA, dA, d_Abig, st));
   }
-  if (b_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Bbig, 0, sizeof(double) * b_elems, st));
-  GBX_TRY(run_moves(packB, dB, d_Bbig, st));
-  if (engine == Engine::F64) {
-    GBX_TRY(f64.run(st));
-  } else {
-    GBX_TRY(run_split_plan(split, !skipA, st));
+  if (!skipB) {
+    if (b_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Bbig, 0, sizeof(double) * b_elems, st));
+    GBX_TRY(run_moves(packB, dB, d_Bbig, st));
   }
-  if (a_static) a_ready = true;
+  GBX_TRY(f64.run(st));
+  if (split) GBX_TRY(run_split_plan(split, !skipA, !skipB, st));
   return run_moves_scaled(unpackC, d_Cbig, dC, alpha, st);
 }
 

@@ -102,6 +102,11 @@ struct GroupBlock {   // one irrep block of the packed operands
 
 enum class Engine { F64 = 0, Split = 1 };
 
+// A packed GEMM goes to the split engine only when it is large enough to feed
+// the tensor cores; smaller ones (and every K < kSplitMinK) stay on FP64.
+constexpr int64_t kSplitMinK = 128;
+constexpr double kSplitMinFlops = 2.0 * 128 * 64 * 1024;
+
 struct SplitPlan;  // the split-precision GEMM state (gemm_split.cu)
 
 struct ContractionPlan {
@@ -121,20 +126,25 @@ struct ContractionPlan {
   SplitPlan* split = nullptr;
   double flops = 0.0;        // algorithmic: 2 * sum over nonzero triples m*n*k
   double gemm_flops = 0.0;   // what the packed GEMMs execute
-  bool a_static = false;     // A's values do not change between executes (split once)
-  bool a_ready = false;
+  // Operands whose values never change (integrals) are packed and split once
+  // by prepare_static and skipped by execute.
+  bool a_static = false, b_static = false;
+  bool static_ready = false;
+  int n_split_groups = 0, n_f64_groups = 0;
+  bool split_all = false;
 
   ~ContractionPlan();
   int build(Engine e, int nslices);
-  // C += alpha * A * B.  When skip_pack_a is set the packed / split A from the
-  // previous execute is reused (the operand is constant, e.g. integrals).
+  int prepare_static(const double* dA, const double* dB, cudaStream_t st);
+  // C += alpha * A * B.
   int execute(const double* dA, const double* dB, double* dC, double alpha, cudaStream_t st);
 };
 
+// split_all: every packed GEMM of a split plan uses the split engine (tests).
 int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorLayout& C,
                      const std::vector<std::string>& la, const std::vector<std::string>& lb,
                      const std::vector<std::string>& lc, Engine e, int nslices,
-                     std::unique_ptr<ContractionPlan>& out);
+                     std::unique_ptr<ContractionPlan>& out, bool split_all = false);
 
 // Tile moves accumulating alpha * permuted A into C: C[c] += alpha * A[a],
 // the DLTC Summation (DLTC/task.cc:51-81) over block-sparse layouts.

@@ -20,10 +20,15 @@ struct SplitProblem {
 
 struct SplitPlan;
 int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitPlan** out);
-// split_a: re-split A (false when A is unchanged since the last run).
-int run_split_plan(SplitPlan* sp, bool split_a, cudaStream_t st);
+// split_a / split_b: re-split that operand (false when it is unchanged since
+// the last run, e.g. constant integrals).
+int run_split_plan(SplitPlan* sp, bool split_a, bool split_b, cudaStream_t st);
+// Only the split kernels (for operands that stay constant afterwards).
+int split_operands(SplitPlan* sp, bool split_a, bool split_b, cudaStream_t st);
 void destroy_split_plan(SplitPlan* sp);
 double split_plan_bytes(const SplitPlan* sp);
+// bf16 tensor flops one run issues (S(S+1)/2 slice products on padded tiles).
+double split_plan_tensor_flops(const SplitPlan* sp);
 // Error word of the GEMM kernel (0 = ok, else the wait that ran out); syncs.
 int split_plan_error(SplitPlan* sp);
 

@@ -31,6 +31,7 @@ typedef struct {
     int engine;          /* GBX_MODE_FP64 or GBX_MODE_SPLIT */
     int slices;          /* split engine: bf16 slices per operand (0 = default) */
     int use_graph;       /* capture one iteration as a CUDA graph */
+    int split_all;       /* split engine on every GEMM, however small (default: large ones only) */
     uint64_t seed;
     double eps_occ_lo, eps_occ_hi, eps_vir_lo, eps_vir_hi;
     double v_scale, v_decay; /* |<pq||rs>| = v_scale * exp(-(|p-q| + |r-s|) / v_decay) */
@@ -78,10 +79,16 @@ GBX_API int gbx_cc_set_amplitudes(gbx_cc_job* job, const double* t1, const doubl
 GBX_API int gbx_cc_read_energy(gbx_cc_job* job, double* energy, void* stream);
 /* Run one iteration step by step with CUDA events between the steps and
  * report per step: time (ms), algorithmic flops, bytes, kind (0 contraction,
- * 1 permuted sum, 2 zero, 3 denominator, 4 energy) and a name of name_len
- * chars.  Counts as one iteration of the job. */
-GBX_API int gbx_cc_profile(gbx_cc_job* job, int cap, float* ms, double* flops, double* bytes, int* kind, char* names,
-                           int name_len, int* count, void* stream);
+ * 1 permuted sum, 2 zero, 3 denominator, 4 energy), the contraction index
+ * (or -1) and a name of name_len chars.  Counts as one iteration. */
+GBX_API int gbx_cc_profile(gbx_cc_job* job, int cap, float* ms, double* flops, double* bytes, int* kind, int* plan,
+                           char* names, int name_len, int* count, void* stream);
+/* Time only the GEMM launches of one contraction (its operands as the last
+ * iteration left them), reps times, with CUDA events on stream.  Reports
+ * ms per run, the FP64 flops of the packed GEMMs, the bf16 tensor flops the
+ * split engine issues, and the engine (0 FP64, 1 split, 2 both). */
+GBX_API int gbx_cc_time_gemm(gbx_cc_job* job, int contraction, int reps, float* ms, double* fp64_flops,
+                             double* tensor_flops, int* engine, void* stream);
 GBX_API int gbx_cc_destroy(gbx_cc_job* job);
 
 #ifdef __cplusplus

@@ -48,3 +48,32 @@ def test_cc_graph_and_eager_identical():
     assert np.array_equal(ea, eb)
     st = a.stats()
     assert st.flops_per_iter > 0 and st.ncontractions > 30
+
+
+@pytest.mark.parametrize("method", ["ccd", "ccsd"])
+def test_cc_split_engine_energy_within_1e10(method):
+    """Split engine on every GEMM (6 slices): per-iteration correlation energy
+    within 1e-10 Eh of the FP64 oracle."""
+    from dtcf_gb300.cc import Job
+    case = CASES[1]
+    job = Job(method=method, engine="split", split_all=1, **case)
+    ref = occ.CC(_system(case), method)
+    e_ref = np.array(ref.iterate(6))
+    e_gpu = np.concatenate([job.energies()[:1], job.iterate(6)])
+    err = np.max(np.abs(e_gpu - e_ref))
+    assert err <= 1e-10, err
+    t1, t2 = job.amplitudes()
+    assert np.max(np.abs(t2 - ref.t2)) <= 1e-9
+    job.close()
+
+
+def test_cc_gemm_shapes_match_oracle_planner():
+    """The packed GEMM shapes of one iteration equal the oracle's derivation
+    from irrep occupations (the CPU arm times exactly these dgemms)."""
+    from dtcf_gb300.cc import Job
+    from oracle import cc_cpu
+    case = dict(nocc=16, nvir=48, nirrep=8, max_block=6, min_block=1, seed=2)
+    job = Job(method="ccsd", **case)
+    got = sorted(map(tuple, job.gemm_shapes().tolist()))
+    want = sorted(cc_cpu.gemm_shapes(_system(case), "ccsd"))
+    assert got == want
