@@ -101,6 +101,7 @@ struct gbx_cc_job {
   int npartial = 608;
   double flops = 0.0, gemm_flops = 0.0;
   int launches = 0;
+  int iter_plan_begin = 0;  // plans before this index serve only the initial guess
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
 
@@ -341,6 +342,9 @@ int gbx_cc_job::build() {
   GBX_TRY(gbx::run_energy(get("OOVV")->d, get(TAU)->d, get("OOVV")->L.nelem, d_partial, npartial, d_hist, d_count,
                           hist_cap, st0));
   launches = 0;
+  flops = 0.0;
+  gemm_flops = 0.0;
+  iter_plan_begin = (int)cplans.size();
 
   // ---- one iteration --------------------------------------------------------
   if (sd) GBX_TRY(tau_steps());
@@ -599,7 +603,7 @@ int gbx_cc_stats_get(const gbx_cc_job* job, gbx_cc_stats* s) {
   for (auto& kv : job->T) bytes += 8.0 * kv.second->L.nelem;
   for (auto& p : job->cplans) bytes += 8.0 * (p->a_elems + p->b_elems + p->c_elems) + split_plan_bytes(p->split);
   s->resident_bytes = bytes;
-  s->ncontractions = (int)job->cplans.size();
+  s->ncontractions = (int)job->cplans.size() - job->iter_plan_begin;
   s->nsums = (int)job->splans.size();
   s->nblocks_occ = (int)job->occ->ext.size();
   s->nblocks_vir = (int)job->vir->ext.size();
@@ -665,8 +669,8 @@ int gbx_cc_get_amplitudes(gbx_cc_job* job, double* t1, double* t2, void* stream)
 int gbx_cc_gemm_shapes(const gbx_cc_job* job, int64_t* mnk, int* count) {
   if (!job || !count) return fail(GBX_EINVAL, "bad arguments");
   int n = 0;
-  for (auto& p : job->cplans)
-    for (auto& g : p->groups) {
+  for (size_t pi = job->iter_plan_begin; pi < job->cplans.size(); ++pi)
+    for (auto& g : job->cplans[pi]->groups) {
       if (g.M == 0 || g.N == 0 || g.K == 0) continue;
       if (mnk && n < *count) {
         mnk[3 * n] = g.M;

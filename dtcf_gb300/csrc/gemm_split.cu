@@ -522,8 +522,8 @@ struct SplitPlan {
   std::vector<SplitProblem> host;
   __nv_bfloat16* d_slices = nullptr;  // all A and B slices
   int* d_exps = nullptr;
-  SplitRowSet* d_sets_a = nullptr;
-  SplitRowSet* d_sets_b = nullptr;
+  SplitRowSet* d_sets_a = nullptr;  // rows from the plan's packed A
+  SplitRowSet* d_sets_b = nullptr;  // rows from the plan's packed B
   int nsets = 0;
   int64_t rows_a = 0, rows_b = 0;
   DevProblem* d_probs = nullptr;
@@ -602,12 +602,18 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
   for (size_t i = 0; i < probs.size(); ++i) {
     const SplitProblem& p = probs[i];
     const Off& o = offs[i];
-    SplitRowSet a{p.A, p.M, p.K, sp->d_slices + o.a, o.Mp * o.Kp, o.Kp, sp->d_exps + o.ea, ra};
-    SplitRowSet b{p.B, p.N, p.K, sp->d_slices + o.b, o.Np * o.Kp, o.Kp, sp->d_exps + o.eb, rb};
-    ra += p.M;
-    rb += p.N;
-    sa.push_back(a);
-    sb.push_back(b);
+    // row sets are grouped by the plan operand they come from, so constant
+    // plan operands can be split once
+    SplitRowSet a{p.A, p.M, p.K, sp->d_slices + o.a, o.Mp * o.Kp, o.Kp, sp->d_exps + o.ea, 0};
+    SplitRowSet b{p.B, p.N, p.K, sp->d_slices + o.b, o.Np * o.Kp, o.Kp, sp->d_exps + o.eb, 0};
+    SplitRowSet& to_a = p.a_is_plan_b ? b : a;  // rows that come from plan A
+    SplitRowSet& to_b = p.a_is_plan_b ? a : b;
+    to_a.first_row = ra;
+    ra += to_a.rows;
+    to_b.first_row = rb;
+    rb += to_b.rows;
+    sa.push_back(to_a);
+    sb.push_back(to_b);
     DevProblem d;
     d.M = (int)p.M;
     d.N = (int)p.N;
@@ -682,22 +688,22 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
   return GBX_OK;
 }
 
-int split_operands(SplitPlan* sp, bool split_a, bool split_b, cudaStream_t st) {
+int split_operands(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st) {
   if (!sp || sp->nsets == 0) return GBX_OK;
-  if (split_a && sp->rows_a > 0) {
+  if (plan_a && sp->rows_a > 0) {
     split_rows_kernel<<<(unsigned)((sp->rows_a + 7) / 8), 256, 0, st>>>(sp->d_sets_a, sp->nsets, sp->rows_a, sp->S);
     GBX_CUDA(cudaGetLastError());
   }
-  if (split_b && sp->rows_b > 0) {
+  if (plan_b && sp->rows_b > 0) {
     split_rows_kernel<<<(unsigned)((sp->rows_b + 7) / 8), 256, 0, st>>>(sp->d_sets_b, sp->nsets, sp->rows_b, sp->S);
     GBX_CUDA(cudaGetLastError());
   }
   return GBX_OK;
 }
 
-int run_split_plan(SplitPlan* sp, bool split_a, bool split_b, cudaStream_t st) {
+int run_split_plan(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st) {
   if (!sp || sp->nsets == 0) return GBX_OK;
-  GBX_TRY(split_operands(sp, split_a, split_b, st));
+  GBX_TRY(split_operands(sp, plan_a, plan_b, st));
   if (sp->total_tiles == 0) return GBX_OK;
   GemmParams P;
   P.probs = sp->d_probs;

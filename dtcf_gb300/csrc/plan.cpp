@@ -239,6 +239,24 @@ void sub_strides(const std::vector<int64_t>& ext, int64_t base, std::vector<int6
 
 }  // namespace
 
+void choose_engine(GroupBlock& g, bool split_engine, bool split_all, int slices) {
+  g.engine = 0;
+  g.swap = false;
+  if (!split_engine || g.M == 0 || g.N == 0 || g.K == 0) return;
+  auto up = [](int64_t x, int64_t m) { return (double)((x + m - 1) / m * m); };
+  const int S = slices > 0 ? slices : 6;
+  const double pairs = S * (S + 1) / 2.0;
+  const double kp = up(g.K, 64);
+  const double t_split = 2.0 * pairs * up(g.M, 128) * up(g.N, 64) * kp / 1.0e15;
+  const double t_split_sw = 2.0 * pairs * up(g.N, 128) * up(g.M, 64) * kp / 1.0e15;
+  const double t_f64 = 2.0 * up(g.M, 64) * up(g.N, 64) * (double)g.K / 0.95e12;
+  const double best_split = std::min(t_split, t_split_sw) + 4e-6;  // + split and launch overhead
+  if (split_all || best_split < t_f64) {
+    g.engine = 1;
+    g.swap = t_split_sw < t_split;
+  }
+}
+
 ContractionPlan::~ContractionPlan() {
   if (own_workspace) {
     dev_free(d_Abig);
@@ -323,6 +341,7 @@ int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorL
   p->a_elems = ao;
   p->b_elems = bo;
   p->c_elems = co;
+  for (auto& g : p->groups) choose_engine(g, e == Engine::Split, split_all, nslices);
 
   // pack moves: A (rows = extA tuples of irrep h, cols = K tuples of irrep h)
   auto pack = [&](const TensorLayout& T, const std::vector<int>& ext_dims, const std::vector<int>& contr_dims,
@@ -389,8 +408,10 @@ int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorL
     std::vector<int64_t> eR, eC, sR, sC;
     for (size_t i = 0; i < s.extA.size(); ++i) eR.push_back(dA[i]->ext[c_row[t][i]]);
     for (size_t i = 0; i < s.extB.size(); ++i) eC.push_back(dB[i]->ext[c_col[t][i]]);
-    sub_strides(eR, g.N, sR);
-    sub_strides(eC, 1, sC);
+    // C block of the group: row-major M x N, or N x M when the GEMM is swapped
+    sub_strides(eR, g.swap ? 1 : g.N, sR);
+    sub_strides(eC, g.swap ? g.M : 1, sC);
+    const int64_t blk_off = g.swap ? coff * g.M + roff : roff * g.N + coff;
     int64_t ext[kMaxDims], sstr[kMaxDims], dstr[kMaxDims];
     dstr[C.rank - 1] = 1;
     for (int d = C.rank - 2; d >= 0; --d) dstr[d] = dstr[d + 1] * C.dims[d + 1]->ext[cc[d + 1]];
@@ -398,7 +419,7 @@ int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorL
       ext[d] = C.dims[d]->ext[cc[d]];
       sstr[d] = s.c_from[d] >= 0 ? sR[s.c_from[d]] : sC[-1 - s.c_from[d]];
     }
-    p->unpackC.host.push_back(make_move(C.rank, ext, sstr, dstr, g.c_off + roff * g.N + coff, C.off[t], 1, 1.0));
+    p->unpackC.host.push_back(make_move(C.rank, ext, sstr, dstr, g.c_off + blk_off, C.off[t], 1, 1.0));
   }
 
   // algorithmic flops over nonzero (A-block, B-block -> C-block) triples
@@ -447,16 +468,22 @@ int ContractionPlan::build(Engine e, int nslices) {
     if (g.M == 0 || g.N == 0 || g.K == 0) continue;
     if (g.M >= (1ll << 31) || g.N >= (1ll << 31) || g.K >= (1ll << 31))
       return fail(GBX_EUNSUPPORTED, "packed block too large");
-    const bool use_split =
-        e == Engine::Split &&
-        (split_all || (g.K >= kSplitMinK && 2.0 * (double)g.M * (double)g.N * (double)g.K >= kSplitMinFlops));
-    if (use_split) {
+    if (g.engine == 1) {
       SplitProblem q;
-      q.A = d_Abig + g.a_off;
-      q.B = d_Bbig + g.b_off;
+      if (g.swap) {  // C^T = B A^T: rows from B, C block stored N x M
+        q.A = d_Bbig + g.b_off;
+        q.B = d_Abig + g.a_off;
+        q.M = g.N;
+        q.N = g.M;
+        q.a_is_plan_b = true;
+      } else {
+        q.A = d_Abig + g.a_off;
+        q.B = d_Bbig + g.b_off;
+        q.M = g.M;
+        q.N = g.N;
+        q.a_is_plan_b = false;
+      }
       q.C = d_Cbig + g.c_off;
-      q.M = g.M;
-      q.N = g.N;
       q.K = g.K;
       sp.push_back(q);
       continue;

@@ -98,14 +98,17 @@ struct GroupBlock {   // one irrep block of the packed operands
   int h;
   int64_t M, N, K;
   int64_t a_off, b_off, c_off;  // element offsets in the packed buffers
+  int engine = 0;               // 0 FP64 (DMMA), 1 split (tcgen05)
+  bool swap = false;            // split engine computes C^T = B A^T (C block stored N x M)
 };
+
+// Engine and orientation of one packed GEMM from a throughput model of this
+// GPU: FP64 DMMA near 0.95 TFLOP/s on 64x64 tiles, the split engine near
+// 1 PFLOP/s of bf16 slice products on 128x64 tiles (S(S+1)/2 products).
+void choose_engine(GroupBlock& g, bool split_engine, bool split_all, int slices);
 
 enum class Engine { F64 = 0, Split = 1 };
 
-// A packed GEMM goes to the split engine only when it is large enough to feed
-// the tensor cores; smaller ones (and every K < kSplitMinK) stay on FP64.
-constexpr int64_t kSplitMinK = 128;
-constexpr double kSplitMinFlops = 2.0 * 128 * 64 * 1024;
 
 struct SplitPlan;  // the split-precision GEMM state (gemm_split.cu)
 

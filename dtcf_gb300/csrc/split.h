@@ -16,15 +16,18 @@ struct SplitProblem {
   const double* B;
   double* C;
   int64_t M, N, K;
+  // the GEMM's A rows come from the plan's packed B operand (swapped
+  // orientation); split_operands(plan_a, plan_b) maps accordingly
+  bool a_is_plan_b = false;
 };
 
 struct SplitPlan;
 int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitPlan** out);
-// split_a / split_b: re-split that operand (false when it is unchanged since
-// the last run, e.g. constant integrals).
-int run_split_plan(SplitPlan* sp, bool split_a, bool split_b, cudaStream_t st);
+// plan_a / plan_b: re-split the operands that come from the plan's packed A /
+// B (false when unchanged since the last run, e.g. constant integrals).
+int run_split_plan(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st);
 // Only the split kernels (for operands that stay constant afterwards).
-int split_operands(SplitPlan* sp, bool split_a, bool split_b, cudaStream_t st);
+int split_operands(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st);
 void destroy_split_plan(SplitPlan* sp);
 double split_plan_bytes(const SplitPlan* sp);
 // bf16 tensor flops one run issues (S(S+1)/2 slice products on padded tiles).

@@ -179,3 +179,22 @@ def test_rrr_plan_cntr4a_shape(gbx):
     got = host(C.tiles).reshape(want.shape)
     assert np.max(np.abs(got - want)) <= 1e-12 * np.abs(want).max()
     assert ctr.plan("a,b,k,l", "m,n,k,l", "a,b,m,n").flops == 2.0 * n ** 6
+
+
+@pytest.mark.parametrize("sign", [1, -1])
+def test_rrr_plan_split_engine(gbx, sign):
+    """The same unique-block ladder on the split-precision engine (6 slices):
+    within 1e-13 of the FP64 oracle relative to the largest element."""
+    from dtcf_gb300.rrr import Contraction
+    o, v, blk = 16, 48, 8
+    V, T, C = _rrr_case("aabb", "aabb", "aabb", [(v, v, v, v), (v, v, o, o), (v, v, o, o)],
+                        [(v // blk,) * 4, (v // blk, v // blk, o // blk, o // blk), (v // blk, v // blk, o // blk, o // blk)],
+                        21)
+    want = oracle.rrr.contract(_as_oracle(V), _as_oracle(T), _as_oracle(C), "a,b,e,f", "e,f,i,j", "a,b,i,j", 0.5,
+                               sign)
+    ctr = Contraction(V, T, C, mode="split", sign=sign)
+    ctr.contract("a,b,e,f", "e,f,i,j", "a,b,i,j", 0.5)
+    got = host(C.tiles).reshape(want.shape)
+    assert np.max(np.abs(got - want)) <= 1e-13 * np.abs(want).max()
+    # the unique-block flop count of this contraction (o=16, v=48, block 8)
+    assert ctr.plan("a,b,e,f", "e,f,i,j", "a,b,i,j").flops == 2.0 * 63 * 4096 * 2304
