@@ -102,7 +102,7 @@ struct GemmProblem {
   int m, n, k;
   double alpha;
   int accumulate;
-  // split-K (filled by F64Gemm::build)
+  // split-K and tile shape (filled by F64Gemm::build)
   int ksplit, kchunk, pad_;
   double* partial;
 };
@@ -110,13 +110,18 @@ struct GemmProblem {
 // Grouped FP64 GEMM: C_p (+)= alpha_p * A_p * B_p^T for all problems in one
 // persistent launch (plus a fixed-order split-K reduction when needed).
 struct F64Gemm {
-  GemmProblem* d_probs = nullptr;
-  int* d_first = nullptr;
-  int* d_ticket = nullptr;
+  struct Sub {  // one launch: the problems of one tile shape
+    GemmProblem* d_probs = nullptr;
+    int* d_first = nullptr;
+    int* d_ticket = nullptr;
+    int nprob = 0, total_tiles = 0, variant = 0;
+  };
+  std::vector<Sub> subs;
+  GemmProblem* d_all = nullptr;  // every problem (for the split-K reduction)
   double* d_partial = nullptr;
   int* d_red_prob = nullptr;
   uint32_t* d_red_first = nullptr;
-  int nprob = 0, total_tiles = 0, nred = 0;
+  int nprob = 0, nred = 0;
   uint32_t red_chunks = 0;
   double workspace_bytes = 0.0;
   bool async_stream_set = false;
@@ -127,9 +132,10 @@ struct F64Gemm {
   void release();
   ~F64Gemm() { release(); }
 };
-// Tile decomposition shared by the host planner and the kernel.
-constexpr int kF64TileM = 64;
-constexpr int kF64TileN = 64;
+// Tile shapes shared by the host planner and the kernels.
+int f64_variant(int m, int n);
+int f64_tile_m(int variant);
+int f64_tile_n(int variant);
 int f64_tiles(int m, int n);
 
 // Device scratch allocation helpers (the library's own allocations go

@@ -20,7 +20,7 @@
 namespace gbx {
 
 namespace {
-constexpr int BM = kF64TileM, BN = kF64TileN, BK = 16;
+constexpr int BK = 16;
 constexpr int kThreads = 128;
 constexpr int kPad = 1;               // pad rows to spread shared-memory banks
 constexpr int kFillTiles = 152 * 3;   // work items that keep every SM busy
@@ -29,7 +29,15 @@ constexpr int kRedThreads = 256;
 constexpr int kRedChunk = 2048;
 }  // namespace
 
-int f64_tiles(int m, int n) { return ((m + BM - 1) / BM) * ((n + BN - 1) / BN); }
+// Tile shapes: 64x64 for large problems, 64x16 / 16x64 / 16x16 for skinny ones
+// (output dimensions below 48), so small outputs do not waste the FP64 pipe.
+int f64_variant(int m, int n) { return (m < 48 ? 2 : 0) + (n < 48 ? 1 : 0); }
+int f64_tile_m(int variant) { return (variant & 2) ? 16 : 64; }
+int f64_tile_n(int variant) { return (variant & 1) ? 16 : 64; }
+int f64_tiles(int m, int n) {
+  const int v = f64_variant(m, n), tm = f64_tile_m(v), tn = f64_tile_n(v);
+  return ((m + tm - 1) / tm) * ((n + tn - 1) / tn);
+}
 
 __device__ __forceinline__ void dmma884(double (&c)[2], double a, double b) {
   asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
@@ -37,9 +45,12 @@ __device__ __forceinline__ void dmma884(double (&c)[2], double a, double b) {
                : "d"(a), "d"(b));
 }
 
+template <int BM, int BN>
 __global__ void __launch_bounds__(kThreads) grouped_gemm_f64_kernel(const GemmProblem* __restrict__ probs, int nprob,
                                                                     const int* __restrict__ tile_first,
                                                                     int total_tiles, int* __restrict__ ticket) {
+  constexpr int WM = BM / 16, WN = BN / 16;  // m8n8 blocks per warp (2x2 warps)
+  constexpr int LA = BM * BK / kThreads, LB = BN * BK / kThreads;
   // ticket == nullptr: static round-robin over work items; otherwise a device
   // work queue (one atomic ticket per item) balances uneven problem sizes.
   __shared__ double As[2][BM][BK + kPad];
@@ -47,7 +58,7 @@ __global__ void __launch_bounds__(kThreads) grouped_gemm_f64_kernel(const GemmPr
   __shared__ int s_tile;
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
-  const int wm = warp >> 1, wn = warp & 1;  // 2x2 warps, 32x32 each
+  const int wm = warp >> 1, wn = warp & 1;  // 2x2 warps
 
   for (int iter = 0;; ++iter) {
     if (ticket) {
@@ -71,31 +82,40 @@ __global__ void __launch_bounds__(kThreads) grouped_gemm_f64_kernel(const GemmPr
     const int kbeg = kc * p.kchunk;
     const int kend = min(p.k, kbeg + p.kchunk);
 
-    double acc[4][4][2];
+    double acc[WM][WN][2];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < WM; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
+      for (int j = 0; j < WN; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
 
-    // register staging: each thread loads 8 A and 8 B elements per K step
-    double ra[8], rb[8];
+    // register staging: each thread loads LA elements of A and LB of B per K step
+    double ra[LA], rb[LB];
     auto load_regs = [&](int k0) {
 #pragma unroll
-      for (int r = 0; r < 8; ++r) {
-        int e = tid + r * kThreads;  // 0..1023 over a 64 x 16 tile
+      for (int r = 0; r < LA; ++r) {
+        int e = tid + r * kThreads;
         int row = e / BK, col = e % BK;
-        int gm = m0 + row, gk = k0 + col, gn = n0 + row;
+        int gm = m0 + row, gk = k0 + col;
         ra[r] = (gm < p.m && gk < kend) ? __ldg(p.A + (int64_t)gm * p.a_rs + (int64_t)gk * p.a_cs) : 0.0;
+      }
+#pragma unroll
+      for (int r = 0; r < LB; ++r) {
+        int e = tid + r * kThreads;
+        int row = e / BK, col = e % BK;
+        int gn = n0 + row, gk = k0 + col;
         rb[r] = (gn < p.n && gk < kend) ? __ldg(p.B + (int64_t)gn * p.b_rs + (int64_t)gk * p.b_cs) : 0.0;
       }
     };
     auto store_regs = [&](int buf) {
 #pragma unroll
-      for (int r = 0; r < 8; ++r) {
+      for (int r = 0; r < LA; ++r) {
         int e = tid + r * kThreads;
-        int row = e / BK, col = e % BK;
-        As[buf][row][col] = ra[r];
-        Bs[buf][row][col] = rb[r];
+        As[buf][e / BK][e % BK] = ra[r];
+      }
+#pragma unroll
+      for (int r = 0; r < LB; ++r) {
+        int e = tid + r * kThreads;
+        Bs[buf][e / BK][e % BK] = rb[r];
       }
     };
 
@@ -110,15 +130,15 @@ __global__ void __launch_bounds__(kThreads) grouped_gemm_f64_kernel(const GemmPr
       if (kt + 1 < nk) load_regs(kbeg + (kt + 1) * BK);
 #pragma unroll
       for (int k4 = 0; k4 < BK; k4 += 4) {
-        double af[4], bf[4];
+        double af[WM], bf[WN];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) af[i] = As[buf][wm * 32 + i * 8 + (lane >> 2)][k4 + (lane & 3)];
+        for (int i = 0; i < WM; ++i) af[i] = As[buf][wm * (BM / 2) + i * 8 + (lane >> 2)][k4 + (lane & 3)];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) bf[j] = Bs[buf][wn * 32 + j * 8 + (lane >> 2)][k4 + (lane & 3)];
+        for (int j = 0; j < WN; ++j) bf[j] = Bs[buf][wn * (BN / 2) + j * 8 + (lane >> 2)][k4 + (lane & 3)];
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < WM; ++i)
 #pragma unroll
-          for (int j = 0; j < 4; ++j) dmma884(acc[i][j], af[i], bf[j]);
+          for (int j = 0; j < WN; ++j) dmma884(acc[i][j], af[i], bf[j]);
       }
       if (kt + 1 < nk) store_regs(buf ^ 1);
       __syncthreads();
@@ -127,14 +147,14 @@ __global__ void __launch_bounds__(kThreads) grouped_gemm_f64_kernel(const GemmPr
     // epilogue: C (+)= alpha * acc, or the raw partial of this K range
     double* part = p.partial ? p.partial + (int64_t)kc * p.m * p.n : nullptr;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int gm = m0 + wm * 32 + i * 8 + (lane >> 2);
+    for (int i = 0; i < WM; ++i) {
+      const int gm = m0 + wm * (BM / 2) + i * 8 + (lane >> 2);
       if (gm >= p.m) continue;
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
+      for (int j = 0; j < WN; ++j) {
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-          const int gn = n0 + wn * 32 + j * 8 + (lane & 3) * 2 + h;
+          const int gn = n0 + wn * (BN / 2) + j * 8 + (lane & 3) * 2 + h;
           if (gn >= p.n) continue;
           if (part) {
             part[(int64_t)gm * p.n + gn] = acc[i][j][h];
@@ -181,19 +201,21 @@ void F64Gemm::release() {
     if (!q) return;
     if (async_stream_set) cudaFreeAsync(q, async_stream); else cudaFree(q);
   };
-  fr(d_probs);
-  fr(d_first);
-  fr(d_ticket);
+  for (auto& sb : subs) {
+    fr(sb.d_probs);
+    fr(sb.d_first);
+    fr(sb.d_ticket);
+  }
+  subs.clear();
+  fr(d_all);
   fr(d_partial);
   fr(d_red_prob);
   fr(d_red_first);
-  d_probs = nullptr;
-  d_first = nullptr;
-  d_ticket = nullptr;
+  d_all = nullptr;
   d_partial = nullptr;
   d_red_prob = nullptr;
   d_red_first = nullptr;
-  total_tiles = nprob = nred = 0;
+  nprob = nred = 0;
   red_chunks = 0;
 }
 
@@ -210,14 +232,11 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
   int64_t out_tiles = 0;
   for (auto& q : probs) out_tiles += f64_tiles(q.m, q.n);
   int64_t part_elems = 0;
-  std::vector<int> first(nprob);
   std::vector<int> red;
   std::vector<uint32_t> red_first;
-  int64_t tiles = 0;
   uint64_t rc = 0;
   for (int i = 0; i < nprob; ++i) {
     GemmProblem& q = probs[i];
-    int t = f64_tiles(q.m, q.n);
     int ks = 1;
     if (out_tiles < kFillTiles && q.k > 2 * kMinChunk) {
       int want = (int)((kFillTiles + out_tiles - 1) / out_tiles);
@@ -229,7 +248,7 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
     q.ksplit = ks;
     q.kchunk = std::max(chunk, BK);
     q.partial = nullptr;
-    q.pad_ = 0;
+    q.pad_ = f64_variant(q.m, q.n);
     if (ks > 1) {
       q.partial = (double*)(intptr_t)(part_elems + 1);  // offset + 1, patched below
       part_elems += (int64_t)ks * q.m * q.n;
@@ -237,11 +256,7 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
       red_first.push_back((uint32_t)rc);
       rc += ((uint64_t)q.m * q.n + kRedChunk - 1) / kRedChunk;
     }
-    first[i] = (int)tiles;
-    tiles += (int64_t)t * ks;
   }
-  if (tiles >= (1ll << 31)) return fail(GBX_EUNSUPPORTED, "grouped GEMM has too many work items");
-  total_tiles = (int)tiles;
   nred = (int)red.size();
   red_chunks = (uint32_t)rc;
   auto alloc = [&](void** q, size_t bytes) -> int {
@@ -264,12 +279,33 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
   GBX_TRY(alloc((void**)&d_partial, sizeof(double) * part_elems));
   for (auto& q : probs)
     if (q.partial) q.partial = d_partial + ((intptr_t)q.partial - 1);
-  GBX_TRY(alloc((void**)&d_probs, sizeof(GemmProblem) * nprob));
-  GBX_TRY(alloc((void**)&d_first, sizeof(int) * nprob));
-  GBX_TRY(alloc((void**)&d_ticket, sizeof(int)));
-  GBX_TRY(copy(d_probs, probs.data(), sizeof(GemmProblem) * nprob));
-  GBX_TRY(copy(d_first, first.data(), sizeof(int) * nprob));
+  // one launch per tile shape
+  for (int v = 0; v < 4; ++v) {
+    std::vector<GemmProblem> vp;
+    std::vector<int> first;
+    int64_t tiles = 0;
+    for (auto& q : probs) {
+      if (q.pad_ != v) continue;
+      vp.push_back(q);
+      first.push_back((int)tiles);
+      tiles += (int64_t)f64_tiles(q.m, q.n) * q.ksplit;
+    }
+    if (vp.empty()) continue;
+    if (tiles >= (1ll << 31)) return fail(GBX_EUNSUPPORTED, "grouped GEMM has too many work items");
+    Sub sb;
+    sb.variant = v;
+    sb.nprob = (int)vp.size();
+    sb.total_tiles = (int)tiles;
+    GBX_TRY(alloc((void**)&sb.d_probs, sizeof(GemmProblem) * vp.size()));
+    GBX_TRY(alloc((void**)&sb.d_first, sizeof(int) * vp.size()));
+    GBX_TRY(alloc((void**)&sb.d_ticket, sizeof(int)));
+    GBX_TRY(copy(sb.d_probs, vp.data(), sizeof(GemmProblem) * vp.size()));
+    GBX_TRY(copy(sb.d_first, first.data(), sizeof(int) * vp.size()));
+    subs.push_back(sb);
+  }
   if (nred) {
+    GBX_TRY(alloc((void**)&d_all, sizeof(GemmProblem) * nprob));
+    GBX_TRY(copy(d_all, probs.data(), sizeof(GemmProblem) * nprob));
     GBX_TRY(alloc((void**)&d_red_prob, sizeof(int) * nred));
     GBX_TRY(alloc((void**)&d_red_first, sizeof(uint32_t) * nred));
     GBX_TRY(copy(d_red_prob, red.data(), sizeof(int) * nred));
@@ -280,14 +316,33 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
 }
 
 int F64Gemm::run(cudaStream_t st) const {
-  if (nprob == 0 || total_tiles == 0) return GBX_OK;
-  GBX_CUDA(cudaMemsetAsync(d_ticket, 0, sizeof(int), st));
-  int grid = std::min(total_tiles, 152 * 4);
-  grouped_gemm_f64_kernel<<<grid, kThreads, 0, st>>>(d_probs, nprob, d_first, total_tiles, d_ticket);
-  GBX_CUDA(cudaGetLastError());
+  if (nprob == 0) return GBX_OK;
+  for (const Sub& sb : subs) {
+    GBX_CUDA(cudaMemsetAsync(sb.d_ticket, 0, sizeof(int), st));
+    int grid = std::min(sb.total_tiles, 152 * 4);
+    switch (sb.variant) {
+      case 0:
+        grouped_gemm_f64_kernel<64, 64><<<grid, kThreads, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first, sb.total_tiles,
+                                                                   sb.d_ticket);
+        break;
+      case 1:
+        grouped_gemm_f64_kernel<64, 16><<<grid, kThreads, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first, sb.total_tiles,
+                                                                   sb.d_ticket);
+        break;
+      case 2:
+        grouped_gemm_f64_kernel<16, 64><<<grid, kThreads, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first, sb.total_tiles,
+                                                                   sb.d_ticket);
+        break;
+      default:
+        grouped_gemm_f64_kernel<16, 16><<<grid, kThreads, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first, sb.total_tiles,
+                                                                   sb.d_ticket);
+        break;
+    }
+    GBX_CUDA(cudaGetLastError());
+  }
   if (nred) {
     int rg = (int)std::min<uint32_t>(red_chunks, 152u * 8u);
-    splitk_reduce_kernel<<<rg, kRedThreads, 0, st>>>(d_probs, d_red_prob, d_red_first, nred, red_chunks);
+    splitk_reduce_kernel<<<rg, kRedThreads, 0, st>>>(d_all, d_red_prob, d_red_first, nred, red_chunks);
     GBX_CUDA(cudaGetLastError());
   }
   return GBX_OK;

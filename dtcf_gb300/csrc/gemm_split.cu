@@ -60,7 +60,7 @@ struct SplitRowSet {   // one operand of one problem for the split kernel
   __nv_bfloat16* dst;  // slice 0, row 0
   int64_t slice_stride, Kp;
   int* exps;
-  int64_t first_row;   // prefix over all row sets
+  int64_t first_row;   // first (row, K chunk) work item of this set
 };
 
 struct DevProblem {
@@ -398,13 +398,14 @@ __global__ void __launch_bounds__(kThreads, 1) split_gemm_kernel(const GemmParam
       if (!ok) break;
       const int row = m0 + row_in_tile;
       if (row < pr.M) {
-        const int ea = pr.eA[row];
+        const int ea = pr.eA[row];  // 0 only for an all-zero row, whose acc is 0
         double* crow = pr.ksplit > 1 ? pr.partial + ((int64_t)ti.kc * pr.M + row) * pr.N : pr.C + (int64_t)row * pr.ldc;
 #pragma unroll
         for (int j = 0; j < BN; ++j) {
           const int col = n0 + j;
           if (col < pr.N) {
-            int ex = ea + pr.eB[col] - 14 + 1023;
+            // exps are biased row exponents E; the row scale is 2^(E - 1022)
+            int ex = ea + pr.eB[col] - 2 * 1022 - 14 + 1023;
             ex = ex < 1 ? 1 : (ex > 2046 ? 2046 : ex);
             crow[col] = acc[j] * __longlong_as_double((long long)ex << 52);
           }
@@ -442,48 +443,84 @@ __global__ void __launch_bounds__(256) split_reduce_kernel(const DevProblem* __r
   }
 }
 
-// FP64 rows -> S bf16 digit slices + row exponents (integer arithmetic only).
-__global__ void __launch_bounds__(256) split_rows_kernel(const SplitRowSet* __restrict__ sets, int nsets,
-                                                         int64_t total_rows, int S) {
-  const int64_t row_g = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (row_g >= total_rows) return;
+// Splitting runs in two passes over (row, K chunk) work items so that rows
+// with very long K spread over the whole GPU.  Pass 1 takes the largest biased
+// exponent of each row chunk and folds it into the row with atomicMax (exact,
+// order independent); pass 2 writes the digits.
+constexpr int kSplitChunk = 2048;
+
+__device__ __forceinline__ void locate_chunk(const SplitRowSet* __restrict__ sets, int nsets, int64_t chunk,
+                                             int& set, int64_t& row, int64_t& k0) {
   int lo = 0, hi = nsets - 1;
   while (lo < hi) {
     int mid = (lo + hi + 1) >> 1;
-    if (sets[mid].first_row <= row_g) lo = mid; else hi = mid - 1;
+    if (sets[mid].first_row <= chunk) lo = mid; else hi = mid - 1;
   }
+  set = lo;
   const SplitRowSet& rs = sets[lo];
-  const int64_t row = row_g - rs.first_row;
-  const double* src = rs.src + row * rs.K;
-  // row maximum of |x| as the largest biased exponent of a normal number
-  uint32_t emax = 0;
-  for (int64_t k = lane; k < rs.K; k += 32) {
-    uint32_t e = (uint32_t)((__double_as_longlong(__ldg(src + k)) >> 52) & 0x7FF);
-    emax = max(emax, e);
+  const int64_t per_row = (rs.K + kSplitChunk - 1) / kSplitChunk;
+  const int64_t local = chunk - rs.first_row;
+  row = local / per_row;
+  k0 = (local - row * per_row) * kSplitChunk;
+}
+
+__global__ void __launch_bounds__(256) row_exponent_kernel(const SplitRowSet* __restrict__ sets, int nsets,
+                                                           int64_t total_chunks) {
+  __shared__ uint32_t red[8];
+  for (int64_t chunk = blockIdx.x; chunk < total_chunks; chunk += gridDim.x) {
+    int set;
+    int64_t row, k0;
+    locate_chunk(sets, nsets, chunk, set, row, k0);
+    const SplitRowSet& rs = sets[set];
+    const double* src = rs.src + row * rs.K;
+    const int64_t k1 = min(rs.K, k0 + kSplitChunk);
+    uint32_t emax = 0;
+    for (int64_t k = k0 + threadIdx.x; k < k1; k += 256)
+      emax = max(emax, (uint32_t)((__double_as_longlong(__ldg(src + k)) >> 52) & 0x7FF));
+    for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = emax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t m = 0;
+      for (int w = 0; w < 8; ++w) m = max(m, red[w]);
+      if (m) atomicMax((unsigned int*)(rs.exps + row), m);
+    }
+    __syncthreads();
   }
-  for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
-  if (lane == 0) rs.exps[row] = emax == 0 ? 0 : (int)emax - 1022;
+}
+
+// exps hold the largest biased exponent of each row (0 for an all-zero row).
+__global__ void __launch_bounds__(256) digits_kernel(const SplitRowSet* __restrict__ sets, int nsets,
+                                                     int64_t total_chunks, int S) {
   const int F = 7 + 8 * (S - 1);
-  __nv_bfloat16* dst = rs.dst + row * rs.Kp;
-  for (int64_t k = lane; k < rs.K; k += 32) {
-    const long long bits = __double_as_longlong(__ldg(src + k));
-    const uint32_t e = (uint32_t)((bits >> 52) & 0x7FF);
-    long long X = 0;
-    if (e != 0 && emax != 0) {
-      const long long mant = (bits & 0xFFFFFFFFFFFFFll) | (1ll << 52);
-      const int sh = 53 + (int)(emax - e) - F;  // X = mant * 2^-sh, rounded
-      if (sh <= 0) X = mant << (-sh);
-      else if (sh < 63) X = (mant + (1ll << (sh - 1))) >> sh;
-      if (bits < 0) X = -X;
+  for (int64_t chunk = blockIdx.x; chunk < total_chunks; chunk += gridDim.x) {
+    int set;
+    int64_t row, k0;
+    locate_chunk(sets, nsets, chunk, set, row, k0);
+    const SplitRowSet& rs = sets[set];
+    const double* src = rs.src + row * rs.K;
+    __nv_bfloat16* dst = rs.dst + row * rs.Kp;
+    const uint32_t emax = (uint32_t)rs.exps[row];
+    const int64_t k1 = min(rs.K, k0 + kSplitChunk);
+    for (int64_t k = k0 + threadIdx.x; k < k1; k += 256) {
+      const long long bits = __double_as_longlong(__ldg(src + k));
+      const uint32_t e = (uint32_t)((bits >> 52) & 0x7FF);
+      long long X = 0;
+      if (e != 0 && emax != 0) {
+        const long long mant = (bits & 0xFFFFFFFFFFFFFll) | (1ll << 52);
+        const int sh = 53 + (int)(emax - e) - F;  // X = mant * 2^-sh, rounded half up
+        if (sh <= 0) X = mant << (-sh);
+        else if (sh < 63) X = (mant + (1ll << (sh - 1))) >> sh;
+        if (bits < 0) X = -X;
+      }
+      // balanced base-256 digits, least significant first
+      for (int s = S - 1; s >= 1; --s) {
+        const long long d = ((X + 128) & 255) - 128;
+        X = (X - d) >> 8;
+        dst[s * rs.slice_stride + k] = __int2bfloat16_rn((int)d);
+      }
+      dst[k] = __int2bfloat16_rn((int)X);
     }
-    // balanced base-256 digits, least significant first
-    for (int s = S - 1; s >= 1; --s) {
-      const long long d = ((X + 128) & 255) - 128;
-      X = (X - d) >> 8;
-      dst[s * rs.slice_stride + k] = __int2bfloat16_rn((int)d);
-    }
-    dst[k] = __int2bfloat16_rn((int)X);
   }
 }
 
@@ -492,7 +529,7 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
   if (!fn) {
     cudaDriverEntryPointQueryResult q;
     void* p = nullptr;
-    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
       fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
   }
@@ -525,7 +562,8 @@ struct SplitPlan {
   SplitRowSet* d_sets_a = nullptr;  // rows from the plan's packed A
   SplitRowSet* d_sets_b = nullptr;  // rows from the plan's packed B
   int nsets = 0;
-  int64_t rows_a = 0, rows_b = 0;
+  int64_t rows_a = 0, rows_b = 0;  // (row, K chunk) work items per side
+  std::vector<std::pair<void*, size_t>> exp_ranges_a, exp_ranges_b;  // exponent words reset before a split
   DevProblem* d_probs = nullptr;
   int* d_tile_first = nullptr;
   CUtensorMap* d_maps = nullptr;
@@ -609,11 +647,13 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
     SplitRowSet& to_a = p.a_is_plan_b ? b : a;  // rows that come from plan A
     SplitRowSet& to_b = p.a_is_plan_b ? a : b;
     to_a.first_row = ra;
-    ra += to_a.rows;
+    ra += to_a.rows * ((to_a.K + kSplitChunk - 1) / kSplitChunk);
     to_b.first_row = rb;
-    rb += to_b.rows;
+    rb += to_b.rows * ((to_b.K + kSplitChunk - 1) / kSplitChunk);
     sa.push_back(to_a);
     sb.push_back(to_b);
+    sp->exp_ranges_a.push_back({(void*)to_a.exps, sizeof(int) * (size_t)to_a.rows});
+    sp->exp_ranges_b.push_back({(void*)to_b.exps, sizeof(int) * (size_t)to_b.rows});
     DevProblem d;
     d.M = (int)p.M;
     d.N = (int)p.N;
@@ -690,12 +730,17 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
 
 int split_operands(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st) {
   if (!sp || sp->nsets == 0) return GBX_OK;
-  if (plan_a && sp->rows_a > 0) {
-    split_rows_kernel<<<(unsigned)((sp->rows_a + 7) / 8), 256, 0, st>>>(sp->d_sets_a, sp->nsets, sp->rows_a, sp->S);
+  for (int side = 0; side < 2; ++side) {
+    if ((side == 0 && !plan_a) || (side == 1 && !plan_b)) continue;
+    const int64_t chunks = side == 0 ? sp->rows_a : sp->rows_b;
+    if (chunks == 0) continue;
+    const SplitRowSet* sets = side == 0 ? sp->d_sets_a : sp->d_sets_b;
+    for (auto& z : (side == 0 ? sp->exp_ranges_a : sp->exp_ranges_b))
+      GBX_CUDA(cudaMemsetAsync(z.first, 0, z.second, st));
+    const int grid = (int)std::min<int64_t>(chunks, 152 * 16);
+    row_exponent_kernel<<<grid, 256, 0, st>>>(sets, sp->nsets, chunks);
     GBX_CUDA(cudaGetLastError());
-  }
-  if (plan_b && sp->rows_b > 0) {
-    split_rows_kernel<<<(unsigned)((sp->rows_b + 7) / 8), 256, 0, st>>>(sp->d_sets_b, sp->nsets, sp->rows_b, sp->S);
+    digits_kernel<<<grid, 256, 0, st>>>(sets, sp->nsets, chunks, sp->S);
     GBX_CUDA(cudaGetLastError());
   }
   return GBX_OK;
