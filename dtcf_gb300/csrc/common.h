@@ -134,6 +134,7 @@ struct F64Gemm {
 };
 // Tile shapes shared by the host planner and the kernels.
 int f64_variant(int m, int n);
+int f64_variant(int m, int n, int k);
 int f64_tile_m(int variant);
 int f64_tile_n(int variant);
 int f64_tiles(int m, int n);

@@ -27,16 +27,72 @@ constexpr int kFillTiles = 152 * 3;   // work items that keep every SM busy
 constexpr int kMinChunk = 256;        // smallest K range of a split
 constexpr int kRedThreads = 256;
 constexpr int kRedChunk = 2048;
+constexpr int kThinN = 32, kThinK = 64;
 }  // namespace
 
 // Tile shapes: 64x64 for large problems, 64x16 / 16x64 / 16x16 for skinny ones
 // (output dimensions below 48), so small outputs do not waste the FP64 pipe.
+// Thin problems (one output dimension <= 32 and K <= 64) run on CUDA-core
+// FP64 with exact shapes: variant 4 = one thread per row of C (N thin),
+// variant 5 = one thread per column (M thin).
+int f64_variant(int m, int n, int k) {
+  if (k <= kThinK && n <= kThinN && m >= 4 * n) return 4;
+  if (k <= kThinK && m <= kThinN && n >= 4 * m) return 5;
+  return (m < 48 ? 2 : 0) + (n < 48 ? 1 : 0);
+}
 int f64_variant(int m, int n) { return (m < 48 ? 2 : 0) + (n < 48 ? 1 : 0); }
 int f64_tile_m(int variant) { return (variant & 2) ? 16 : 64; }
 int f64_tile_n(int variant) { return (variant & 1) ? 16 : 64; }
 int f64_tiles(int m, int n) {
   const int v = f64_variant(m, n), tm = f64_tile_m(v), tn = f64_tile_n(v);
   return ((m + tm - 1) / tm) * ((n + tn - 1) / tn);
+}
+
+// One thread per row (variant 4) or per column (variant 5) of C; the thin
+// operand (at most kThinN x kThinK) sits in shared memory.  Each output is a
+// k-ordered FMA chain, so results are deterministic.
+template <bool kRows>
+__global__ void __launch_bounds__(256) thin_gemm_f64_kernel(const GemmProblem* __restrict__ probs, int nprob,
+                                                            const int* __restrict__ block_first, int total_blocks) {
+  __shared__ double Ts[kThinN * kThinK];
+  for (int blk = blockIdx.x; blk < total_blocks; blk += gridDim.x) {
+    int lo = 0, hi = nprob - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (block_first[mid] <= blk) lo = mid; else hi = mid - 1;
+    }
+    const GemmProblem& p = probs[lo];
+    const int64_t i0 = (int64_t)(blk - block_first[lo]) * 256;
+    // thin operand: B (N x K) for row mode, A (M x K) for column mode
+    const int tn = kRows ? p.n : p.m;
+    const double* T = kRows ? p.B : p.A;
+    const int64_t trs = kRows ? p.b_rs : p.a_rs, tcs = kRows ? p.b_cs : p.a_cs;
+    __syncthreads();
+    for (int e = threadIdx.x; e < tn * p.k; e += 256) Ts[e] = __ldg(T + (int64_t)(e / p.k) * trs + (int64_t)(e % p.k) * tcs);
+    __syncthreads();
+    const int64_t i = i0 + threadIdx.x;
+    const int64_t wide = kRows ? p.m : p.n;
+    if (i < wide) {
+      const double* W = kRows ? p.A + i * p.a_rs : p.B + i * p.b_rs;
+      const int64_t wcs = kRows ? p.a_cs : p.b_cs;
+      double acc[kThinN];
+#pragma unroll
+      for (int j = 0; j < kThinN; ++j) acc[j] = 0.0;
+      for (int k = 0; k < p.k; ++k) {
+        const double w = __ldg(W + k * wcs);
+#pragma unroll
+        for (int j = 0; j < kThinN; ++j)
+          if (j < tn) acc[j] = fma(w, Ts[j * p.k + k], acc[j]);
+      }
+#pragma unroll
+      for (int j = 0; j < kThinN; ++j) {
+        if (j >= tn) break;
+        double* c = kRows ? p.C + i * p.c_rs + j : p.C + (int64_t)j * p.c_rs + i;
+        const double v = __dmul_rn(p.alpha, acc[j]);
+        *c = p.accumulate ? __dadd_rn(*c, v) : v;
+      }
+    }
+  }
 }
 
 __device__ __forceinline__ void dmma884(double (&c)[2], double a, double b) {
@@ -238,6 +294,14 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
   for (int i = 0; i < nprob; ++i) {
     GemmProblem& q = probs[i];
     int ks = 1;
+    const int thin = f64_variant(q.m, q.n, q.k);
+    if (thin >= 4) {
+      q.ksplit = 1;
+      q.kchunk = std::max(q.k, BK);
+      q.partial = nullptr;
+      q.pad_ = thin;
+      continue;
+    }
     if (out_tiles < kFillTiles && q.k > 2 * kMinChunk) {
       int want = (int)((kFillTiles + out_tiles - 1) / out_tiles);
       ks = std::max(1, std::min(want, (q.k + kMinChunk - 1) / kMinChunk));
@@ -280,7 +344,7 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
   for (auto& q : probs)
     if (q.partial) q.partial = d_partial + ((intptr_t)q.partial - 1);
   // one launch per tile shape
-  for (int v = 0; v < 4; ++v) {
+  for (int v = 0; v < 6; ++v) {
     std::vector<GemmProblem> vp;
     std::vector<int> first;
     int64_t tiles = 0;
@@ -288,7 +352,9 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
       if (q.pad_ != v) continue;
       vp.push_back(q);
       first.push_back((int)tiles);
-      tiles += (int64_t)f64_tiles(q.m, q.n) * q.ksplit;
+      if (v == 4) tiles += (q.m + 255) / 256;
+      else if (v == 5) tiles += (q.n + 255) / 256;
+      else tiles += (int64_t)f64_tiles(q.m, q.n) * q.ksplit;
     }
     if (vp.empty()) continue;
     if (tiles >= (1ll << 31)) return fail(GBX_EUNSUPPORTED, "grouped GEMM has too many work items");
@@ -333,9 +399,17 @@ int F64Gemm::run(cudaStream_t st) const {
         grouped_gemm_f64_kernel<16, 64><<<grid, kThreads, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first, sb.total_tiles,
                                                                    sb.d_ticket);
         break;
-      default:
+      case 3:
         grouped_gemm_f64_kernel<16, 16><<<grid, kThreads, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first, sb.total_tiles,
                                                                    sb.d_ticket);
+        break;
+      case 4:
+        thin_gemm_f64_kernel<true><<<std::min(sb.total_tiles, 152 * 8), 256, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first,
+                                                                                      sb.total_tiles);
+        break;
+      default:
+        thin_gemm_f64_kernel<false><<<std::min(sb.total_tiles, 152 * 8), 256, 0, st>>>(sb.d_probs, sb.nprob,
+                                                                                       sb.d_first, sb.total_tiles);
         break;
     }
     GBX_CUDA(cudaGetLastError());

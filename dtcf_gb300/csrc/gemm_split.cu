@@ -448,6 +448,7 @@ __global__ void __launch_bounds__(256) split_reduce_kernel(const DevProblem* __r
 // exponent of each row chunk and folds it into the row with atomicMax (exact,
 // order independent); pass 2 writes the digits.
 constexpr int kSplitChunk = 2048;
+constexpr int64_t kShortRow = 1024;  // rows up to this length: one warp per row, both passes fused
 
 __device__ __forceinline__ void locate_chunk(const SplitRowSet* __restrict__ sets, int nsets, int64_t chunk,
                                              int& set, int64_t& row, int64_t& k0) {
@@ -524,6 +525,48 @@ __global__ void __launch_bounds__(256) digits_kernel(const SplitRowSet* __restri
   }
 }
 
+// Short rows: one warp handles a whole row (exponent by warp shuffles, then
+// the digits); the row sets here carry first_row in rows.
+__global__ void __launch_bounds__(256) split_short_rows_kernel(const SplitRowSet* __restrict__ sets, int nsets,
+                                                               int64_t total_rows, int S) {
+  const int F = 7 + 8 * (S - 1);
+  const int lane = threadIdx.x & 31;
+  for (int64_t rg = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5); rg < total_rows; rg += (int64_t)gridDim.x * 8) {
+    int lo = 0, hi = nsets - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (sets[mid].first_row <= rg) lo = mid; else hi = mid - 1;
+    }
+    const SplitRowSet& rs = sets[lo];
+    const int64_t row = rg - rs.first_row;
+    const double* src = rs.src + row * rs.K;
+    uint32_t emax = 0;
+    for (int64_t k = lane; k < rs.K; k += 32)
+      emax = max(emax, (uint32_t)((__double_as_longlong(__ldg(src + k)) >> 52) & 0x7FF));
+    for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+    if (lane == 0) rs.exps[row] = (int)emax;
+    __nv_bfloat16* dst = rs.dst + row * rs.Kp;
+    for (int64_t k = lane; k < rs.K; k += 32) {
+      const long long bits = __double_as_longlong(__ldg(src + k));
+      const uint32_t e = (uint32_t)((bits >> 52) & 0x7FF);
+      long long X = 0;
+      if (e != 0 && emax != 0) {
+        const long long mant = (bits & 0xFFFFFFFFFFFFFll) | (1ll << 52);
+        const int sh = 53 + (int)(emax - e) - F;
+        if (sh <= 0) X = mant << (-sh);
+        else if (sh < 63) X = (mant + (1ll << (sh - 1))) >> sh;
+        if (bits < 0) X = -X;
+      }
+      for (int s = S - 1; s >= 1; --s) {
+        const long long d = ((X + 128) & 255) - 128;
+        X = (X - d) >> 8;
+        dst[s * rs.slice_stride + k] = __int2bfloat16_rn((int)d);
+      }
+      dst[k] = __int2bfloat16_rn((int)X);
+    }
+  }
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   if (!fn) {
@@ -559,8 +602,12 @@ struct SplitPlan {
   std::vector<SplitProblem> host;
   __nv_bfloat16* d_slices = nullptr;  // all A and B slices
   int* d_exps = nullptr;
-  SplitRowSet* d_sets_a = nullptr;  // rows from the plan's packed A
-  SplitRowSet* d_sets_b = nullptr;  // rows from the plan's packed B
+  SplitRowSet* d_sets_a = nullptr;  // long rows from the plan's packed A
+  SplitRowSet* d_sets_b = nullptr;  // long rows from the plan's packed B
+  SplitRowSet* d_short_a = nullptr;  // short rows (first_row counts rows)
+  SplitRowSet* d_short_b = nullptr;
+  int nlong_a = 0, nlong_b = 0, nshort_a = 0, nshort_b = 0;
+  int64_t short_rows_a = 0, short_rows_b = 0;
   int nsets = 0;
   int64_t rows_a = 0, rows_b = 0;  // (row, K chunk) work items per side
   std::vector<std::pair<void*, size_t>> exp_ranges_a, exp_ranges_b;  // exponent words reset before a split
@@ -583,6 +630,8 @@ struct SplitPlan {
     dev_free(d_exps);
     dev_free(d_sets_a);
     dev_free(d_sets_b);
+    dev_free(d_short_a);
+    dev_free(d_short_b);
     dev_free(d_probs);
     dev_free(d_tile_first);
     dev_free(d_maps);
@@ -625,7 +674,8 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
   GBX_CUDA(cudaMemset(sp->d_slices, 0, sizeof(__nv_bfloat16) * std::max<int64_t>(slice_elems, 1)));
   GBX_CUDA(cudaMemset(sp->d_exps, 0, sizeof(int) * std::max<int64_t>(exp_elems, 1)));
   sp->bytes = 2.0 * slice_elems + 4.0 * exp_elems;
-  std::vector<SplitRowSet> sa, sb;
+  std::vector<SplitRowSet> sa, sb, ssa, ssb;
+  int64_t sra = 0, srb = 0;
   std::vector<DevProblem> dp;
   std::vector<int> first;
   std::vector<CUtensorMap> maps;
@@ -646,14 +696,26 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
     SplitRowSet b{p.B, p.N, p.K, sp->d_slices + o.b, o.Np * o.Kp, o.Kp, sp->d_exps + o.eb, 0};
     SplitRowSet& to_a = p.a_is_plan_b ? b : a;  // rows that come from plan A
     SplitRowSet& to_b = p.a_is_plan_b ? a : b;
-    to_a.first_row = ra;
-    ra += to_a.rows * ((to_a.K + kSplitChunk - 1) / kSplitChunk);
-    to_b.first_row = rb;
-    rb += to_b.rows * ((to_b.K + kSplitChunk - 1) / kSplitChunk);
-    sa.push_back(to_a);
-    sb.push_back(to_b);
-    sp->exp_ranges_a.push_back({(void*)to_a.exps, sizeof(int) * (size_t)to_a.rows});
-    sp->exp_ranges_b.push_back({(void*)to_b.exps, sizeof(int) * (size_t)to_b.rows});
+    if (to_a.K <= kShortRow) {
+      to_a.first_row = sra;
+      sra += to_a.rows;
+      ssa.push_back(to_a);
+    } else {
+      to_a.first_row = ra;
+      ra += to_a.rows * ((to_a.K + kSplitChunk - 1) / kSplitChunk);
+      sa.push_back(to_a);
+    }
+    if (to_b.K <= kShortRow) {
+      to_b.first_row = srb;
+      srb += to_b.rows;
+      ssb.push_back(to_b);
+    } else {
+      to_b.first_row = rb;
+      rb += to_b.rows * ((to_b.K + kSplitChunk - 1) / kSplitChunk);
+      sb.push_back(to_b);
+    }
+    if (to_a.K > kShortRow) sp->exp_ranges_a.push_back({(void*)to_a.exps, sizeof(int) * (size_t)to_a.rows});
+    if (to_b.K > kShortRow) sp->exp_ranges_b.push_back({(void*)to_b.exps, sizeof(int) * (size_t)to_b.rows});
     DevProblem d;
     d.M = (int)p.M;
     d.N = (int)p.N;
@@ -709,15 +771,27 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
   sp->nsets = (int)probs.size();
   sp->rows_a = ra;
   sp->rows_b = rb;
+  sp->short_rows_a = sra;
+  sp->short_rows_b = srb;
+  sp->nlong_a = (int)sa.size();
+  sp->nlong_b = (int)sb.size();
+  sp->nshort_a = (int)ssa.size();
+  sp->nshort_b = (int)ssb.size();
   sp->total_tiles = tiles;
-  GBX_TRY(dev_alloc((void**)&sp->d_sets_a, sizeof(SplitRowSet) * sp->nsets));
-  GBX_TRY(dev_alloc((void**)&sp->d_sets_b, sizeof(SplitRowSet) * sp->nsets));
+  auto up_sets = [&](const std::vector<SplitRowSet>& v, SplitRowSet** d) -> int {
+    if (v.empty()) return GBX_OK;
+    GBX_TRY(dev_alloc((void**)d, sizeof(SplitRowSet) * v.size()));
+    GBX_CUDA(cudaMemcpy(*d, v.data(), sizeof(SplitRowSet) * v.size(), cudaMemcpyHostToDevice));
+    return GBX_OK;
+  };
+  GBX_TRY(up_sets(sa, &sp->d_sets_a));
+  GBX_TRY(up_sets(sb, &sp->d_sets_b));
+  GBX_TRY(up_sets(ssa, &sp->d_short_a));
+  GBX_TRY(up_sets(ssb, &sp->d_short_b));
   GBX_TRY(dev_alloc((void**)&sp->d_probs, sizeof(DevProblem) * sp->nsets));
   GBX_TRY(dev_alloc((void**)&sp->d_tile_first, sizeof(int) * sp->nsets));
   GBX_TRY(dev_alloc((void**)&sp->d_maps, sizeof(CUtensorMap) * maps.size()));
   GBX_TRY(dev_alloc((void**)&sp->d_err, sizeof(int)));
-  GBX_CUDA(cudaMemcpy(sp->d_sets_a, sa.data(), sizeof(SplitRowSet) * sp->nsets, cudaMemcpyHostToDevice));
-  GBX_CUDA(cudaMemcpy(sp->d_sets_b, sb.data(), sizeof(SplitRowSet) * sp->nsets, cudaMemcpyHostToDevice));
   GBX_CUDA(cudaMemcpy(sp->d_probs, dp.data(), sizeof(DevProblem) * sp->nsets, cudaMemcpyHostToDevice));
   GBX_CUDA(cudaMemcpy(sp->d_tile_first, first.data(), sizeof(int) * sp->nsets, cudaMemcpyHostToDevice));
   GBX_CUDA(cudaMemcpy(sp->d_maps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice));
@@ -733,15 +807,25 @@ int split_operands(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st) {
   for (int side = 0; side < 2; ++side) {
     if ((side == 0 && !plan_a) || (side == 1 && !plan_b)) continue;
     const int64_t chunks = side == 0 ? sp->rows_a : sp->rows_b;
-    if (chunks == 0) continue;
-    const SplitRowSet* sets = side == 0 ? sp->d_sets_a : sp->d_sets_b;
-    for (auto& z : (side == 0 ? sp->exp_ranges_a : sp->exp_ranges_b))
-      GBX_CUDA(cudaMemsetAsync(z.first, 0, z.second, st));
-    const int grid = (int)std::min<int64_t>(chunks, 152 * 16);
-    row_exponent_kernel<<<grid, 256, 0, st>>>(sets, sp->nsets, chunks);
-    GBX_CUDA(cudaGetLastError());
-    digits_kernel<<<grid, 256, 0, st>>>(sets, sp->nsets, chunks, sp->S);
-    GBX_CUDA(cudaGetLastError());
+    if (chunks > 0) {
+      const SplitRowSet* sets = side == 0 ? sp->d_sets_a : sp->d_sets_b;
+      const int nsets = side == 0 ? sp->nlong_a : sp->nlong_b;
+      for (auto& z : (side == 0 ? sp->exp_ranges_a : sp->exp_ranges_b))
+        GBX_CUDA(cudaMemsetAsync(z.first, 0, z.second, st));
+      const int grid = (int)std::min<int64_t>(chunks, 152 * 16);
+      row_exponent_kernel<<<grid, 256, 0, st>>>(sets, nsets, chunks);
+      GBX_CUDA(cudaGetLastError());
+      digits_kernel<<<grid, 256, 0, st>>>(sets, nsets, chunks, sp->S);
+      GBX_CUDA(cudaGetLastError());
+    }
+    const int64_t srows = side == 0 ? sp->short_rows_a : sp->short_rows_b;
+    if (srows > 0) {
+      const SplitRowSet* sets = side == 0 ? sp->d_short_a : sp->d_short_b;
+      const int nsets = side == 0 ? sp->nshort_a : sp->nshort_b;
+      const int grid = (int)std::min<int64_t>((srows + 7) / 8, 152 * 32);
+      split_short_rows_kernel<<<grid, 256, 0, st>>>(sets, nsets, srows, sp->S);
+      GBX_CUDA(cudaGetLastError());
+    }
   }
   return GBX_OK;
 }

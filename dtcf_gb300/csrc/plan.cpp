@@ -249,8 +249,10 @@ void choose_engine(GroupBlock& g, bool split_engine, bool split_all, int slices)
   const double kp = up(g.K, 64);
   const double t_split = 2.0 * pairs * up(g.M, 128) * up(g.N, 64) * kp / 1.0e15;
   const double t_split_sw = 2.0 * pairs * up(g.N, 128) * up(g.M, 64) * kp / 1.0e15;
-  const int v = f64_variant((int)std::min<int64_t>(g.M, 1 << 30), (int)std::min<int64_t>(g.N, 1 << 30));
-  const double t_f64 = 2.0 * up(g.M, f64_tile_m(v)) * up(g.N, f64_tile_n(v)) * up(g.K, 16) / 0.95e12;
+  const int mi = (int)std::min<int64_t>(g.M, 1 << 30), ni = (int)std::min<int64_t>(g.N, 1 << 30);
+  const int v = f64_variant(mi, ni, (int)std::min<int64_t>(g.K, 1 << 30));
+  const double t_f64 = v >= 4 ? 2.0 * (double)g.M * (double)g.N * (double)g.K / 0.9e12 + 2e-6
+                              : 2.0 * up(g.M, f64_tile_m(v)) * up(g.N, f64_tile_n(v)) * up(g.K, 16) / 0.95e12;
   const double best_split = std::min(t_split, t_split_sw) + 4e-6;  // + split and launch overhead
   if (split_all || best_split < t_f64) {
     g.engine = 1;

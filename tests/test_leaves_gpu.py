@@ -198,3 +198,15 @@ def test_rrr_plan_split_engine(gbx, sign):
     assert np.max(np.abs(got - want)) <= 1e-13 * np.abs(want).max()
     # the unique-block flop count of this contraction (o=16, v=48, block 8)
     assert ctr.plan("a,b,e,f", "e,f,i,j", "a,b,i,j").flops == 2.0 * 63 * 4096 * 2304
+
+
+@pytest.mark.parametrize("m,n,k", [(5000, 6, 30), (7, 3000, 20), (300, 32, 64), (40, 33, 64), (2000, 1, 1)])
+def test_grouped_gemm_thin_shapes(gbx, m, n, k):
+    """Thin problems (one output side <= 32, K <= 64) take the exact-shape
+    CUDA-core FP64 path; results match numpy to FP64 rounding."""
+    from dtcf_gb300.leaves import Triple
+    rng = np.random.default_rng(m + n + k)
+    A, B, C = rng.standard_normal((m, k)), rng.standard_normal((n, k)), rng.standard_normal((m, n))
+    dA, dB, dC = dev(A), dev(B), dev(C)
+    gbx.grouped_gemm_f64([Triple(dA.data_ptr(), dB.data_ptr(), dC.data_ptr(), k, 1, k, 1, n, m, n, k, -2.0, 1)])
+    np.testing.assert_allclose(host(dC).reshape(m, n), C - 2.0 * A @ B.T, rtol=1e-12, atol=1e-12)
