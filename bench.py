@@ -33,7 +33,8 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gbx", choices=["gbx", "reference"])
-    p.add_argument("--engine", default="auto", choices=["auto", "split", "fp64"])
+    p.add_argument("--engine", default="auto", choices=["auto", "split", "fp64"],
+                   help="auto: split path timed, FP64 path timed beside it; split / fp64: that path only")
     p.add_argument("--nocc", type=int, default=48)
     p.add_argument("--nvir", type=int, default=240)
     p.add_argument("--nirrep", type=int, default=8)
@@ -166,9 +167,7 @@ def main():
 
     common = dict(nocc=a.nocc, nvir=a.nvir, nirrep=a.nirrep, max_block=a.max_block, min_block=a.min_block,
                   seed=a.seed, method="ccsd", slices=a.slices)
-    engines = ["fp64"]
-    if a.engine in ("auto", "split"):
-        engines = ["split", "fp64"]
+    engines = {"auto": ["split", "fp64"], "split": ["split"], "fp64": ["fp64"]}[a.engine]
     stream = torch.cuda.current_stream()
 
     def time_job(job, steps, warmup):
@@ -192,7 +191,7 @@ def main():
         try:
             job = Job(engine=eng, **common)
         except Exception as ex:  # split engine unavailable in this build
-            if eng == "split" and a.engine == "auto":
+            if eng == "split" and a.engine == "auto":  # noqa: SIM102
                 print("split engine unavailable: %s" % ex, file=sys.stderr)
                 continue
             raise
