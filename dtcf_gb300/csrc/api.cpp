@@ -88,6 +88,8 @@ int gbx_split_gemm(const double* d_A, const double* d_B, double* d_C, int64_t M,
   return rc;
 }
 
+int gbx_split_set_width(int width) { return split_set_width(width); }
+
 int gbx_plan_destroy(gbx_plan* plan) {
   delete plan;
   return GBX_OK;

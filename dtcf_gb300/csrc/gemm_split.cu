@@ -46,11 +46,10 @@ namespace {
 
 constexpr int BM = 128;
 constexpr int BK = 64;             // bf16 elements per 128-byte swizzled row
-constexpr int kStages = 5;
 constexpr int kAcc = 2;            // TMEM accumulator buffers
 constexpr int kChunkKb = 16;       // k-blocks per exact FP32 chunk (16 * 64 = 1024)
 constexpr int kFoldChunks = 127;   // int32 drain sums fold into FP64 before overflow
-constexpr int kThreads = 192;
+
 constexpr long long kWaitCycles = 2000000000ll;  // ~1 s at 2 GHz
 constexpr int kSplitFill = 152 * 2;  // work items that keep every SM busy
 
@@ -200,36 +199,54 @@ __device__ __forceinline__ int level_pairs(int l, int S) {
 }
 
 template <int BN>
-struct Smem {
-  alignas(1024) __nv_bfloat16 a[kStages][BM * BK];
-  alignas(1024) __nv_bfloat16 b[kStages][BN * BK];
-  uint64_t full[kStages], empty[kStages], accfull[kAcc], accempty[kAcc], done;
-  uint32_t tmem_base;
+struct SplitCfg {
+  static constexpr int kStageBytes = (BM + BN) * BK * 2;
+  static constexpr int kStages = (200 * 1024 / kStageBytes) < 8 ? (200 * 1024 / kStageBytes) : 8;
+  static constexpr uint32_t kTmemCols = (2 * BN <= 32) ? 32 : (2 * BN <= 64) ? 64 : (2 * BN <= 128) ? 128
+                                        : (2 * BN <= 256) ? 256 : 512;
+  // drain warps: 4 per 64 columns (one per TMEM lane quarter), at least 4
+  static constexpr int kDrainWarps = BN >= 64 ? 4 * (BN / 64) : 4;
+  static constexpr int kCols = BN >= 64 ? 64 : BN;  // columns per drain thread
+  static constexpr int kThreads = 64 + 32 * kDrainWarps;
 };
 
 template <int BN>
-__global__ void __launch_bounds__(kThreads, 1) split_gemm_kernel(const GemmParams P) {
+struct Smem {
+  alignas(1024) __nv_bfloat16 a[SplitCfg<BN>::kStages][BM * BK];
+  alignas(1024) __nv_bfloat16 b[SplitCfg<BN>::kStages][BN * BK];
+  uint64_t full[SplitCfg<BN>::kStages], empty[SplitCfg<BN>::kStages], accfull[kAcc], accempty[kAcc], done;
+  uint32_t tmem_base;
+};
+
+// Warp roles: 0 TMA producer, 1 TMEM owner + MMA issuer, 2.. drain.  A drain
+// thread owns one row (its TMEM lane) and up to 64 columns; its exact int32 sums
+// fold into an FP64 Horner accumulator kept in the output tile itself (or the
+// split-K partial), which stays in L2 between the few folds of a tile.
+template <int BN>
+__global__ void __launch_bounds__(SplitCfg<BN>::kThreads, 1) split_gemm_kernel(const GemmParams P) {
+  using Cfg = SplitCfg<BN>;
+  constexpr int kStagesN = Cfg::kStages;
+  constexpr int kCols = Cfg::kCols;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   Smem<BN>& sm = *reinterpret_cast<Smem<BN>*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   constexpr uint32_t kTxBytes = (BM + BN) * BK * 2;
-  constexpr uint32_t kTmemCols = (kAcc * BN < 32) ? 32 : kAcc * BN;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages; ++s) {
+    for (int s = 0; s < kStagesN; ++s) {
       mbar_init(&sm.full[s], 1);
       mbar_init(&sm.empty[s], 1);
     }
     for (int b = 0; b < kAcc; ++b) {
       mbar_init(&sm.accfull[b], 1);
-      mbar_init(&sm.accempty[b], 4);
+      mbar_init(&sm.accempty[b], Cfg::kDrainWarps);
     }
     mbar_init(&sm.done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm.tmem_base)),
-                 "r"(kTmemCols));
+                 "r"(Cfg::kTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   tc_fence_before();
@@ -246,7 +263,6 @@ __global__ void __launch_bounds__(kThreads, 1) split_gemm_kernel(const GemmParam
       bool ok = true;
       for (int tile = blockIdx.x; tile < P.total_tiles && ok; tile += gridDim.x) {
         const TileInfo ti = decode_tile<BN>(P, tile);
-        const int m0 = ti.m0, n0 = ti.n0;
         const CUtensorMap* ma = P.maps + 2 * ti.p;
         const CUtensorMap* mb = P.maps + 2 * ti.p + 1;
         for (int l = L; l >= 0 && ok; --l)
@@ -258,9 +274,9 @@ __global__ void __launch_bounds__(kThreads, 1) split_gemm_kernel(const GemmParam
                 break;
               }
               mbar_expect_tx(&sm.full[stage], kTxBytes);
-              tma_load_3d(sm.a[stage], ma, &sm.full[stage], kb * BK, m0, s - 1);
-              tma_load_3d(sm.b[stage], mb, &sm.full[stage], kb * BK, n0, t - 1);
-              if (++stage == kStages) {
+              tma_load_3d(sm.a[stage], ma, &sm.full[stage], kb * BK, ti.m0, s - 1);
+              tma_load_3d(sm.b[stage], mb, &sm.full[stage], kb * BK, ti.n0, t - 1);
+              if (++stage == kStagesN) {
                 stage = 0;
                 phase ^= 1;
               }
@@ -268,12 +284,11 @@ __global__ void __launch_bounds__(kThreads, 1) split_gemm_kernel(const GemmParam
           }
       }
       // wait (bounded) for the copies this warp issued to land before leaving
-      for (int i = 0; i < kStages; ++i) {
+      for (int i = 0; i < kStagesN; ++i) {
         if (--stage < 0) {
-          stage = kStages - 1;
+          stage = kStagesN - 1;
           phase ^= 1;
         }
-        // stage was last filled with parity `phase`; completion flips it
         long long t0 = clock64();
         while (!mbar_try_wait(&sm.full[stage], phase) && !mbar_try_wait(&sm.empty[stage], phase)) {
           if (clock64() - t0 > kWaitCycles) {
@@ -314,7 +329,7 @@ __global__ void __launch_bounds__(kThreads, 1) split_gemm_kernel(const GemmParam
               for (int k = 0; k < BK / 16; ++k)
                 umma(d, a0 + (uint64_t)(k * 2), b0 + (uint64_t)(k * 2), idesc, (in_chunk > 0 || k > 0) ? 1u : 0u);
               umma_commit(&sm.empty[stage]);
-              if (++stage == kStages) {
+              if (++stage == kStagesN) {
                 stage = 0;
                 phase ^= 1;
               }
@@ -334,31 +349,34 @@ __global__ void __launch_bounds__(kThreads, 1) split_gemm_kernel(const GemmParam
       mbar_wait(&sm.done, 0, P.err, 6);
     }
   } else {
-    // ---------------- drain / epilogue (warps 2..5) ----------------
+    // ---------------- drain / fold (warps 2..) ----------------
     const int quarter = warp & 3;
+    const int group = (warp - 2) >> 2;
     const int row_in_tile = quarter * 32 + lane;
     const uint32_t lane_addr = (uint32_t)(quarter * 32) << 16;
+    const int col0 = group * kCols;
     int buf = 0;
     uint32_t aphase = 0;
     bool ok = true;
     for (int tile = blockIdx.x; tile < P.total_tiles && ok; tile += gridDim.x) {
       const TileInfo ti = decode_tile<BN>(P, tile);
       const DevProblem& pr = P.probs[ti.p];
-      const int m0 = ti.m0, n0 = ti.n0;
-      double acc[BN];
-      int32_t X[BN];
-#pragma unroll
-      for (int j = 0; j < BN; ++j) {
-        acc[j] = 0.0;
-        X[j] = 0;
+      const int row = ti.m0 + row_in_tile;
+      const bool row_ok = row < pr.M;
+      double* crow = nullptr;
+      double scale[1] = {0.0};
+      if (row_ok) {
+        crow = pr.ksplit > 1 ? pr.partial + ((int64_t)ti.kc * pr.M + row) * pr.N : pr.C + (int64_t)row * pr.ldc;
+        scale[0] = (double)pr.eA[row];  // biased row exponent, combined per column below
       }
-      for (int l = L; l >= 0 && ok; --l) {
-        if (l != L) {
+      int32_t X[kCols];
 #pragma unroll
-          for (int j = 0; j < BN; ++j) acc[j] *= 0x1.0p-8;  // exact
-        }
+      for (int j = 0; j < kCols; ++j) X[j] = 0;
+      bool first_fold = true;
+      for (int l = L; l >= 0 && ok; --l) {
         const int items = level_pairs(l, S) * ti.nkb;
         const int chunks = (items + kChunkKb - 1) / kChunkKb;
+        bool scale_pending = l != L;  // Horner: acc = acc * 2^-8 + X_l at the first fold of level l
         int since_fold = 0;
         for (int c = 0; c < chunks; ++c) {
           // one lane waits, the warp follows (tcgen05.ld must stay warp-uniform)
@@ -371,9 +389,9 @@ __global__ void __launch_bounds__(kThreads, 1) split_gemm_kernel(const GemmParam
           __syncwarp();
           tc_fence_after();
 #pragma unroll
-          for (int j0 = 0; j0 < BN; j0 += 16) {
+          for (int j0 = 0; j0 < kCols; j0 += 16) {
             uint32_t r[16];
-            tmem_ld16(tmem + lane_addr + (uint32_t)(buf * BN + j0), r);
+            tmem_ld16(tmem + lane_addr + (uint32_t)(buf * BN + col0 + j0), r);
             tmem_wait_ld();
 #pragma unroll
             for (int q = 0; q < 16; ++q) X[j0 + q] += __float2int_rn(__uint_as_float(r[q]));
@@ -385,29 +403,31 @@ __global__ void __launch_bounds__(kThreads, 1) split_gemm_kernel(const GemmParam
             buf = 0;
             aphase ^= 1;
           }
+          const bool last = (l == 0 && c == chunks - 1);
           if (++since_fold == kFoldChunks || c == chunks - 1) {
+            if (row_ok) {
 #pragma unroll
-            for (int j = 0; j < BN; ++j) {
-              acc[j] += (double)X[j];
-              X[j] = 0;
+              for (int j = 0; j < kCols; ++j) {
+                const int col = ti.n0 + col0 + j;
+                if (col < pr.N) {
+                  double acc = first_fold ? 0.0 : crow[col];
+                  if (scale_pending) acc *= 0x1.0p-8;  // exact
+                  acc += (double)X[j];
+                  if (last) {
+                    // row scale 2^(eA - 1022), column 2^(eB - 1022), digit weights 2^-14
+                    int ex = (int)scale[0] + pr.eB[col] - 2 * 1022 - 14 + 1023;
+                    ex = ex < 1 ? 1 : (ex > 2046 ? 2046 : ex);
+                    acc *= __longlong_as_double((long long)ex << 52);
+                  }
+                  crow[col] = acc;
+                }
+              }
             }
-            since_fold = 0;
-          }
-        }
-      }
-      if (!ok) break;
-      const int row = m0 + row_in_tile;
-      if (row < pr.M) {
-        const int ea = pr.eA[row];  // 0 only for an all-zero row, whose acc is 0
-        double* crow = pr.ksplit > 1 ? pr.partial + ((int64_t)ti.kc * pr.M + row) * pr.N : pr.C + (int64_t)row * pr.ldc;
 #pragma unroll
-        for (int j = 0; j < BN; ++j) {
-          const int col = n0 + j;
-          if (col < pr.N) {
-            // exps are biased row exponents E; the row scale is 2^(E - 1022)
-            int ex = ea + pr.eB[col] - 2 * 1022 - 14 + 1023;
-            ex = ex < 1 ? 1 : (ex > 2046 ? 2046 : ex);
-            crow[col] = acc[j] * __longlong_as_double((long long)ex << 52);
+            for (int j = 0; j < kCols; ++j) X[j] = 0;
+            first_fold = false;
+            scale_pending = false;
+            since_fold = 0;
           }
         }
       }
@@ -418,7 +438,7 @@ __global__ void __launch_bounds__(kThreads, 1) split_gemm_kernel(const GemmParam
   if (warp == 1) {
     __syncwarp();
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Cfg::kTmemCols));
   }
 }
 
@@ -595,11 +615,45 @@ int encode_slices(CUtensorMap* map, const __nv_bfloat16* base, int64_t S, int64_
 
 }  // namespace
 
-constexpr int kBN = 64;
+// Output tile width per problem: the smallest modelled time over the
+// instantiated widths.  A k-block costs the largest of: tensor 2.72 * BN
+// cycles (128 x BN x 64 MACs at ~3000 MAC/clk), shared-memory reads
+// (16 KB of A + BN * 128 B of B at 128 B/clk) and L2 -> SM traffic (same
+// bytes at ~76 B/clk per SM).  The 256 width spills a little and is de-rated.
+// gbx_split_set_width() overrides the choice (tuning).
+constexpr int kWidths[4] = {32, 64, 128, 256};
+static int g_width_override = 0;
+
+int choose_width(int64_t N) {
+  if (g_width_override) return g_width_override;
+  int best = 256;
+  double best_cost = 1e300;
+  for (int bn : kWidths) {
+    const double tiles = (double)((N + bn - 1) / bn);
+    const double bytes = 16384.0 + 128.0 * bn;
+    double per_kb = std::max(std::max(2.72 * bn, 128.0 + bn), bytes / 76.0);
+    if (bn == 256) per_kb *= 1.15;
+    const double cost = tiles * per_kb;
+    if (cost < best_cost * 0.999) {
+      best_cost = cost;
+      best = bn;
+    }
+  }
+  return best;
+}
+
+struct SplitLaunch {  // the problems of one output tile width
+  int bn = 0;
+  DevProblem* d_probs = nullptr;
+  int* d_tile_first = nullptr;
+  CUtensorMap* d_maps = nullptr;
+  int nprob = 0, total_tiles = 0;
+};
 
 struct SplitPlan {
   int S = 0, L = 0;
   std::vector<SplitProblem> host;
+  std::vector<int> width;  // per problem
   __nv_bfloat16* d_slices = nullptr;  // all A and B slices
   int* d_exps = nullptr;
   SplitRowSet* d_sets_a = nullptr;  // long rows from the plan's packed A
@@ -611,16 +665,14 @@ struct SplitPlan {
   int nsets = 0;
   int64_t rows_a = 0, rows_b = 0;  // (row, K chunk) work items per side
   std::vector<std::pair<void*, size_t>> exp_ranges_a, exp_ranges_b;  // exponent words reset before a split
-  DevProblem* d_probs = nullptr;
-  int* d_tile_first = nullptr;
-  CUtensorMap* d_maps = nullptr;
+  std::vector<SplitLaunch> launches;
+  DevProblem* d_all = nullptr;  // every problem, for the split-K reduction
   int* d_err = nullptr;
   double* d_partial = nullptr;
   int* d_red_prob = nullptr;
   int64_t* d_red_first = nullptr;
   int nred = 0;
   int64_t red_total = 0;
-  int total_tiles = 0;
   double bytes = 0.0;
   ~SplitPlan() {
     dev_free(d_partial);
@@ -632,12 +684,22 @@ struct SplitPlan {
     dev_free(d_sets_b);
     dev_free(d_short_a);
     dev_free(d_short_b);
-    dev_free(d_probs);
-    dev_free(d_tile_first);
-    dev_free(d_maps);
+    dev_free(d_all);
+    for (auto& l : launches) {
+      dev_free(l.d_probs);
+      dev_free(l.d_tile_first);
+      dev_free(l.d_maps);
+    }
     dev_free(d_err);
   }
 };
+
+template <int BN>
+int set_smem_attr() {
+  const size_t smem = sizeof(Smem<BN>) + 1024;
+  GBX_CUDA(cudaFuncSetAttribute(split_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  return GBX_OK;
+}
 
 int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitPlan** out) {
   *out = nullptr;
@@ -655,9 +717,11 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
   for (auto& p : probs) {
     if (p.M <= 0 || p.N <= 0 || p.K <= 0) return fail(GBX_EINVAL, "empty split problem");
     if (p.M >= (1ll << 30) || p.N >= (1ll << 30) || p.K >= (1ll << 30)) return fail(GBX_EUNSUPPORTED, "split problem too large");
+    const int bn = choose_width(p.N);
+    sp->width.push_back(bn);
     Off o;
     o.Mp = (p.M + BM - 1) / BM * BM;
-    o.Np = (p.N + kBN - 1) / kBN * kBN;
+    o.Np = (p.N + bn - 1) / bn * bn;
     o.Kp = (p.K + BK - 1) / BK * BK;
     o.a = slice_elems;
     slice_elems += S * o.Mp * o.Kp;
@@ -677,12 +741,10 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
   std::vector<SplitRowSet> sa, sb, ssa, ssb;
   int64_t sra = 0, srb = 0;
   std::vector<DevProblem> dp;
-  std::vector<int> first;
   std::vector<CUtensorMap> maps;
   int64_t ra = 0, rb = 0;
-  int tiles = 0;
   int64_t out_tiles = 0;
-  for (size_t i = 0; i < probs.size(); ++i) out_tiles += (offs[i].Mp / BM) * (offs[i].Np / kBN);
+  for (size_t i = 0; i < probs.size(); ++i) out_tiles += (offs[i].Mp / BM) * (offs[i].Np / sp->width[i]);
   int64_t part_elems = 0;
   std::vector<int> red;
   std::vector<int64_t> red_first;
@@ -690,6 +752,7 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
   for (size_t i = 0; i < probs.size(); ++i) {
     const SplitProblem& p = probs[i];
     const Off& o = offs[i];
+    const int bn = sp->width[i];
     // row sets are grouped by the plan operand they come from, so constant
     // plan operands can be split once
     SplitRowSet a{p.A, p.M, p.K, sp->d_slices + o.a, o.Mp * o.Kp, o.Kp, sp->d_exps + o.ea, 0};
@@ -704,6 +767,7 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
       to_a.first_row = ra;
       ra += to_a.rows * ((to_a.K + kSplitChunk - 1) / kSplitChunk);
       sa.push_back(to_a);
+      sp->exp_ranges_a.push_back({(void*)to_a.exps, sizeof(int) * (size_t)to_a.rows});
     }
     if (to_b.K <= kShortRow) {
       to_b.first_row = srb;
@@ -713,16 +777,15 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
       to_b.first_row = rb;
       rb += to_b.rows * ((to_b.K + kSplitChunk - 1) / kSplitChunk);
       sb.push_back(to_b);
+      sp->exp_ranges_b.push_back({(void*)to_b.exps, sizeof(int) * (size_t)to_b.rows});
     }
-    if (to_a.K > kShortRow) sp->exp_ranges_a.push_back({(void*)to_a.exps, sizeof(int) * (size_t)to_a.rows});
-    if (to_b.K > kShortRow) sp->exp_ranges_b.push_back({(void*)to_b.exps, sizeof(int) * (size_t)to_b.rows});
     DevProblem d;
     d.M = (int)p.M;
     d.N = (int)p.N;
     d.K = (int)p.K;
     d.nkb = (int)(o.Kp / BK);
     d.tiles_m = (int)(o.Mp / BM);
-    d.tiles_n = (int)(o.Np / kBN);
+    d.tiles_n = (int)(o.Np / bn);
     // split K when the output tiles of all problems leave SMs idle; ranges are
     // whole exact-accumulation chunks
     int ks = 1;
@@ -748,11 +811,9 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
     }
     d.ldc = p.N;
     dp.push_back(d);
-    first.push_back(tiles);
-    tiles += d.tiles_m * d.tiles_n * ks;
     CUtensorMap ma, mb;
     GBX_TRY(encode_slices(&ma, sp->d_slices + o.a, S, o.Mp, o.Kp, BM));
-    GBX_TRY(encode_slices(&mb, sp->d_slices + o.b, S, o.Np, o.Kp, kBN));
+    GBX_TRY(encode_slices(&mb, sp->d_slices + o.b, S, o.Np, o.Kp, bn));
     maps.push_back(ma);
     maps.push_back(mb);
   }
@@ -777,27 +838,47 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
   sp->nlong_b = (int)sb.size();
   sp->nshort_a = (int)ssa.size();
   sp->nshort_b = (int)ssb.size();
-  sp->total_tiles = tiles;
-  auto up_sets = [&](const std::vector<SplitRowSet>& v, SplitRowSet** d) -> int {
-    if (v.empty()) return GBX_OK;
-    GBX_TRY(dev_alloc((void**)d, sizeof(SplitRowSet) * v.size()));
-    GBX_CUDA(cudaMemcpy(*d, v.data(), sizeof(SplitRowSet) * v.size(), cudaMemcpyHostToDevice));
+  auto up = [&](const void* h, size_t bytes, void** d) -> int {
+    if (bytes == 0) return GBX_OK;
+    GBX_TRY(dev_alloc(d, bytes));
+    GBX_CUDA(cudaMemcpy(*d, h, bytes, cudaMemcpyHostToDevice));
     return GBX_OK;
   };
-  GBX_TRY(up_sets(sa, &sp->d_sets_a));
-  GBX_TRY(up_sets(sb, &sp->d_sets_b));
-  GBX_TRY(up_sets(ssa, &sp->d_short_a));
-  GBX_TRY(up_sets(ssb, &sp->d_short_b));
-  GBX_TRY(dev_alloc((void**)&sp->d_probs, sizeof(DevProblem) * sp->nsets));
-  GBX_TRY(dev_alloc((void**)&sp->d_tile_first, sizeof(int) * sp->nsets));
-  GBX_TRY(dev_alloc((void**)&sp->d_maps, sizeof(CUtensorMap) * maps.size()));
+  GBX_TRY(up(sa.data(), sizeof(SplitRowSet) * sa.size(), (void**)&sp->d_sets_a));
+  GBX_TRY(up(sb.data(), sizeof(SplitRowSet) * sb.size(), (void**)&sp->d_sets_b));
+  GBX_TRY(up(ssa.data(), sizeof(SplitRowSet) * ssa.size(), (void**)&sp->d_short_a));
+  GBX_TRY(up(ssb.data(), sizeof(SplitRowSet) * ssb.size(), (void**)&sp->d_short_b));
+  GBX_TRY(up(dp.data(), sizeof(DevProblem) * dp.size(), (void**)&sp->d_all));
+  // one launch per output tile width
+  for (int bn : kWidths) {
+    std::vector<DevProblem> lp;
+    std::vector<CUtensorMap> lm;
+    std::vector<int> first;
+    int tiles = 0;
+    for (size_t i = 0; i < probs.size(); ++i) {
+      if (sp->width[i] != bn) continue;
+      lp.push_back(dp[i]);
+      lm.push_back(maps[2 * i]);
+      lm.push_back(maps[2 * i + 1]);
+      first.push_back(tiles);
+      tiles += dp[i].tiles_m * dp[i].tiles_n * dp[i].ksplit;
+    }
+    if (lp.empty()) continue;
+    SplitLaunch L;
+    L.bn = bn;
+    L.nprob = (int)lp.size();
+    L.total_tiles = tiles;
+    GBX_TRY(up(lp.data(), sizeof(DevProblem) * lp.size(), (void**)&L.d_probs));
+    GBX_TRY(up(first.data(), sizeof(int) * first.size(), (void**)&L.d_tile_first));
+    GBX_TRY(up(lm.data(), sizeof(CUtensorMap) * lm.size(), (void**)&L.d_maps));
+    sp->launches.push_back(L);
+  }
   GBX_TRY(dev_alloc((void**)&sp->d_err, sizeof(int)));
-  GBX_CUDA(cudaMemcpy(sp->d_probs, dp.data(), sizeof(DevProblem) * sp->nsets, cudaMemcpyHostToDevice));
-  GBX_CUDA(cudaMemcpy(sp->d_tile_first, first.data(), sizeof(int) * sp->nsets, cudaMemcpyHostToDevice));
-  GBX_CUDA(cudaMemcpy(sp->d_maps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice));
   GBX_CUDA(cudaMemset(sp->d_err, 0, sizeof(int)));
-  size_t smem = sizeof(Smem<kBN>) + 1024;
-  GBX_CUDA(cudaFuncSetAttribute(split_gemm_kernel<kBN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  GBX_TRY(set_smem_attr<32>());
+  GBX_TRY(set_smem_attr<64>());
+  GBX_TRY(set_smem_attr<128>());
+  GBX_TRY(set_smem_attr<256>());
   *out = sp.release();
   return GBX_OK;
 }
@@ -830,29 +911,40 @@ int split_operands(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st) {
   return GBX_OK;
 }
 
-int run_split_plan(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st) {
-  if (!sp || sp->nsets == 0) return GBX_OK;
-  GBX_TRY(split_operands(sp, plan_a, plan_b, st));
-  if (sp->total_tiles == 0) return GBX_OK;
+template <int BN>
+int launch_width(const SplitPlan* sp, const SplitLaunch& L, int nsm, cudaStream_t st) {
   GemmParams P;
-  P.probs = sp->d_probs;
-  P.tile_first = sp->d_tile_first;
-  P.maps = sp->d_maps;
-  P.nprob = sp->nsets;
-  P.total_tiles = sp->total_tiles;
+  P.probs = L.d_probs;
+  P.tile_first = L.d_tile_first;
+  P.maps = L.d_maps;
+  P.nprob = L.nprob;
+  P.total_tiles = L.total_tiles;
   P.S = sp->S;
   P.L = sp->L;
   P.err = sp->d_err;
+  const int grid = std::min(L.total_tiles, nsm);
+  split_gemm_kernel<BN><<<grid, SplitCfg<BN>::kThreads, sizeof(Smem<BN>) + 1024, st>>>(P);
+  GBX_CUDA(cudaGetLastError());
+  return GBX_OK;
+}
+
+int run_split_plan(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st) {
+  if (!sp || sp->nsets == 0) return GBX_OK;
+  GBX_TRY(split_operands(sp, plan_a, plan_b, st));
   int dev = 0, nsm = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  int grid = std::min(sp->total_tiles, nsm);
-  size_t smem = sizeof(Smem<kBN>) + 1024;
-  split_gemm_kernel<kBN><<<grid, kThreads, smem, st>>>(P);
-  GBX_CUDA(cudaGetLastError());
+  for (const SplitLaunch& L : sp->launches) {
+    switch (L.bn) {
+      case 32: GBX_TRY(launch_width<32>(sp, L, nsm, st)); break;
+      case 64: GBX_TRY(launch_width<64>(sp, L, nsm, st)); break;
+      case 128: GBX_TRY(launch_width<128>(sp, L, nsm, st)); break;
+      default: GBX_TRY(launch_width<256>(sp, L, nsm, st)); break;
+    }
+  }
   if (sp->nred > 0) {
     int rg = (int)std::min<int64_t>((sp->red_total + 255) / 256, 152 * 8);
-    split_reduce_kernel<<<rg, 256, 0, st>>>(sp->d_probs, sp->d_red_prob, sp->d_red_first, sp->nred, sp->red_total);
+    split_reduce_kernel<<<rg, 256, 0, st>>>(sp->d_all, sp->d_red_prob, sp->d_red_first, sp->nred, sp->red_total);
     GBX_CUDA(cudaGetLastError());
   }
   return GBX_OK;
@@ -869,8 +961,10 @@ double split_plan_tensor_flops(const SplitPlan* sp) {
   if (!sp) return 0.0;
   double f = 0.0;
   const double pairs = sp->S * (sp->S + 1) / 2.0;
-  for (auto& p : sp->host) {
-    double Mp = (double)((p.M + BM - 1) / BM * BM), Np = (double)((p.N + kBN - 1) / kBN * kBN);
+  for (size_t i = 0; i < sp->host.size(); ++i) {
+    const SplitProblem& p = sp->host[i];
+    const int bn = sp->width[i];
+    double Mp = (double)((p.M + BM - 1) / BM * BM), Np = (double)((p.N + bn - 1) / bn * bn);
     double Kp = (double)((p.K + BK - 1) / BK * BK);
     f += 2.0 * pairs * Mp * Np * Kp;
   }
@@ -878,6 +972,12 @@ double split_plan_tensor_flops(const SplitPlan* sp) {
 }
 
 void destroy_split_plan(SplitPlan* sp) { delete sp; }
+
+int split_set_width(int bn) {
+  if (bn != 0 && bn != 32 && bn != 64 && bn != 128 && bn != 256) return fail(GBX_EINVAL, "width must be 0, 32, 64, 128 or 256");
+  g_width_override = bn;
+  return GBX_OK;
+}
 
 double split_plan_bytes(const SplitPlan* sp) { return sp ? sp->bytes : 0.0; }
 

@@ -29,6 +29,8 @@ int run_split_plan(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st);
 // Only the split kernels (for operands that stay constant afterwards).
 int split_operands(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st);
 void destroy_split_plan(SplitPlan* sp);
+// Force the output tile width of plans created afterwards (0 = model).
+int split_set_width(int bn);
 double split_plan_bytes(const SplitPlan* sp);
 // bf16 tensor flops one run issues (S(S+1)/2 slice products on padded tiles).
 double split_plan_tensor_flops(const SplitPlan* sp);

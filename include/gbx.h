@@ -151,6 +151,11 @@ GBX_API int gbx_plan_destroy(gbx_plan* plan);
 GBX_API int gbx_split_gemm(const double* d_A, const double* d_B, double* d_C, int64_t M, int64_t N, int64_t K,
                            int slices, void* stream);
 
+/* Tuning knob of the split engine: output tile width (32, 64, 128 or 256
+ * columns) for plans created after the call; 0 restores the built-in
+ * throughput model.  Process-wide; used by the autotuner. */
+GBX_API int gbx_split_set_width(int width);
+
 /* ---- grouped block GEMM ------------------------------------------------- */
 
 /* One block triple: C[m x n] (+)= alpha * A[m x k] * B[n x k]^T with element

@@ -40,3 +40,23 @@ def test_split_gemm_random_fp64(slices, tol):
     got = C.cpu().numpy()
     err = np.linalg.norm(got - want) / np.linalg.norm(want)
     assert err < tol, err
+
+
+@pytest.mark.parametrize("width", [32, 64, 128, 256])
+@pytest.mark.parametrize("M,N,K", [(300, 270, 2100), (129, 33, 70)])
+def test_split_gemm_exact_every_tile_width(width, M, N, K):
+    """Every output tile width of the split kernel (forced through the tuning
+    knob) gives the exact integer product."""
+    import dtcf_gb300
+    from dtcf_gb300._lib import lib
+    rng = np.random.default_rng(M * N + K + width)
+    A = rng.integers(-(1 << 20), 1 << 20, size=(M, K)).astype(np.float64)
+    B = rng.integers(-(1 << 20), 1 << 20, size=(N, K)).astype(np.float64)
+    want = (A.astype(np.int64) @ B.astype(np.int64).T).astype(np.float64)
+    C = torch.zeros((M, N), dtype=torch.float64, device="cuda")
+    assert lib().gbx_split_set_width(width) == 0
+    try:
+        dtcf_gb300.split_gemm(dev(A), dev(B), C, slices=6)
+    finally:
+        lib().gbx_split_set_width(0)
+    assert np.array_equal(C.cpu().numpy(), want)
