@@ -22,12 +22,12 @@
 // (acc = acc * 2^-8 + X, levels from S - 1 down to 0), and writes
 // 2^(e_i + f_j - 14) * acc.  Only the fold and the final scale are FP64.
 //
-// Kernel roles (one CTA per SM, persistent over 128 x BN output tiles of
-// all problems): warp 0 issues TMA loads into a ring of shared-memory stages,
-// warp 1 allocates TMEM and issues the MMAs (one elected lane), warps 2..5
-// drain the accumulators (each owns one 32-lane TMEM quarter, i.e. 32 rows).
-// Two TMEM accumulator buffers let the drain of one chunk overlap the MMAs of
-// the next.  Every mbarrier wait is bounded (about a second); on timeout the
+// Kernel roles (one or two CTAs per SM, persistent over 128 x BN output
+// tiles of all problems): warp 0 issues TMA loads into a ring of shared-
+// memory stages, warp 1 allocates TMEM and issues the MMAs (one elected
+// lane), the drain warps (one per TMEM lane quarter and 64 columns) empty
+// the accumulators.  Two to eight TMEM accumulator buffers let the drain of
+// one chunk overlap the MMAs of the next.  Every mbarrier wait is bounded (about a second); on timeout the
 // kernel records an error, stops issuing work, waits (bounded) for its own
 // TMA copies and MMAs in flight, frees its TMEM and returns.
 #include <cuda.h>
@@ -46,7 +46,6 @@ namespace {
 
 constexpr int BM = 128;
 constexpr int BK = 64;             // bf16 elements per 128-byte swizzled row
-constexpr int kAcc = 2;            // TMEM accumulator buffers
 constexpr int kChunkKb = 16;       // k-blocks per exact FP32 chunk (16 * 64 = 1024)
 constexpr int kFoldChunks = 127;   // int32 drain sums fold into FP64 before overflow
 
@@ -201,9 +200,14 @@ __device__ __forceinline__ int level_pairs(int l, int S) {
 template <int BN>
 struct SplitCfg {
   static constexpr int kStageBytes = (BM + BN) * BK * 2;
-  static constexpr int kStages = (200 * 1024 / kStageBytes) < 8 ? (200 * 1024 / kStageBytes) : 8;
-  static constexpr uint32_t kTmemCols = (2 * BN <= 32) ? 32 : (2 * BN <= 64) ? 64 : (2 * BN <= 128) ? 128
-                                        : (2 * BN <= 256) ? 256 : 512;
+  // narrow tiles: two CTAs per SM (half the shared memory each) and deeper
+  // TMEM buffering, since their chunks are short and drains come often
+  static constexpr int kCtasPerSm = BN <= 64 ? 2 : 1;
+  static constexpr int kSmemBudget = (BN <= 64 ? 100 : 200) * 1024;
+  static constexpr int kStages = (kSmemBudget / kStageBytes) < 8 ? (kSmemBudget / kStageBytes) : 8;
+  static constexpr int kAccBufs = BN <= 32 ? 8 : (BN <= 64 ? 4 : 2);
+  static constexpr uint32_t kTmemCols = (kAccBufs * BN <= 32) ? 32 : (kAccBufs * BN <= 64) ? 64
+                                        : (kAccBufs * BN <= 128) ? 128 : (kAccBufs * BN <= 256) ? 256 : 512;
   // drain warps: 4 per 64 columns (one per TMEM lane quarter), at least 4
   static constexpr int kDrainWarps = BN >= 64 ? 4 * (BN / 64) : 4;
   static constexpr int kCols = BN >= 64 ? 64 : BN;  // columns per drain thread
@@ -214,7 +218,8 @@ template <int BN>
 struct Smem {
   alignas(1024) __nv_bfloat16 a[SplitCfg<BN>::kStages][BM * BK];
   alignas(1024) __nv_bfloat16 b[SplitCfg<BN>::kStages][BN * BK];
-  uint64_t full[SplitCfg<BN>::kStages], empty[SplitCfg<BN>::kStages], accfull[kAcc], accempty[kAcc], done;
+  uint64_t full[SplitCfg<BN>::kStages], empty[SplitCfg<BN>::kStages], accfull[SplitCfg<BN>::kAccBufs],
+      accempty[SplitCfg<BN>::kAccBufs], done;
   uint32_t tmem_base;
 };
 
@@ -223,8 +228,10 @@ struct Smem {
 // fold into an FP64 Horner accumulator kept in the output tile itself (or the
 // split-K partial), which stays in L2 between the few folds of a tile.
 template <int BN>
-__global__ void __launch_bounds__(SplitCfg<BN>::kThreads, 1) split_gemm_kernel(const GemmParams P) {
+__global__ void __launch_bounds__(SplitCfg<BN>::kThreads, SplitCfg<BN>::kCtasPerSm)
+    split_gemm_kernel(const GemmParams P) {
   using Cfg = SplitCfg<BN>;
+  constexpr int kAcc = Cfg::kAccBufs;
   constexpr int kStagesN = Cfg::kStages;
   constexpr int kCols = Cfg::kCols;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -922,7 +929,7 @@ int launch_width(const SplitPlan* sp, const SplitLaunch& L, int nsm, cudaStream_
   P.S = sp->S;
   P.L = sp->L;
   P.err = sp->d_err;
-  const int grid = std::min(L.total_tiles, nsm);
+  const int grid = std::min(L.total_tiles, nsm * SplitCfg<BN>::kCtasPerSm);
   split_gemm_kernel<BN><<<grid, SplitCfg<BN>::kThreads, sizeof(Smem<BN>) + 1024, st>>>(P);
   GBX_CUDA(cudaGetLastError());
   return GBX_OK;
