@@ -43,6 +43,10 @@ def parse():
     p.add_argument("--seed", type=int, default=1)
     p.add_argument("--slices", type=int, default=0)
     p.add_argument("--profile", action="store_true", help="print the per-step breakdown to stderr")
+    p.add_argument("--kernel", choices=["ladder"], default=None,
+                   help="time one kernel alone: 'ladder' = the split GEMM on one irrep block of the "
+                        "<ab||ef> ladder of this workload (7200 x 288 x 7200)")
+    p.add_argument("--rates", action="store_true", help="build and run the arithmetic-rate probe")
     return p.parse_args()
 
 
@@ -122,9 +126,47 @@ def cpu_arm(a, steps, warmup, label_impl):
                        % (len(shapes), fl, cores), gemm_tflops=fl / dt / 1e12)
 
 
+def kernel_arm(a):
+    """One kernel alone, for profiling: the split GEMM on a ladder block."""
+    import torch
+    import dtcf_gb300
+    M, N, K = 7200, 288, 7200
+    g = torch.Generator(device="cuda").manual_seed(a.seed)
+    A = torch.rand(M, K, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+    B = torch.rand(N, K, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+    C = torch.zeros(M, N, dtype=torch.float64, device="cuda")
+    S = a.slices or 6
+    for _ in range(max(a.warmup, 1)):
+        dtcf_gb300.split_gemm(A, B, C, slices=S)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(a.steps):
+        dtcf_gb300.split_gemm(A, B, C, slices=S)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t) / a.steps
+    ref = A @ B.T
+    err = float(torch.linalg.norm(C - ref) / torch.linalg.norm(ref))
+    print(json.dumps({"kernel": "split_gemm ladder block", "M": M, "N": N, "K": K, "slices": S,
+                      "ms_per_call_incl_plan": dt * 1e3, "fp64_equiv_tflops": 2 * M * N * K / dt / 1e12,
+                      "rel_err_vs_fp64": err}))
+    return 0
+
+
+def rates_arm():
+    import tempfile
+    src = os.path.join(ROOT, "dtcf_gb300", "measure", "rates_probe.cu")
+    exe = os.path.join(tempfile.mkdtemp(), "rates_probe")
+    subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-o", exe, src], check=True)
+    return subprocess.run([exe]).returncode
+
+
 def main():
     a = parse()
     world, rank, local = dist_setup()
+    if a.rates:
+        return rates_arm()
+    if a.kernel:
+        return kernel_arm(a)
     if a.impl == "reference":
         if rank != 0:
             return 0

@@ -32,12 +32,13 @@ constexpr int kThinN = 32, kThinK = 64;
 
 // Tile shapes: 64x64 for large problems, 64x16 / 16x64 / 16x16 for skinny ones
 // (output dimensions below 48), so small outputs do not waste the FP64 pipe.
-// Thin problems (one output dimension <= 32 and K <= 64) run on CUDA-core
-// FP64 with exact shapes: variant 4 = one thread per row of C (N thin),
-// variant 5 = one thread per column (M thin).
+// Thin problems (one output dimension <= 32, the other at least 4x larger)
+// run on CUDA-core FP64 with exact shapes: variant 4 = one thread per row of
+// C (N thin), variant 5 = one thread per column (M thin).
 int f64_variant(int m, int n, int k) {
-  if (k <= kThinK && n <= kThinN && m >= 4 * n) return 4;
-  if (k <= kThinK && m <= kThinN && n >= 4 * m) return 5;
+  (void)k;
+  if (n <= kThinN && m >= 4 * n) return 4;
+  if (m <= kThinN && n >= 4 * m) return 5;
   return (m < 48 ? 2 : 0) + (n < 48 ? 1 : 0);
 }
 int f64_variant(int m, int n) { return (m < 48 ? 2 : 0) + (n < 48 ? 1 : 0); }
@@ -49,8 +50,9 @@ int f64_tiles(int m, int n) {
 }
 
 // One thread per row (variant 4) or per column (variant 5) of C; the thin
-// operand (at most kThinN x kThinK) sits in shared memory.  Each output is a
-// k-ordered FMA chain, so results are deterministic.
+// operand (at most kThinN rows) is staged through shared memory kThinK
+// columns at a time, so K is unbounded.  Each output is a k-ordered FMA
+// chain, so results are deterministic.
 template <bool kRows>
 __global__ void __launch_bounds__(256) thin_gemm_f64_kernel(const GemmProblem* __restrict__ probs, int nprob,
                                                             const int* __restrict__ block_first, int total_blocks) {
@@ -67,23 +69,29 @@ __global__ void __launch_bounds__(256) thin_gemm_f64_kernel(const GemmProblem* _
     const int tn = kRows ? p.n : p.m;
     const double* T = kRows ? p.B : p.A;
     const int64_t trs = kRows ? p.b_rs : p.a_rs, tcs = kRows ? p.b_cs : p.a_cs;
-    __syncthreads();
-    for (int e = threadIdx.x; e < tn * p.k; e += 256) Ts[e] = __ldg(T + (int64_t)(e / p.k) * trs + (int64_t)(e % p.k) * tcs);
-    __syncthreads();
     const int64_t i = i0 + threadIdx.x;
     const int64_t wide = kRows ? p.m : p.n;
-    if (i < wide) {
-      const double* W = kRows ? p.A + i * p.a_rs : p.B + i * p.b_rs;
-      const int64_t wcs = kRows ? p.a_cs : p.b_cs;
-      double acc[kThinN];
+    const double* W = kRows ? p.A + i * p.a_rs : p.B + i * p.b_rs;
+    const int64_t wcs = kRows ? p.a_cs : p.b_cs;
+    double acc[kThinN];
 #pragma unroll
-      for (int j = 0; j < kThinN; ++j) acc[j] = 0.0;
-      for (int k = 0; k < p.k; ++k) {
-        const double w = __ldg(W + k * wcs);
+    for (int j = 0; j < kThinN; ++j) acc[j] = 0.0;
+    for (int k0 = 0; k0 < p.k; k0 += kThinK) {
+      const int kc = min(kThinK, p.k - k0);
+      __syncthreads();
+      for (int e = threadIdx.x; e < tn * kc; e += 256)
+        Ts[e] = __ldg(T + (int64_t)(e / kc) * trs + (int64_t)(k0 + e % kc) * tcs);
+      __syncthreads();
+      if (i < wide) {
+        for (int k = 0; k < kc; ++k) {
+          const double w = __ldg(W + (int64_t)(k0 + k) * wcs);
 #pragma unroll
-        for (int j = 0; j < kThinN; ++j)
-          if (j < tn) acc[j] = fma(w, Ts[j * p.k + k], acc[j]);
+          for (int j = 0; j < kThinN; ++j)
+            if (j < tn) acc[j] = fma(w, Ts[j * kc + k], acc[j]);
+        }
       }
+    }
+    if (i < wide) {
 #pragma unroll
       for (int j = 0; j < kThinN; ++j) {
         if (j >= tn) break;

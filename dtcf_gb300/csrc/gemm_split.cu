@@ -449,6 +449,195 @@ __global__ void __launch_bounds__(SplitCfg<BN>::kThreads, SplitCfg<BN>::kCtasPer
   }
 }
 
+// ---- thin-K kernel: K <= 64, N <= 32 -----------------------------------
+//
+// One k-block per problem, so every slice is loaded once per 128-row tile
+// and all S(S+1)/2 slice products go into per-level TMEM accumulators
+// (level l at columns l*32 of a buffer; two buffers alternate between tiles).
+// A level sums at most S products of 64 K-elements, below 2^24, so no drains
+// are needed mid-tile: the drain warps read the levels from S-1 down to 0 and
+// recombine them with FP64 Horner steps directly.
+constexpr int kThinBN = 32;
+constexpr int kThinSlots = 10;   // ring of (A slice, B slice) pairs, 20 KB each
+constexpr int kThinThreads = 192;
+
+struct ThinSmem {
+  alignas(1024) __nv_bfloat16 a[kThinSlots][BM * BK];
+  alignas(1024) __nv_bfloat16 b[kThinSlots][kThinBN * BK];
+  uint64_t full[kThinSlots], empty[kThinSlots], accfull[2], accempty[2], done;
+  uint32_t tmem_base;
+};
+
+__global__ void __launch_bounds__(kThinThreads, 1) split_thin_kernel(const GemmParams P) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  ThinSmem& sm = *reinterpret_cast<ThinSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int S = P.S, L = P.L;
+  constexpr uint32_t kTx = (BM + kThinBN) * BK * 2;
+  constexpr uint32_t kCols = 512;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kThinSlots; ++i) {
+      mbar_init(&sm.full[i], 1);
+      mbar_init(&sm.empty[i], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&sm.accfull[b], 1);
+      mbar_init(&sm.accempty[b], 4);
+    }
+    mbar_init(&sm.done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm.tmem_base)),
+                 "r"(kCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = sm.tmem_base;
+  const uint32_t buf_cols = (uint32_t)(S * kThinBN);
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int slot = 0;
+      uint32_t phase = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < P.total_tiles && ok; tile += gridDim.x) {
+        const TileInfo ti = decode_tile<kThinBN>(P, tile);
+        const CUtensorMap* ma = P.maps + 2 * ti.p;
+        const CUtensorMap* mb = P.maps + 2 * ti.p + 1;
+        for (int s = 0; s < S; ++s) {
+          if (!mbar_wait(&sm.empty[slot], phase ^ 1, P.err, 11)) {
+            ok = false;
+            break;
+          }
+          mbar_expect_tx(&sm.full[slot], kTx);
+          tma_load_3d(sm.a[slot], ma, &sm.full[slot], 0, ti.m0, s);
+          tma_load_3d(sm.b[slot], mb, &sm.full[slot], 0, ti.n0, s);
+          if (++slot == kThinSlots) {
+            slot = 0;
+            phase ^= 1;
+          }
+        }
+      }
+      for (int i = 0; i < kThinSlots; ++i) {
+        if (--slot < 0) {
+          slot = kThinSlots - 1;
+          phase ^= 1;
+        }
+        long long t0 = clock64();
+        while (!mbar_try_wait(&sm.full[slot], phase) && !mbar_try_wait(&sm.empty[slot], phase)) {
+          if (clock64() - t0 > kWaitCycles) {
+            atomicCAS(P.err, 0, 15);
+            break;
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      int slot = 0, buf = 0;
+      uint32_t phase = 0, aphase = 0;
+      bool ok = true;
+      constexpr uint32_t idesc = idesc_bf16<kThinBN>();
+      for (int tile = blockIdx.x; tile < P.total_tiles && ok; tile += gridDim.x) {
+        // the tile's S slices occupy S consecutive ring slots
+        int sl[8];
+        for (int s = 0; s < S; ++s) {
+          sl[s] = slot;
+          if (!mbar_wait(&sm.full[slot], phase, P.err, 13)) {
+            ok = false;
+            break;
+          }
+          if (++slot == kThinSlots) {
+            slot = 0;
+            phase ^= 1;
+          }
+        }
+        if (!ok) break;
+        if (!mbar_wait(&sm.accempty[buf], aphase ^ 1, P.err, 12)) break;
+        tc_fence_after();
+        for (int l = 0; l <= L; ++l) {
+          const uint32_t d = tmem + (uint32_t)buf * buf_cols + (uint32_t)(l * kThinBN);
+          bool first = true;
+          for (int s = max(1, l + 2 - S); s <= min(S, l + 1); ++s) {
+            const int t = l + 2 - s;
+            const uint64_t a0 = sdesc(smem_u32(sm.a[sl[s - 1]]));
+            const uint64_t b0 = sdesc(smem_u32(sm.b[sl[t - 1]]));
+#pragma unroll
+            for (int k = 0; k < BK / 16; ++k) {
+              umma(d, a0 + (uint64_t)(k * 2), b0 + (uint64_t)(k * 2), idesc, first ? 0u : 1u);
+              first = false;
+            }
+          }
+        }
+        for (int s = 0; s < S; ++s) umma_commit(&sm.empty[sl[s]]);
+        umma_commit(&sm.accfull[buf]);
+        if (++buf == 2) {
+          buf = 0;
+          aphase ^= 1;
+        }
+      }
+      umma_commit(&sm.done);
+      mbar_wait(&sm.done, 0, P.err, 16);
+    }
+  } else {
+    const int quarter = warp & 3;
+    const uint32_t lane_addr = (uint32_t)(quarter * 32) << 16;
+    int buf = 0;
+    uint32_t aphase = 0;
+    for (int tile = blockIdx.x; tile < P.total_tiles; tile += gridDim.x) {
+      const TileInfo ti = decode_tile<kThinBN>(P, tile);
+      const DevProblem& pr = P.probs[ti.p];
+      int w_ok = lane == 0 ? (int)mbar_wait(&sm.accfull[buf], aphase, P.err, 14) : 1;
+      w_ok = __shfl_sync(0xffffffffu, w_ok, 0);
+      if (!w_ok) break;
+      __syncwarp();
+      tc_fence_after();
+      double acc[kThinBN];
+#pragma unroll
+      for (int j = 0; j < kThinBN; ++j) acc[j] = 0.0;
+      for (int l = L; l >= 0; --l) {
+        uint32_t r[2][16];
+        tmem_ld16(tmem + lane_addr + (uint32_t)buf * buf_cols + (uint32_t)(l * kThinBN), r[0]);
+        tmem_ld16(tmem + lane_addr + (uint32_t)buf * buf_cols + (uint32_t)(l * kThinBN + 16), r[1]);
+        tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < kThinBN; ++j)
+          if (j < pr.N) acc[j] = acc[j] * 0x1.0p-8 + (double)__uint_as_float(r[j >> 4][j & 15]);
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.accempty[buf]);
+      if (++buf == 2) {
+        buf = 0;
+        aphase ^= 1;
+      }
+      const int row = ti.m0 + quarter * 32 + lane;
+      if (row < pr.M) {
+        const int ea = pr.eA[row];
+        double* crow = pr.C + (int64_t)row * pr.ldc;
+#pragma unroll
+        for (int j = 0; j < kThinBN; ++j) {
+          if (j < pr.N) {
+            int ex = ea + pr.eB[j] - 2 * 1022 - 14 + 1023;
+            ex = ex < 1 ? 1 : (ex > 2046 ? 2046 : ex);
+            crow[j] = acc[j] * __longlong_as_double((long long)ex << 52);
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols));
+  }
+}
+
 // Fixed-order sum of the split-K partial contributions into C.
 __global__ void __launch_bounds__(256) split_reduce_kernel(const DevProblem* __restrict__ probs,
                                                            const int* __restrict__ red_prob,
@@ -661,6 +850,7 @@ struct SplitPlan {
   int S = 0, L = 0;
   std::vector<SplitProblem> host;
   std::vector<int> width;  // per problem
+  std::vector<bool> thin;  // per problem: thin-K kernel
   __nv_bfloat16* d_slices = nullptr;  // all A and B slices
   int* d_exps = nullptr;
   SplitRowSet* d_sets_a = nullptr;  // long rows from the plan's packed A
@@ -724,8 +914,11 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
   for (auto& p : probs) {
     if (p.M <= 0 || p.N <= 0 || p.K <= 0) return fail(GBX_EINVAL, "empty split problem");
     if (p.M >= (1ll << 30) || p.N >= (1ll << 30) || p.K >= (1ll << 30)) return fail(GBX_EUNSUPPORTED, "split problem too large");
-    const int bn = choose_width(p.N);
+    // thin-K problems (one k-block, at most 32 columns) take the thin kernel
+    const bool thin = p.K <= BK && p.N <= kThinBN && S <= 7;
+    const int bn = thin ? kThinBN : choose_width(p.N);
     sp->width.push_back(bn);
+    sp->thin.push_back(thin);
     Off o;
     o.Mp = (p.M + BM - 1) / BM * BM;
     o.Np = (p.N + bn - 1) / bn * bn;
@@ -796,7 +989,7 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
     // split K when the output tiles of all problems leave SMs idle; ranges are
     // whole exact-accumulation chunks
     int ks = 1;
-    if (out_tiles < kSplitFill && d.nkb > 2 * kChunkKb) {
+    if (!sp->thin[i] && out_tiles < kSplitFill && d.nkb > 2 * kChunkKb) {
       int want = (int)((kSplitFill + out_tiles - 1) / out_tiles);
       ks = std::max(1, std::min(want, d.nkb / kChunkKb));
     }
@@ -856,14 +1049,14 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
   GBX_TRY(up(ssa.data(), sizeof(SplitRowSet) * ssa.size(), (void**)&sp->d_short_a));
   GBX_TRY(up(ssb.data(), sizeof(SplitRowSet) * ssb.size(), (void**)&sp->d_short_b));
   GBX_TRY(up(dp.data(), sizeof(DevProblem) * dp.size(), (void**)&sp->d_all));
-  // one launch per output tile width
-  for (int bn : kWidths) {
+  // one launch per output tile width, plus one for the thin-K problems (bn 0)
+  for (int bn : {0, 32, 64, 128, 256}) {
     std::vector<DevProblem> lp;
     std::vector<CUtensorMap> lm;
     std::vector<int> first;
     int tiles = 0;
     for (size_t i = 0; i < probs.size(); ++i) {
-      if (sp->width[i] != bn) continue;
+      if (bn == 0 ? !sp->thin[i] : (sp->thin[i] || sp->width[i] != bn)) continue;
       lp.push_back(dp[i]);
       lm.push_back(maps[2 * i]);
       lm.push_back(maps[2 * i + 1]);
@@ -886,6 +1079,8 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
   GBX_TRY(set_smem_attr<64>());
   GBX_TRY(set_smem_attr<128>());
   GBX_TRY(set_smem_attr<256>());
+  GBX_CUDA(cudaFuncSetAttribute(split_thin_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(sizeof(ThinSmem) + 1024)));
   *out = sp.release();
   return GBX_OK;
 }
@@ -942,6 +1137,20 @@ int run_split_plan(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   for (const SplitLaunch& L : sp->launches) {
+    if (L.bn == 0) {
+      GemmParams P;
+      P.probs = L.d_probs;
+      P.tile_first = L.d_tile_first;
+      P.maps = L.d_maps;
+      P.nprob = L.nprob;
+      P.total_tiles = L.total_tiles;
+      P.S = sp->S;
+      P.L = sp->L;
+      P.err = sp->d_err;
+      split_thin_kernel<<<std::min(L.total_tiles, nsm), kThinThreads, sizeof(ThinSmem) + 1024, st>>>(P);
+      GBX_CUDA(cudaGetLastError());
+      continue;
+    }
     switch (L.bn) {
       case 32: GBX_TRY(launch_width<32>(sp, L, nsm, st)); break;
       case 64: GBX_TRY(launch_width<64>(sp, L, nsm, st)); break;
@@ -970,7 +1179,7 @@ double split_plan_tensor_flops(const SplitPlan* sp) {
   const double pairs = sp->S * (sp->S + 1) / 2.0;
   for (size_t i = 0; i < sp->host.size(); ++i) {
     const SplitProblem& p = sp->host[i];
-    const int bn = sp->width[i];
+    const int bn = sp->width[i];  // thin-K problems: 32
     double Mp = (double)((p.M + BM - 1) / BM * BM), Np = (double)((p.N + bn - 1) / bn * bn);
     double Kp = (double)((p.K + BK - 1) / BK * BK);
     f += 2.0 * pairs * Mp * Np * Kp;

@@ -247,11 +247,22 @@ void choose_engine(GroupBlock& g, bool split_engine, bool split_all, int slices)
   const int S = slices > 0 ? slices : 6;
   const double pairs = S * (S + 1) / 2.0;
   const double kp = up(g.K, 64);
-  const double t_split = 2.0 * pairs * up(g.M, 128) * up(g.N, 64) * kp / 1.0e15;
-  const double t_split_sw = 2.0 * pairs * up(g.N, 128) * up(g.M, 64) * kp / 1.0e15;
+  // slice products at ~1 PFLOP/s, or the wide operand's slices streamed once
+  // per slice pair (2 bytes per element per pair), whichever binds; a thin-K
+  // problem (K <= 64, at most 32 columns) streams each slice once
+  auto split_cost = [&](int64_t rows, int64_t cols) {
+    const double mp = up(rows, 128);
+    if (g.K <= 64 && cols <= 32)
+      return std::max(2.0 * pairs * mp * 32.0 * 64.0 / 1.0e15, S * 2.0 * mp * 64.0 / 6e12);
+    return std::max(2.0 * pairs * mp * up(cols, 64) * kp / 1.0e15, pairs * 2.0 * mp * kp / 6e12);
+  };
+  const double t_split = split_cost(g.M, g.N);
+  const double t_split_sw = split_cost(g.N, g.M);
   const int mi = (int)std::min<int64_t>(g.M, 1 << 30), ni = (int)std::min<int64_t>(g.N, 1 << 30);
   const int v = f64_variant(mi, ni, (int)std::min<int64_t>(g.K, 1 << 30));
-  const double t_f64 = v >= 4 ? 2.0 * (double)g.M * (double)g.N * (double)g.K / 0.9e12 + 2e-6
+  // thin FP64: exact flops, or streaming the wide operand once, whichever binds
+  const double wide = (double)std::max(g.M, g.N) * (double)g.K * 8.0;
+  const double t_f64 = v >= 4 ? std::max(2.0 * (double)g.M * (double)g.N * (double)g.K / 0.9e12, wide / 5e12) + 2e-6
                               : 2.0 * up(g.M, f64_tile_m(v)) * up(g.N, f64_tile_n(v)) * up(g.K, 16) / 0.95e12;
   const double best_split = std::min(t_split, t_split_sw) + 4e-6;  // + split and launch overhead
   if (split_all || best_split < t_f64) {

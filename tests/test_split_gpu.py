@@ -60,3 +60,22 @@ def test_split_gemm_exact_every_tile_width(width, M, N, K):
     finally:
         lib().gbx_split_set_width(0)
     assert np.array_equal(C.cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("M,N,K", [(5000, 8, 38), (300, 1, 1), (1000, 32, 64), (129, 17, 5)])
+def test_split_gemm_thin_k_exact(M, N, K):
+    """K <= 64 and N <= 32: the thin-K kernel (all slice products of a tile
+    in per-level TMEM accumulators) is exact on integer data."""
+    import dtcf_gb300
+    rng = np.random.default_rng(M + N + K)
+    A = rng.integers(-(1 << 20), 1 << 20, size=(M, K)).astype(np.float64)
+    B = rng.integers(-(1 << 20), 1 << 20, size=(N, K)).astype(np.float64)
+    want = (A.astype(np.int64) @ B.astype(np.int64).T).astype(np.float64)
+    C = torch.zeros((M, N), dtype=torch.float64, device="cuda")
+    dtcf_gb300.split_gemm(dev(A), dev(B), C, slices=6)
+    assert np.array_equal(C.cpu().numpy(), want)
+    Af = rng.uniform(-1, 1, (M, K))
+    Bf = rng.uniform(-1, 1, (N, K))
+    dtcf_gb300.split_gemm(dev(Af), dev(Bf), C, slices=7)
+    ref = Af @ Bf.T
+    assert np.linalg.norm(C.cpu().numpy() - ref) <= 1e-15 * max(np.linalg.norm(ref), 1e-300) * 10
