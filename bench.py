@@ -43,9 +43,10 @@ def parse():
     p.add_argument("--seed", type=int, default=1)
     p.add_argument("--slices", type=int, default=0)
     p.add_argument("--profile", action="store_true", help="print the per-step breakdown to stderr")
-    p.add_argument("--kernel", choices=["ladder"], default=None,
-                   help="time one kernel alone: 'ladder' = the split GEMM on one irrep block of the "
-                        "<ab||ef> ladder of this workload (7200 x 288 x 7200)")
+    p.add_argument("--kernel", choices=["ladder", "thin"], default=None,
+                   help="time one split GEMM alone: 'ladder' = one irrep block of the <ab||ef> ladder of "
+                        "this workload (7200 x 288 x 7200); 'thin' = one irrep block of t_i^e <ab||ej> "
+                        "(346174 x 8 x 38, the thin-K kernel)")
     p.add_argument("--rates", action="store_true", help="build and run the arithmetic-rate probe")
     return p.parse_args()
 
@@ -130,7 +131,7 @@ def kernel_arm(a):
     """One kernel alone, for profiling: the split GEMM on a ladder block."""
     import torch
     import dtcf_gb300
-    M, N, K = 7200, 288, 7200
+    M, N, K = (7200, 288, 7200) if a.kernel == "ladder" else (346174, 8, 38)
     g = torch.Generator(device="cuda").manual_seed(a.seed)
     A = torch.rand(M, K, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
     B = torch.rand(N, K, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
@@ -146,7 +147,7 @@ def kernel_arm(a):
     dt = (time.perf_counter() - t) / a.steps
     ref = A @ B.T
     err = float(torch.linalg.norm(C - ref) / torch.linalg.norm(ref))
-    print(json.dumps({"kernel": "split_gemm ladder block", "M": M, "N": N, "K": K, "slices": S,
+    print(json.dumps({"kernel": "split_gemm %s block" % a.kernel, "M": M, "N": N, "K": K, "slices": S,
                       "ms_per_call_incl_plan": dt * 1e3, "fp64_equiv_tflops": 2 * M * N * K / dt / 1e12,
                       "rel_err_vs_fp64": err}))
     return 0

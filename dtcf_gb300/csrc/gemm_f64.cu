@@ -27,18 +27,23 @@ constexpr int kFillTiles = 152 * 3;   // work items that keep every SM busy
 constexpr int kMinChunk = 256;        // smallest K range of a split
 constexpr int kRedThreads = 256;
 constexpr int kRedChunk = 2048;
-constexpr int kThinN = 32, kThinK = 64;
+constexpr int kThinN = 32, kThinK = 64, kThinMinWide = 16384;
+constexpr int kSmallK = 8;
+constexpr int kSmallKElems = 2048;  // output elements per CTA
 }  // namespace
 
 // Tile shapes: 64x64 for large problems, 64x16 / 16x64 / 16x16 for skinny ones
 // (output dimensions below 48), so small outputs do not waste the FP64 pipe.
-// Thin problems (one output dimension <= 32, the other at least 4x larger)
-// run on CUDA-core FP64 with exact shapes: variant 4 = one thread per row of
-// C (N thin), variant 5 = one thread per column (M thin).
+// Thin problems (one output dimension <= 32, the other at least 4x larger,
+// and either K <= 64 or at least 16384 wide rows to spread over the GPU) run
+// on CUDA-core FP64 with exact shapes: variant 4 = one thread per row of C
+// (N thin), variant 5 = one thread per column (M thin).
 int f64_variant(int m, int n, int k) {
-  (void)k;
-  if (n <= kThinN && m >= 4 * n) return 4;
-  if (m <= kThinN && n >= 4 * m) return 5;
+  // K <= 8 (outer products): one thread per output element
+  if (k <= kSmallK) return 6;
+  // one thread per wide row: only with enough rows to fill the GPU, or short K
+  if (n <= kThinN && m >= 4 * n && (k <= kThinK || m >= kThinMinWide)) return 4;
+  if (m <= kThinN && n >= 4 * m && (k <= kThinK || n >= kThinMinWide)) return 5;
   return (m < 48 ? 2 : 0) + (n < 48 ? 1 : 0);
 }
 int f64_variant(int m, int n) { return (m < 48 ? 2 : 0) + (n < 48 ? 1 : 0); }
@@ -233,6 +238,33 @@ __global__ void __launch_bounds__(kThreads) grouped_gemm_f64_kernel(const GemmPr
   }
 }
 
+// K <= 8: every output element is its own k-ordered FMA chain (outer
+// products and other tiny-K contractions), written coalesced along columns.
+__global__ void __launch_bounds__(256) small_k_gemm_f64_kernel(const GemmProblem* __restrict__ probs, int nprob,
+                                                               const int* __restrict__ block_first, int total_blocks) {
+  for (int blk = blockIdx.x; blk < total_blocks; blk += gridDim.x) {
+    int lo = 0, hi = nprob - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (block_first[mid] <= blk) lo = mid; else hi = mid - 1;
+    }
+    const GemmProblem& p = probs[lo];
+    const int64_t mn = (int64_t)p.m * p.n;
+    const int64_t e0 = (int64_t)(blk - block_first[lo]) * kSmallKElems;
+    for (int r = 0; r < kSmallKElems / 256; ++r) {
+      const int64_t e = e0 + r * 256 + threadIdx.x;
+      if (e >= mn) break;
+      const int64_t i = e / p.n, j = e - i * p.n;
+      double acc = 0.0;
+      for (int k = 0; k < p.k; ++k)
+        acc = fma(__ldg(p.A + i * p.a_rs + (int64_t)k * p.a_cs), __ldg(p.B + j * p.b_rs + (int64_t)k * p.b_cs), acc);
+      double* c = p.C + i * p.c_rs + j;
+      const double v = __dmul_rn(p.alpha, acc);
+      *c = p.accumulate ? __dadd_rn(*c, v) : v;
+    }
+  }
+}
+
 // Fixed-order reduction of split-K partials into C.
 __global__ void __launch_bounds__(kRedThreads) splitk_reduce_kernel(const GemmProblem* __restrict__ probs,
                                                                     const int* __restrict__ red_prob,
@@ -303,7 +335,7 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
     GemmProblem& q = probs[i];
     int ks = 1;
     const int thin = f64_variant(q.m, q.n, q.k);
-    if (thin >= 4) {
+    if (thin >= 4) {  // thin and small-K kernels: no split-K
       q.ksplit = 1;
       q.kchunk = std::max(q.k, BK);
       q.partial = nullptr;
@@ -352,7 +384,7 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
   for (auto& q : probs)
     if (q.partial) q.partial = d_partial + ((intptr_t)q.partial - 1);
   // one launch per tile shape
-  for (int v = 0; v < 6; ++v) {
+  for (int v = 0; v < 7; ++v) {
     std::vector<GemmProblem> vp;
     std::vector<int> first;
     int64_t tiles = 0;
@@ -362,6 +394,7 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
       first.push_back((int)tiles);
       if (v == 4) tiles += (q.m + 255) / 256;
       else if (v == 5) tiles += (q.n + 255) / 256;
+      else if (v == 6) tiles += ((int64_t)q.m * q.n + kSmallKElems - 1) / kSmallKElems;
       else tiles += (int64_t)f64_tiles(q.m, q.n) * q.ksplit;
     }
     if (vp.empty()) continue;
@@ -414,6 +447,10 @@ int F64Gemm::run(cudaStream_t st) const {
       case 4:
         thin_gemm_f64_kernel<true><<<std::min(sb.total_tiles, 152 * 8), 256, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first,
                                                                                       sb.total_tiles);
+        break;
+      case 6:
+        small_k_gemm_f64_kernel<<<std::min(sb.total_tiles, 152 * 8), 256, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first,
+                                                                                   sb.total_tiles);
         break;
       default:
         thin_gemm_f64_kernel<false><<<std::min(sb.total_tiles, 152 * 8), 256, 0, st>>>(sb.d_probs, sb.nprob,

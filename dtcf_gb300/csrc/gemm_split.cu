@@ -595,17 +595,37 @@ __global__ void __launch_bounds__(kThinThreads, 1) split_thin_kernel(const GemmP
       if (!w_ok) break;
       __syncwarp();
       tc_fence_after();
+      // Horner over the levels in exact int64 fixed point, Y = sum_l X_l 2^(8 (L - l)),
+      // from level 0 up (|X_l| <= 7 * 64 * 2^14 < 2^23, so |Y| < 2^63 for L <= 5);
+      // S = 7 keeps the FP64 recombination
+      const int ncol = min(kThinBN, pr.N - ti.n0);
+      long long Y[kThinBN];
       double acc[kThinBN];
 #pragma unroll
-      for (int j = 0; j < kThinBN; ++j) acc[j] = 0.0;
-      for (int l = L; l >= 0; --l) {
-        uint32_t r[2][16];
-        tmem_ld16(tmem + lane_addr + (uint32_t)buf * buf_cols + (uint32_t)(l * kThinBN), r[0]);
-        tmem_ld16(tmem + lane_addr + (uint32_t)buf * buf_cols + (uint32_t)(l * kThinBN + 16), r[1]);
-        tmem_wait_ld();
+      for (int j = 0; j < kThinBN; ++j) {
+        Y[j] = 0;
+        acc[j] = 0.0;
+      }
+      if (L <= 5) {
+        for (int l = 0; l <= L; ++l) {
+          uint32_t r[2][16];
+          tmem_ld16(tmem + lane_addr + (uint32_t)buf * buf_cols + (uint32_t)(l * kThinBN), r[0]);
+          tmem_ld16(tmem + lane_addr + (uint32_t)buf * buf_cols + (uint32_t)(l * kThinBN + 16), r[1]);
+          tmem_wait_ld();
 #pragma unroll
-        for (int j = 0; j < kThinBN; ++j)
-          if (j < pr.N) acc[j] = acc[j] * 0x1.0p-8 + (double)__uint_as_float(r[j >> 4][j & 15]);
+          for (int j = 0; j < kThinBN; ++j)
+            if (j < ncol) Y[j] = Y[j] * 256 + (long long)__float2int_rn(__uint_as_float(r[j >> 4][j & 15]));
+        }
+      } else {
+        for (int l = L; l >= 0; --l) {
+          uint32_t r[2][16];
+          tmem_ld16(tmem + lane_addr + (uint32_t)buf * buf_cols + (uint32_t)(l * kThinBN), r[0]);
+          tmem_ld16(tmem + lane_addr + (uint32_t)buf * buf_cols + (uint32_t)(l * kThinBN + 16), r[1]);
+          tmem_wait_ld();
+#pragma unroll
+          for (int j = 0; j < kThinBN; ++j)
+            if (j < ncol) acc[j] = acc[j] * 0x1.0p-8 + (double)__uint_as_float(r[j >> 4][j & 15]);
+        }
       }
       tc_fence_before();
       __syncwarp();
@@ -618,12 +638,14 @@ __global__ void __launch_bounds__(kThinThreads, 1) split_thin_kernel(const GemmP
       if (row < pr.M) {
         const int ea = pr.eA[row];
         double* crow = pr.C + (int64_t)row * pr.ldc;
+        const int lshift = L <= 5 ? 8 * L : 0;  // the int64 path carries 2^(8L)
 #pragma unroll
         for (int j = 0; j < kThinBN; ++j) {
-          if (j < pr.N) {
-            int ex = ea + pr.eB[j] - 2 * 1022 - 14 + 1023;
+          if (j < ncol) {
+            int ex = ea + pr.eB[j] - 2 * 1022 - 14 - lshift + 1023;
             ex = ex < 1 ? 1 : (ex > 2046 ? 2046 : ex);
-            crow[j] = acc[j] * __longlong_as_double((long long)ex << 52);
+            const double v = L <= 5 ? (double)Y[j] : acc[j];
+            crow[j] = v * __longlong_as_double((long long)ex << 52);
           }
         }
       }

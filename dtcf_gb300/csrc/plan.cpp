@@ -262,8 +262,11 @@ void choose_engine(GroupBlock& g, bool split_engine, bool split_all, int slices)
   const int v = f64_variant(mi, ni, (int)std::min<int64_t>(g.K, 1 << 30));
   // thin FP64: exact flops, or streaming the wide operand once, whichever binds
   const double wide = (double)std::max(g.M, g.N) * (double)g.K * 8.0;
-  const double t_f64 = v >= 4 ? std::max(2.0 * (double)g.M * (double)g.N * (double)g.K / 0.9e12, wide / 5e12) + 2e-6
-                              : 2.0 * up(g.M, f64_tile_m(v)) * up(g.N, f64_tile_n(v)) * up(g.K, 16) / 0.95e12;
+  const double outs = (double)g.M * (double)g.N * 8.0;
+  const double t_f64 =
+      v == 6 ? std::max(2.0 * (double)g.M * (double)g.N * (double)g.K / 0.9e12, outs / 5e12) + 2e-6
+      : v >= 4 ? std::max(2.0 * (double)g.M * (double)g.N * (double)g.K / 0.9e12, wide / 5e12) + 2e-6
+               : 2.0 * up(g.M, f64_tile_m(v)) * up(g.N, f64_tile_n(v)) * up(g.K, 16) / 0.95e12;
   const double best_split = std::min(t_split, t_split_sw) + 4e-6;  // + split and launch overhead
   if (split_all || best_split < t_f64) {
     g.engine = 1;

@@ -210,3 +210,14 @@ def test_grouped_gemm_thin_shapes(gbx, m, n, k):
     dA, dB, dC = dev(A), dev(B), dev(C)
     gbx.grouped_gemm_f64([Triple(dA.data_ptr(), dB.data_ptr(), dC.data_ptr(), k, 1, k, 1, n, m, n, k, -2.0, 1)])
     np.testing.assert_allclose(host(dC).reshape(m, n), C - 2.0 * A @ B.T, rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("m,n,k", [(1475, 1475, 1), (300, 700, 8), (5, 9, 3)])
+def test_grouped_gemm_small_k(gbx, m, n, k):
+    """K <= 8 problems (outer products) take the per-element FP64 kernel."""
+    from dtcf_gb300.leaves import Triple
+    rng = np.random.default_rng(m + n + k)
+    A, B, C = rng.standard_normal((m, k)), rng.standard_normal((n, k)), rng.standard_normal((m, n))
+    dA, dB, dC = dev(A), dev(B), dev(C)
+    gbx.grouped_gemm_f64([Triple(dA.data_ptr(), dB.data_ptr(), dC.data_ptr(), k, 1, k, 1, n, m, n, k, 0.5, 1)])
+    np.testing.assert_allclose(host(dC).reshape(m, n), C + 0.5 * A @ B.T, rtol=1e-13, atol=1e-13)
