@@ -18,6 +18,7 @@ SIGNATURES = {
     "gbx_transpose_blocks": (_i, [_p, _p, _i, _p, _i, _p, _p]),
     "gbx_dltc_transpose": (_i, [_p, _p, _p, _p, _i, _p, _p]),
     "gbx_local_contraction": (_i, [_i, _i, _i, _p, _p, _p, _i, _i, _d, _p]),
+    "gbx_local_contraction_noalloc": (_i, [_i, _i, _i, _p, _p, _p, _i, _i, _d, _p]),
     "gbx_dltc_compute": (_i, [_p, _p, _p, _i, _i, _i, _p]),
     "gbx_create_big_matrix": (_i, [_i, _p, _p, _i, _p, _p, _i, _i, _i, _p, _ip, _ip, _p]),
     "gbx_revert_big_matrix": (_i, [_i, _p, _p, _i, _p, _i, _i, _i, _p, _p, _p]),

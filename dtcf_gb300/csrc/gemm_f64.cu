@@ -14,6 +14,8 @@
 // kernel is FP64-issue bound at any reasonable occupancy; the data path is
 // kept simple (register-staged shared-memory tiles, double buffered).
 #include <algorithm>
+#include <cstring>
+#include <mutex>
 
 #include "common.h"
 
@@ -468,3 +470,134 @@ int F64Gemm::run(cudaStream_t st) const {
 }
 
 }  // namespace gbx
+
+// ---- allocation-free local contraction ----------------------------------
+//
+// Some callers cannot let a library allocate device memory: a framework that
+// has handed nearly all of the device's memory to its own caching pool (a
+// library cudaMalloc then fails, or forces the pool to give memory back), and
+// latency-bound loops that keep other streams busy (cudaFree synchronises the
+// device and stalls them).  For them gbx_local_contraction_noalloc runs the
+// same FP64 GEMM with its descriptor and split-K partial sums in one
+// file-scope device array of kNoAllocBytes, which every GPU that loads the
+// library holds until the process exits.  What must start at zero: the
+// work-queue ticket, written (with the whole descriptor) by every call before
+// its kernels run.  The partial-sum slabs need no clearing: every split-K
+// range overwrites its slab in full before the reduction reads it.
+namespace gbx {
+namespace {
+constexpr size_t kNoAllocHeader = 4096;                   // descriptor, schedule words
+constexpr size_t kNoAllocPartialBytes = 32ull << 20;      // split-K partial sums
+constexpr size_t kNoAllocBytes = kNoAllocHeader + kNoAllocPartialBytes;
+constexpr int64_t kNoAllocMaxElems = (int64_t)(kNoAllocPartialBytes / sizeof(double));
+
+struct NoAllocHeader {
+  GemmProblem prob;
+  int first;         // first work item of the problem (always 0)
+  int ticket;        // work-queue counter, reset by every call
+  int red_prob;      // split-K reduction: problem index (0)
+  uint32_t red_first;
+};
+static_assert(sizeof(NoAllocHeader) <= kNoAllocHeader, "header does not fit");
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+// Device address of the scratch array, looked up once per device (the host
+// symbol is only a stand-in for it).
+static int noalloc_scratch(unsigned char** out) {
+  static std::mutex mu;
+  static unsigned char* addr[256] = {nullptr};
+  int dev = 0;
+  GBX_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 256) return fail(GBX_EUNSUPPORTED, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lk(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)", __FILE__, __LINE__);
+    addr[dev] = (unsigned char*)p;
+  }
+  *out = addr[dev];
+  return GBX_OK;
+}
+
+}  // namespace gbx
+
+extern "C" int gbx_local_contraction_noalloc(int n_a, int n_b, int n_k, const double* d_A, const double* d_B,
+                                             double* d_C, int at, int bt, double alpha, void* stream) {
+  using namespace gbx;
+  if (n_a < 0 || n_b < 0 || n_k < 0) return fail(GBX_EINVAL, "negative extent");
+  if (n_a == 0 || n_b == 0) return GBX_OK;
+  if ((int64_t)n_a * n_b > kNoAllocMaxElems)
+    return fail(GBX_EINVAL, "output of %lld elements exceeds the allocation-free workspace (max %lld elements)",
+                (long long)n_a * n_b, (long long)kNoAllocMaxElems);
+  unsigned char* scratch = nullptr;
+  GBX_TRY(noalloc_scratch(&scratch));
+  cudaStream_t st = (cudaStream_t)stream;
+  NoAllocHeader h;
+  std::memset(&h, 0, sizeof(h));
+  GemmProblem& p = h.prob;
+  p.A = d_A;
+  p.B = d_B;
+  p.C = d_C;
+  p.a_rs = at ? 1 : n_k;
+  p.a_cs = at ? n_a : 1;
+  p.b_rs = bt ? n_k : 1;
+  p.b_cs = bt ? 1 : n_b;
+  p.c_rs = n_b;
+  p.m = n_a;
+  p.n = n_b;
+  p.k = n_k;
+  p.alpha = alpha;
+  p.accumulate = 1;
+  // same schedule as the allocating path, split-K capped by the workspace
+  const int variant = f64_variant(n_a, n_b, n_k);
+  int ks = 1;
+  const int out_tiles = f64_tiles(n_a, n_b);
+  if (variant < 4 && out_tiles < kFillTiles && n_k > 2 * kMinChunk) {
+    int want = (kFillTiles + out_tiles - 1) / out_tiles;
+    ks = std::max(1, std::min(want, (n_k + kMinChunk - 1) / kMinChunk));
+    ks = (int)std::min<int64_t>(ks, kNoAllocMaxElems / ((int64_t)n_a * n_b));
+  }
+  int chunk = (n_k + ks - 1) / ks;
+  chunk = ((chunk + BK - 1) / BK) * BK;
+  ks = std::max(1, (n_k + chunk - 1) / chunk);
+  p.ksplit = ks;
+  p.kchunk = std::max(chunk, BK);
+  p.pad_ = variant;
+  p.partial = ks > 1 ? (double*)(scratch + kNoAllocHeader) : nullptr;
+  h.first = 0;
+  h.ticket = 0;
+  h.red_prob = 0;
+  h.red_first = 0;
+  NoAllocHeader* dh = (NoAllocHeader*)scratch;
+  // the header is staged from host memory on the stream; the ticket starts at 0
+  GBX_CUDA(cudaMemcpyAsync(dh, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+  int tiles;
+  if (variant == 4) tiles = (n_a + 255) / 256;
+  else if (variant == 5) tiles = (n_b + 255) / 256;
+  else if (variant == 6) tiles = (int)(((int64_t)n_a * n_b + kSmallKElems - 1) / kSmallKElems);
+  else tiles = f64_tiles(n_a, n_b) * ks;
+  const GemmProblem* dp = &dh->prob;
+  const int* df = &dh->first;
+  int* dt = &dh->ticket;
+  const int grid = std::min(tiles, 152 * 4);
+  switch (variant) {
+    case 0: grouped_gemm_f64_kernel<64, 64><<<grid, kThreads, 0, st>>>(dp, 1, df, tiles, dt); break;
+    case 1: grouped_gemm_f64_kernel<64, 16><<<grid, kThreads, 0, st>>>(dp, 1, df, tiles, dt); break;
+    case 2: grouped_gemm_f64_kernel<16, 64><<<grid, kThreads, 0, st>>>(dp, 1, df, tiles, dt); break;
+    case 3: grouped_gemm_f64_kernel<16, 16><<<grid, kThreads, 0, st>>>(dp, 1, df, tiles, dt); break;
+    case 4: thin_gemm_f64_kernel<true><<<std::min(tiles, 152 * 8), 256, 0, st>>>(dp, 1, df, tiles); break;
+    case 6: small_k_gemm_f64_kernel<<<std::min(tiles, 152 * 8), 256, 0, st>>>(dp, 1, df, tiles); break;
+    default: thin_gemm_f64_kernel<false><<<std::min(tiles, 152 * 8), 256, 0, st>>>(dp, 1, df, tiles); break;
+  }
+  GBX_CUDA(cudaGetLastError());
+  if (ks > 1) {
+    const uint32_t chunks = (uint32_t)(((int64_t)n_a * n_b + kRedChunk - 1) / kRedChunk);
+    const int rg = (int)std::min<uint32_t>(chunks, 152u * 8u);
+    splitk_reduce_kernel<<<rg, kRedThreads, 0, st>>>(dp, &dh->red_prob, &dh->red_first, 1, chunks);
+    GBX_CUDA(cudaGetLastError());
+  }
+  return GBX_OK;
+}

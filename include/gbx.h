@@ -72,6 +72,24 @@ GBX_API int gbx_dltc_transpose(const double* d_x, const int* ids_x, double* d_y,
 GBX_API int gbx_local_contraction(int n_a, int n_b, int n_k, const double* d_A, const double* d_B, double* d_C,
                           int at, int bt, double alpha, void* stream);
 
+/* The same product as gbx_local_contraction, for callers that cannot let a
+ * library allocate device memory: a framework that has handed nearly all of
+ * the GPU's memory to its own caching pool, or a latency-bound loop whose
+ * other streams must not be stalled by the device synchronisation of
+ * cudaFree.  This entry point calls no cudaMalloc, cudaMallocAsync, cudaFree
+ * or allocating library routine.  Its descriptor and split-K partial sums
+ * live in one fixed device array of 32 MiB + 4 KiB that the library defines
+ * and every GPU that loads the library holds until the process exits.
+ * Outputs larger than 4,194,304 elements (n_a * n_b) are rejected with
+ * GBX_EINVAL.  The first call on a device looks up that array's device
+ * address (cudaGetSymbolAddress); make it before any stream capture.  All
+ * calls share the array: calls whose work overlaps on the GPU (different
+ * streams, or different host threads without ordering) race and give wrong
+ * results.
+ * No counterpart in the reference. */
+GBX_API int gbx_local_contraction_noalloc(int n_a, int n_b, int n_k, const double* d_A, const double* d_B,
+                                          double* d_C, int at, int bt, double alpha, void* stream);
+
 /* DLTC tile product c[m x n] += a[m x k] * b[k x n], row-major.
  * Replaces: void DLTC::compute(double*, double*, double*, Multiplication&)
  *           DLTC/compute.h:28 (DLTC/compute.cc:3-36). */
