@@ -48,6 +48,10 @@ def parse():
                         "this workload (7200 x 288 x 7200); 'thin' = one irrep block of t_i^e <ab||ej> "
                         "(346174 x 8 x 38, the thin-K kernel)")
     p.add_argument("--rates", action="store_true", help="build and run the arithmetic-rate probe")
+    p.add_argument("--grouped", type=int, default=0, metavar="T",
+                   help="grouped block-triple sweep instead of CCSD: T triples, m, n, k log-uniform in [8, 256], "
+                        "entries sign * 10^u, u uniform in [-6, 6]; FP64 per-triple launches vs one persistent "
+                        "graph-captured launch, split vs FP64, model vs autotuned engine choice")
     return p.parse_args()
 
 
@@ -153,6 +157,102 @@ def kernel_arm(a):
     return 0
 
 
+def grouped_arm(a):
+    """The grouped block-GEMM sweep: one set of T triples, every engine and launch mode."""
+    import numpy as np
+    import torch
+    from dtcf_gb300.leaves import Group, Triple, MODE_AUTO, MODE_FP64, MODE_SPLIT
+    T = a.grouped
+    rng = np.random.default_rng(a.seed)
+    dims = np.exp(rng.uniform(np.log(8), np.log(256), size=(T, 3))).round().astype(np.int64)
+    m, n, k = dims[:, 0], dims[:, 1], dims[:, 2]
+    oa = np.concatenate([[0], np.cumsum(m * k)])
+    ob = np.concatenate([[0], np.cumsum(n * k)])
+    oc = np.concatenate([[0], np.cumsum(m * n)])
+    g = torch.Generator(device="cuda").manual_seed(a.seed)
+
+    def entries(count):
+        sign = torch.randint(0, 2, (count,), generator=g, device="cuda", dtype=torch.int8).double() * 2 - 1
+        return sign * torch.pow(10.0, torch.rand(count, generator=g, device="cuda", dtype=torch.float64) * 12 - 6)
+
+    A = entries(int(oa[-1]))
+    B = entries(int(ob[-1]))
+    C = torch.zeros(int(oc[-1]), dtype=torch.float64, device="cuda")
+    tri = [Triple(A.data_ptr() + 8 * int(oa[i]), B.data_ptr() + 8 * int(ob[i]), C.data_ptr() + 8 * int(oc[i]),
+                  int(k[i]), 1, int(k[i]), 1, int(n[i]), int(m[i]), int(n[i]), int(k[i]), 1.0, 0) for i in range(T)]
+    flops = 2.0 * float(np.sum(m.astype(float) * n * k))
+    bytes_ = 8.0 * float(oa[-1] + ob[-1] + oc[-1])
+    # FP64 reference: one cuBLAS DGEMM per triple
+    ref = torch.empty_like(C)
+    for i in range(T):
+        ref[oc[i]:oc[i + 1]].view(int(m[i]), int(n[i])).copy_(
+            A[oa[i]:oa[i + 1]].view(int(m[i]), int(k[i])) @ B[ob[i]:ob[i + 1]].view(int(n[i]), int(k[i])).T)
+    refn = [torch.linalg.norm(ref[oc[i]:oc[i + 1]]).item() for i in range(T)]
+
+    def err():
+        d = C - ref
+        worst = 0.0
+        for i in range(T):
+            worst = max(worst, torch.linalg.norm(d[oc[i]:oc[i + 1]]).item() / refn[i])
+        return worst
+
+    stream = torch.cuda.Stream()
+    steps, warm = max(a.steps, 1), max(a.warmup, 3)
+
+    def timed(fn, graph):
+        with torch.cuda.stream(stream):
+            for _ in range(warm):
+                fn()
+        torch.cuda.synchronize()
+        run = fn
+        if graph:
+            gr = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(gr, stream=stream):
+                fn()
+            run = gr.replay
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(steps):
+                run()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    out = {}
+    t0 = time.perf_counter()
+    g64 = Group(tri, mode=MODE_FP64)
+    gsp = Group(tri, mode=MODE_SPLIT)
+    gauto = Group(tri, mode=MODE_AUTO)
+    gtune = Group(tri, mode=MODE_AUTO)
+    plan_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    gtune.autotune(reps=3, stream=stream)
+    tune_s = time.perf_counter() - t0
+    for name, grp, per, graph in [("fp64_per_triple_launches", g64, True, False),
+                                  ("fp64_persistent_graph", g64, False, True),
+                                  ("split_persistent_graph", gsp, False, True),
+                                  ("auto_model_persistent_graph", gauto, False, True),
+                                  ("autotuned_persistent_graph", gtune, False, True)]:
+        ms = timed(lambda: grp.execute(per_triple=per, stream=stream), graph)
+        C.zero_()
+        with torch.cuda.stream(stream):
+            grp.execute(per_triple=per, stream=stream)
+        torch.cuda.synchronize()
+        eng = grp.info()[0]
+        out[name] = {"ms": ms, "fp64_equiv_tflops": flops / ms / 1e9, "max_rel_frob_err": err(),
+                     "split_triples": int(sum(eng)), "launches": (int(T - sum(eng)) if per else None)}
+    line = {"metric": "grouped block-triple GEMM time per launch set", "unit": "ms", "higher_is_better": False,
+            "workload": "grouped_triples_%d_loguniform_8_256" % T, "triples": T, "seed": a.seed, "flops": flops,
+            "operand_bytes": bytes_, "l2": "inputs larger than L2 (%.2f GB)" % (bytes_ / 1e9), "steps": steps,
+            "warmup": warm, "plan_s": plan_s, "autotune_s": tune_s, "modes": out,
+            "reference": "one cuBLAS DGEMM per triple (FP64)"}
+    print(json.dumps(line))
+    for grp in (g64, gsp, gauto, gtune):
+        grp.close()
+    return 0
+
+
 def rates_arm():
     import tempfile
     src = os.path.join(ROOT, "dtcf_gb300", "measure", "rates_probe.cu")
@@ -168,6 +268,8 @@ def main():
         return rates_arm()
     if a.kernel:
         return kernel_arm(a)
+    if a.grouped:
+        return grouped_arm(a)
     if a.impl == "reference":
         if rank != 0:
             return 0

@@ -28,6 +28,11 @@ SIGNATURES = {
     "gbx_plan_flops": (_d, [_p]),
     "gbx_plan_destroy": (_i, [_p]),
     "gbx_grouped_gemm_f64": (_i, [_p, _i, _p]),
+    "gbx_group_create": (_i, [_p, _i, _i, _i, ctypes.POINTER(_p)]),
+    "gbx_group_execute": (_i, [_p, _i, _p]),
+    "gbx_group_autotune": (_i, [_p, _i, _p]),
+    "gbx_group_info": (_i, [_p, _p, _p, ctypes.POINTER(_d)]),
+    "gbx_group_destroy": (_i, [_p]),
     "gbx_split_gemm": (_i, [_p, _p, _p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, _i, _p]),
     "gbx_split_set_width": (_i, [_i]),
     "gbx_cc_default_config": (None, [_p]),

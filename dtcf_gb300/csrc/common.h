@@ -115,6 +115,7 @@ struct F64Gemm {
     int* d_first = nullptr;
     int* d_ticket = nullptr;
     int nprob = 0, total_tiles = 0, variant = 0;
+    std::vector<int> first;  // host copy of d_first (per-problem launches)
   };
   std::vector<Sub> subs;
   GemmProblem* d_all = nullptr;  // every problem (for the split-K reduction)
@@ -126,9 +127,14 @@ struct F64Gemm {
   double workspace_bytes = 0.0;
   bool async_stream_set = false;
   cudaStream_t async_stream = nullptr;
-  // async: allocate / upload stream-ordered on st (for one-shot leaf calls)
-  int build(const std::vector<GemmProblem>& probs, bool async = false, cudaStream_t st = nullptr);
+  // async: allocate / upload stream-ordered on st (for one-shot leaf calls).
+  // variants: tile shape per problem (f64_variant numbering; -1 = model).
+  int build(const std::vector<GemmProblem>& probs, bool async = false, cudaStream_t st = nullptr,
+            const std::vector<int>* variants = nullptr);
   int run(cudaStream_t st) const;
+  // One launch per problem (static schedule), then the split-K reduction:
+  // the per-launch baseline against the single persistent launch of run().
+  int run_each(cudaStream_t st) const;
   void release();
   ~F64Gemm() { release(); }
 };

@@ -317,13 +317,23 @@ void F64Gemm::release() {
   red_chunks = 0;
 }
 
-int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t st) {
+int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t st, const std::vector<int>* variants) {
   release();
   async_stream_set = async;
   async_stream = st;
   std::vector<GemmProblem> probs;
-  for (const GemmProblem& q : in)
-    if (q.m > 0 && q.n > 0) probs.push_back(q);
+  std::vector<int> want;
+  for (size_t i = 0; i < in.size(); ++i) {
+    const GemmProblem& q = in[i];
+    if (q.m <= 0 || q.n <= 0) continue;
+    probs.push_back(q);
+    int v = variants && i < variants->size() ? (*variants)[i] : -1;
+    if (v < -1 || v > 6) return fail(GBX_EINVAL, "FP64 tile variant %d", v);
+    // the thin kernels need their shape limits
+    if ((v == 4 && q.n > kThinN) || (v == 5 && q.m > kThinN) || (v == 6 && q.k > kSmallK))
+      return fail(GBX_EINVAL, "FP64 tile variant %d does not fit %d x %d x %d", v, q.m, q.n, q.k);
+    want.push_back(v);
+  }
   nprob = (int)probs.size();
   if (nprob == 0) return GBX_OK;
   // total output tiles decide how much K splitting the small problems get
@@ -336,7 +346,7 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
   for (int i = 0; i < nprob; ++i) {
     GemmProblem& q = probs[i];
     int ks = 1;
-    const int thin = f64_variant(q.m, q.n, q.k);
+    const int thin = want[i] >= 0 ? want[i] : f64_variant(q.m, q.n, q.k);
     if (thin >= 4) {  // thin and small-K kernels: no split-K
       q.ksplit = 1;
       q.kchunk = std::max(q.k, BK);
@@ -354,7 +364,7 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
     q.ksplit = ks;
     q.kchunk = std::max(chunk, BK);
     q.partial = nullptr;
-    q.pad_ = f64_variant(q.m, q.n);
+    q.pad_ = want[i] >= 0 ? want[i] : f64_variant(q.m, q.n);
     if (ks > 1) {
       q.partial = (double*)(intptr_t)(part_elems + 1);  // offset + 1, patched below
       part_elems += (int64_t)ks * q.m * q.n;
@@ -397,7 +407,7 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
       if (v == 4) tiles += (q.m + 255) / 256;
       else if (v == 5) tiles += (q.n + 255) / 256;
       else if (v == 6) tiles += ((int64_t)q.m * q.n + kSmallKElems - 1) / kSmallKElems;
-      else tiles += (int64_t)f64_tiles(q.m, q.n) * q.ksplit;
+      else tiles += (int64_t)((q.m + f64_tile_m(v) - 1) / f64_tile_m(v)) * ((q.n + f64_tile_n(v) - 1) / f64_tile_n(v)) * q.ksplit;
     }
     if (vp.empty()) continue;
     if (tiles >= (1ll << 31)) return fail(GBX_EUNSUPPORTED, "grouped GEMM has too many work items");
@@ -410,6 +420,8 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
     GBX_TRY(alloc((void**)&sb.d_ticket, sizeof(int)));
     GBX_TRY(copy(sb.d_probs, vp.data(), sizeof(GemmProblem) * vp.size()));
     GBX_TRY(copy(sb.d_first, first.data(), sizeof(int) * vp.size()));
+    sb.first = first;
+    sb.first.push_back((int)tiles);
     subs.push_back(sb);
   }
   if (nred) {
@@ -469,6 +481,40 @@ int F64Gemm::run(cudaStream_t st) const {
   return GBX_OK;
 }
 
+
+namespace {
+// A single-problem launch of variant v over work items [0, tiles).
+int launch_one(int v, const GemmProblem* prob, const int* zero, int tiles, cudaStream_t st) {
+  const int grid = std::min(tiles, 152 * 4), tgrid = std::min(tiles, 152 * 8);
+  switch (v) {
+    case 0: grouped_gemm_f64_kernel<64, 64><<<grid, kThreads, 0, st>>>(prob, 1, zero, tiles, nullptr); break;
+    case 1: grouped_gemm_f64_kernel<64, 16><<<grid, kThreads, 0, st>>>(prob, 1, zero, tiles, nullptr); break;
+    case 2: grouped_gemm_f64_kernel<16, 64><<<grid, kThreads, 0, st>>>(prob, 1, zero, tiles, nullptr); break;
+    case 3: grouped_gemm_f64_kernel<16, 16><<<grid, kThreads, 0, st>>>(prob, 1, zero, tiles, nullptr); break;
+    case 4: thin_gemm_f64_kernel<true><<<tgrid, 256, 0, st>>>(prob, 1, zero, tiles); break;
+    case 6: small_k_gemm_f64_kernel<<<tgrid, 256, 0, st>>>(prob, 1, zero, tiles); break;
+    default: thin_gemm_f64_kernel<false><<<tgrid, 256, 0, st>>>(prob, 1, zero, tiles); break;
+  }
+  GBX_CUDA(cudaGetLastError());
+  return GBX_OK;
+}
+}  // namespace
+
+int F64Gemm::run_each(cudaStream_t st) const {
+  if (nprob == 0) return GBX_OK;
+  for (const Sub& sb : subs) {
+    // d_first[0] is 0: problem i is launched as a one-problem group whose
+    // first-work-item table is that zero
+    for (int i = 0; i < sb.nprob; ++i)
+      GBX_TRY(launch_one(sb.variant, sb.d_probs + i, sb.d_first, sb.first[i + 1] - sb.first[i], st));
+  }
+  if (nred) {
+    int rg = (int)std::min<uint32_t>(red_chunks, 152u * 8u);
+    splitk_reduce_kernel<<<rg, kRedThreads, 0, st>>>(d_all, d_red_prob, d_red_first, nred, red_chunks);
+    GBX_CUDA(cudaGetLastError());
+  }
+  return GBX_OK;
+}
 }  // namespace gbx
 
 // ---- allocation-free local contraction ----------------------------------

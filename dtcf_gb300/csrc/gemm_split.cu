@@ -59,6 +59,7 @@ struct SplitRowSet {   // one operand of one problem for the split kernel
   int64_t slice_stride, Kp;
   int* exps;
   int64_t first_row;   // first (row, K chunk) work item of this set
+  int64_t ld;          // source row stride (elements)
 };
 
 struct DevProblem {
@@ -176,8 +177,11 @@ struct TileInfo {
 template <int BN>
 __device__ __forceinline__ TileInfo decode_tile(const GemmParams& P, int tile) {
   TileInfo t;
-  int p = 0;
-  while (p + 1 < P.nprob && P.tile_first[p + 1] <= tile) ++p;
+  int p = 0, hi = P.nprob - 1;
+  while (p < hi) {
+    const int mid = (p + hi + 1) >> 1;
+    if (P.tile_first[mid] <= tile) p = mid; else hi = mid - 1;
+  }
   const DevProblem& pr = P.probs[p];
   int local = tile - P.tile_first[p];
   const int per_k = pr.tiles_m * pr.tiles_n;
@@ -711,7 +715,7 @@ __global__ void __launch_bounds__(256) row_exponent_kernel(const SplitRowSet* __
     int64_t row, k0;
     locate_chunk(sets, nsets, chunk, set, row, k0);
     const SplitRowSet& rs = sets[set];
-    const double* src = rs.src + row * rs.K;
+    const double* src = rs.src + row * rs.ld;
     const int64_t k1 = min(rs.K, k0 + kSplitChunk);
     uint32_t emax = 0;
     for (int64_t k = k0 + threadIdx.x; k < k1; k += 256)
@@ -737,7 +741,7 @@ __global__ void __launch_bounds__(256) digits_kernel(const SplitRowSet* __restri
     int64_t row, k0;
     locate_chunk(sets, nsets, chunk, set, row, k0);
     const SplitRowSet& rs = sets[set];
-    const double* src = rs.src + row * rs.K;
+    const double* src = rs.src + row * rs.ld;
     __nv_bfloat16* dst = rs.dst + row * rs.Kp;
     const uint32_t emax = (uint32_t)rs.exps[row];
     const int64_t k1 = min(rs.K, k0 + kSplitChunk);
@@ -777,7 +781,7 @@ __global__ void __launch_bounds__(256) split_short_rows_kernel(const SplitRowSet
     }
     const SplitRowSet& rs = sets[lo];
     const int64_t row = rg - rs.first_row;
-    const double* src = rs.src + row * rs.K;
+    const double* src = rs.src + row * rs.ld;
     uint32_t emax = 0;
     for (int64_t k = lane; k < rs.K; k += 32)
       emax = max(emax, (uint32_t)((__double_as_longlong(__ldg(src + k)) >> 52) & 0x7FF));
@@ -938,7 +942,8 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
     if (p.M >= (1ll << 30) || p.N >= (1ll << 30) || p.K >= (1ll << 30)) return fail(GBX_EUNSUPPORTED, "split problem too large");
     // thin-K problems (one k-block, at most 32 columns) take the thin kernel
     const bool thin = p.K <= BK && p.N <= kThinBN && S <= 7;
-    const int bn = thin ? kThinBN : choose_width(p.N);
+    const int bn = thin ? kThinBN : (p.width ? p.width : choose_width(p.N));
+    if (!thin && bn != 32 && bn != 64 && bn != 128 && bn != 256) return fail(GBX_EINVAL, "split tile width %d", bn);
     sp->width.push_back(bn);
     sp->thin.push_back(thin);
     Off o;
@@ -977,8 +982,8 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
     const int bn = sp->width[i];
     // row sets are grouped by the plan operand they come from, so constant
     // plan operands can be split once
-    SplitRowSet a{p.A, p.M, p.K, sp->d_slices + o.a, o.Mp * o.Kp, o.Kp, sp->d_exps + o.ea, 0};
-    SplitRowSet b{p.B, p.N, p.K, sp->d_slices + o.b, o.Np * o.Kp, o.Kp, sp->d_exps + o.eb, 0};
+    SplitRowSet a{p.A, p.M, p.K, sp->d_slices + o.a, o.Mp * o.Kp, o.Kp, sp->d_exps + o.ea, 0, p.lda ? p.lda : p.K};
+    SplitRowSet b{p.B, p.N, p.K, sp->d_slices + o.b, o.Np * o.Kp, o.Kp, sp->d_exps + o.eb, 0, p.ldb ? p.ldb : p.K};
     SplitRowSet& to_a = p.a_is_plan_b ? b : a;  // rows that come from plan A
     SplitRowSet& to_b = p.a_is_plan_b ? a : b;
     if (to_a.K <= kShortRow) {
@@ -1031,7 +1036,7 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
       red_first.push_back(red_total);
       red_total += p.M * p.N;
     }
-    d.ldc = p.N;
+    d.ldc = p.ldc ? p.ldc : p.N;
     dp.push_back(d);
     CUtensorMap ma, mb;
     GBX_TRY(encode_slices(&ma, sp->d_slices + o.a, S, o.Mp, o.Kp, BM));

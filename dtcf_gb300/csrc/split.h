@@ -9,8 +9,8 @@
 
 namespace gbx {
 
-// C[M x N] = A[M x K] * B[N x K]^T, all row-major FP64 (ld = K for A and B,
-// N for C).
+// C[M x N] = A[M x K] * B[N x K]^T, all row-major FP64 (row strides lda,
+// ldb, ldc; 0 means K for A and B, N for C).
 struct SplitProblem {
   const double* A;
   const double* B;
@@ -19,6 +19,8 @@ struct SplitProblem {
   // the GEMM's A rows come from the plan's packed B operand (swapped
   // orientation); split_operands(plan_a, plan_b) maps accordingly
   bool a_is_plan_b = false;
+  int64_t lda = 0, ldb = 0, ldc = 0;
+  int width = 0;  // output tile width 32/64/128/256; 0 = the built-in model
 };
 
 struct SplitPlan;

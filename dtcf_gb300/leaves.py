@@ -110,3 +110,46 @@ def split_gemm(A, B, C, slices=0, stream=None):
     N = B.shape[0]
     check(lib().gbx_split_gemm(_ptr(A), _ptr(B), _ptr(C), M, N, K, slices, _stream(stream)))
     return C
+
+
+MODE_FP64, MODE_SPLIT, MODE_AUTO = 0, 1, 2
+
+
+class Group:
+    """A planned set of block triples (gbx_group_*): C_t (+)= alpha A_t B_t^T.
+
+    ``triples`` are Triple structs over device memory that must outlive the
+    group.  ``execute(per_triple=False)`` runs one persistent launch per
+    kernel kind; ``per_triple=True`` launches each FP64 triple separately.
+    """
+
+    def __init__(self, triples, mode=MODE_AUTO, slices=0):
+        self._arr = (Triple * len(triples))(*triples)
+        self.n = len(triples)
+        h = ctypes.c_void_p()
+        check(lib().gbx_group_create(ctypes.cast(self._arr, ctypes.c_void_p), self.n, mode, slices,
+                                     ctypes.byref(h)))
+        self._h = h
+
+    def execute(self, per_triple=False, stream=None):
+        check(lib().gbx_group_execute(self._h, 1 if per_triple else 0, _stream(stream)))
+
+    def autotune(self, reps=3, stream=None):
+        check(lib().gbx_group_autotune(self._h, reps, _stream(stream)))
+
+    def info(self):
+        """(engines, params, flops): per-triple engine (0 FP64, 1 split) and tile parameter."""
+        eng = (ctypes.c_int * max(self.n, 1))()
+        par = (ctypes.c_int * max(self.n, 1))()
+        fl = ctypes.c_double()
+        check(lib().gbx_group_info(self._h, ctypes.cast(eng, ctypes.c_void_p), ctypes.cast(par, ctypes.c_void_p),
+                                   ctypes.byref(fl)))
+        return list(eng)[:self.n], list(par)[:self.n], fl.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gbx_group_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

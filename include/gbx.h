@@ -194,6 +194,40 @@ typedef struct {
  * stream-ordered temporaries.  Triples whose C overlap must not share a call. */
 GBX_API int gbx_grouped_gemm_f64(const gbx_triple* triples, int num_triples, void* stream);
 
+/* ---- planned triple groups (engine choice and autotuning) --------------- */
+
+#define GBX_MODE_AUTO 2 /* per triple: FP64 or split, by the throughput model */
+
+typedef struct gbx_group gbx_group;
+
+/* Plan a set of triples once (the per-block-pair dgemm calls of
+ * transpose_and_dgemm, contraction.cc:1779-1976, and of DLTC task_mul,
+ * DLTC/task.cc:83-137, as one batch).  mode GBX_MODE_FP64 runs every triple
+ * on the FP64 pipe (DMMA tile shapes 64x64 / 64x16 / 16x64 / 16x16, thin and
+ * small-K kernels), GBX_MODE_SPLIT on the split engine (needs a_cs = b_cs =
+ * 1; GBX_EUNSUPPORTED otherwise), GBX_MODE_AUTO picks per triple.  slices:
+ * split slices (0 = 6).  The triple array is copied; operand memory must
+ * stay valid while the group exists.  Triples whose C overlap must not share
+ * a group. */
+GBX_API int gbx_group_create(const gbx_triple* triples, int num_triples, int mode, int slices, gbx_group** out);
+/* Run every triple: one persistent launch per kernel kind (per_triple = 0;
+ * capturable in a CUDA graph, allocates nothing), or one launch per FP64
+ * triple (per_triple = 1, the per-dgemm-call baseline; split triples still
+ * run batched). */
+GBX_API int gbx_group_execute(gbx_group* g, int per_triple, void* stream);
+/* Autotuner: triples are classed by shape (log4 bins of m, n, k); for each
+ * class every candidate (the four FP64 tile shapes; split output widths 32 to
+ * 256 in both orientations, as the mode allows) is timed with CUDA events on
+ * scratch outputs (marginal cost of 4 copies over 1, best of reps) and the
+ * fastest is kept; the group is then re-planned.  Synchronises the stream;
+ * writes no triple's C. */
+GBX_API int gbx_group_autotune(gbx_group* g, int reps, void* stream);
+/* Per triple: engine (0 FP64, 1 split) and parameter (FP64 tile variant, -1
+ * = model; split: 2 * width + swapped); flops = 2 * sum m*n*k.  Any pointer
+ * may be NULL. */
+GBX_API int gbx_group_info(const gbx_group* g, int* engines, int* params, double* flops);
+GBX_API int gbx_group_destroy(gbx_group* g);
+
 #ifdef __cplusplus
 }
 #endif
