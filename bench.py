@@ -52,6 +52,16 @@ def parse():
                    help="grouped block-triple sweep instead of CCSD: T triples, m, n, k log-uniform in [8, 256], "
                         "entries sign * 10^u, u uniform in [-6, 6]; FP64 per-triple launches vs one persistent "
                         "graph-captured launch, split vs FP64, model vs autotuned engine choice")
+    p.add_argument("--serve", type=int, default=0, metavar="J",
+                   help="serving loop instead of the CCSD step: J concurrent jobs (o uniform in [16, 64], "
+                        "v = o * U[4, 6], 8-irrep symmetry on for half), Poisson iteration requests")
+    p.add_argument("--serve-requests", type=int, default=2, help="iteration requests per job")
+    p.add_argument("--serve-rate", type=float, default=2.0, help="aggregate Poisson arrival rate (requests/s)")
+    p.add_argument("--serve-budget-gb", type=float, default=160.0, help="admission budget for resident job state")
+    p.add_argument("--serve-slots", type=int, default=4, help="requests in flight at once")
+    p.add_argument("--serve-limit", type=float, default=300.0, help="time limit of each serving run (s)")
+    p.add_argument("--serve-engines", default="split,fp64", help="engines to serve with, in order")
+    p.add_argument("--serve-o-max", type=int, default=64, help="largest occupied count of a job")
     return p.parse_args()
 
 
@@ -253,6 +263,68 @@ def grouped_arm(a):
     return 0
 
 
+def serve_jobs(a):
+    """The synthetic job mix and request stream of a serving run (seeded)."""
+    import numpy as np
+    rng = np.random.default_rng(a.seed)
+    jobs = []
+    for j in range(a.serve):
+        o = int(rng.integers(16, a.serve_o_max + 1))
+        v = int(round(o * rng.uniform(4.0, 6.0)))
+        sym = j % 2 == 0
+        method = "ccsd" if rng.uniform() < 0.5 else "ccd"
+        jobs.append(dict(nocc=o, nvir=v, nirrep=8 if sym else 1, max_block=40 if sym else 16,
+                         min_block=4 if sym else 1, method=method, seed=1000 + j))
+    n = a.serve * a.serve_requests
+    arrivals = np.cumsum(rng.exponential(1.0 / a.serve_rate, n))
+    who = np.repeat(np.arange(a.serve), a.serve_requests)
+    rng.shuffle(who)
+    return jobs, list(zip(who.tolist(), arrivals.tolist()))
+
+
+def serve_arm(a):
+    """The serving loop over the job mix, once per engine; one JSON line."""
+    import torch
+    from dtcf_gb300.cc import config
+    from dtcf_gb300.serve import Server
+    torch.cuda.set_device(0)
+    jobs, stream = serve_jobs(a)
+    out, energies = {}, {}
+    for eng in a.serve_engines.split(","):
+        s = Server(budget_bytes=a.serve_budget_gb * 1e9, slots=a.serve_slots)
+        ids = [s.add_job(config(engine=eng, **j)) for j in jobs]
+        for job, t in stream:
+            s.submit(ids[job], t)
+        clocks = Clocks(0)
+        clocks.start()
+        t0 = time.perf_counter()
+        s.run(time_limit_s=a.serve_limit)
+        wall = time.perf_counter() - t0
+        st = s.stats()
+        res = s.results()
+        fps = list(s.footprints)
+        s.close()
+        st["wall_s"] = wall
+        st["clocks"] = clocks.stop()
+        st["jobs_over_budget"] = sum(1 for f in fps if f > a.serve_budget_gb * 1e9)
+        out[eng] = st
+        energies[eng] = {(r["job"], r["iteration"]): r["energy"] for r in res if r["status"] == 0}
+        print(json.dumps({"engine": eng, **st}), file=sys.stderr, flush=True)
+    diff = None
+    if len(energies) == 2:
+        e1, e2 = energies.values()
+        common = set(e1) & set(e2)
+        if common:
+            diff = max(abs(e1[k] - e2[k]) for k in common)
+    print(json.dumps({"metric": "CC serving: p50/p99 per-iteration request latency and aggregate iter/s", "unit": "s",
+                      "workload": "cc_serving_%djobs_o16-%d_v4-6o_halfsym" % (a.serve, a.serve_o_max),
+                      "jobs": a.serve, "requests_per_job": a.serve_requests, "arrival_rate_per_s": a.serve_rate,
+                      "budget_gb": a.serve_budget_gb, "slots": a.serve_slots, "time_limit_s": a.serve_limit,
+                      "seed": a.seed, "engines": out, "energy_max_diff_split_vs_fp64_eh": diff,
+                      "data": "synthetic (seeded)"}))
+    return 0
+
+
 def rates_arm():
     import tempfile
     src = os.path.join(ROOT, "dtcf_gb300", "measure", "rates_probe.cu")
@@ -270,6 +342,8 @@ def main():
         return kernel_arm(a)
     if a.grouped:
         return grouped_arm(a)
+    if a.serve:
+        return serve_arm(a)
     if a.impl == "reference":
         if rank != 0:
             return 0

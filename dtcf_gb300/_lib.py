@@ -33,9 +33,19 @@ SIGNATURES = {
     "gbx_group_autotune": (_i, [_p, _i, _p]),
     "gbx_group_info": (_i, [_p, _p, _p, ctypes.POINTER(_d)]),
     "gbx_group_destroy": (_i, [_p]),
+    "gbx_server_create": (_i, [_p, ctypes.POINTER(_p)]),
+    "gbx_server_add_job": (_i, [_p, _p, ctypes.POINTER(_i), ctypes.POINTER(_d)]),
+    "gbx_server_submit": (_i, [_p, _i, _d]),
+    "gbx_server_run": (_i, [_p, _d]),
+    "gbx_server_results": (_i, [_p, _p, ctypes.POINTER(_i)]),
+    "gbx_server_stats": (_i, [_p, _p]),
+    "gbx_server_destroy": (_i, [_p]),
     "gbx_split_gemm": (_i, [_p, _p, _p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, _i, _p]),
     "gbx_split_set_width": (_i, [_i]),
     "gbx_cc_default_config": (None, [_p]),
+    "gbx_cc_footprint": (_i, [_p, ctypes.POINTER(_d), ctypes.POINTER(_d), ctypes.POINTER(_d)]),
+    "gbx_cc_capture": (_i, [_p]),
+    "gbx_cc_check": (_i, [_p]),
     "gbx_cc_create": (_i, [_p, _p, ctypes.POINTER(_p)]),
     "gbx_cc_enqueue": (_i, [_p, _i, _p]),
     "gbx_cc_iterate": (_i, [_p, _i, _p, _p]),

@@ -5,8 +5,10 @@
 #include "split.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
+#include <set>
 
 namespace gbx {
 
@@ -83,7 +85,13 @@ struct gbx_cc_job {
   std::map<std::string, std::unique_ptr<CCTensor>> T;
   std::vector<std::unique_ptr<ContractionPlan>> cplans;
   std::vector<std::unique_ptr<SumPlan>> splans;
-  std::vector<std::function<int(cudaStream_t)>> steps;  // one iteration
+  std::vector<std::function<int(cudaStream_t)>> steps;       // one iteration
+  std::vector<std::function<int(cudaStream_t)>> init_steps;  // once, after the MP2 guess
+  std::set<std::string> dynamic_use;  // tensors read or written outside constant plan operands
+  std::vector<std::pair<CCTensor*, CCTensor*>> plan_operands;  // A, B of each contraction plan
+  unsigned char* d_arena = nullptr;  // packed operands and split slices, shared by every plan
+  size_t arena_bytes = 0;
+  std::atomic<int64_t> account{0};  // device bytes the job's allocations hold
   struct StepInfo {
     std::string name;
     int kind;  // 0 contraction, 1 sum, 2 zero, 3 denominator, 4 energy
@@ -112,6 +120,7 @@ struct gbx_cc_job {
     splans.clear();
     T.clear();
     tilesets.clear();
+    dev_free(d_arena);
     dev_free(d_irrep);
     dev_free(d_eps);
     dev_free(d_mag);
@@ -123,14 +132,16 @@ struct gbx_cc_job {
   std::shared_ptr<BlockDim> dim_of(char s) { return s == 'o' ? occ : vir; }
   int gstart(char s, int b) { return s == 'o' ? (int)occ->start[b] : o + (int)vir->start[b]; }
 
-  int tensor(const std::string& name, const std::string& spaces) {
+  // Declares a tensor (layout only; device memory comes with materialize()).
+  // groups: antisymmetric index groups (-1 = none) of a tensor that stores
+  // only its canonical tiles, as RRR stores unique blocks (tensor.cc:617-640);
+  // readers recover the other tiles by permutation and sign.
+  int tensor(const std::string& name, const std::string& spaces, const std::vector<int>& groups = {}) {
     auto t = std::make_unique<CCTensor>();
     t->spaces = spaces;
     std::vector<std::shared_ptr<BlockDim>> dims;
     for (char c : spaces) dims.push_back(dim_of(c));
-    t->L = TensorLayout::full(dims, {}, 1, false);
-    GBX_TRY(dev_alloc((void**)&t->d, sizeof(double) * std::max<int64_t>(1, t->L.nelem)));
-    GBX_CUDA(cudaMemset(t->d, 0, sizeof(double) * std::max<int64_t>(1, t->L.nelem)));
+    t->L = TensorLayout::full(dims, groups, groups.empty() ? 1 : -1, !groups.empty());
     T[name] = std::move(t);
     return GBX_OK;
   }
@@ -170,20 +181,22 @@ struct gbx_cc_job {
     std::unique_ptr<ContractionPlan> p;
     Engine e = cfg.engine == GBX_MODE_SPLIT ? Engine::Split : Engine::F64;
     GBX_TRY(plan_contraction(A->L, B->L, C->L, labels(la), labels(lb), labels(lc), e, cfg.slices, p,
-                             cfg.split_all != 0));
-    // integrals never change: pack and split them once, here
+                             cfg.split_all != 0, /*defer=*/true));
+    // integrals never change: packed and split once, when the job is built
     p->a_static = is_integral(a);
     p->b_static = is_integral(b);
-    if (p->a_static || p->b_static) GBX_TRY(p->prepare_static(A->d, B->d, 0));
+    if (!p->a_static) dynamic_use.insert(a);
+    if (!p->b_static) dynamic_use.insert(b);
+    dynamic_use.insert(c);
     flops += p->flops;
     gemm_flops += p->gemm_flops;
     ContractionPlan* pp = p.get();
-    double *dA = A->d, *dB = B->d, *dC = C->d;
-    steps.push_back([=](cudaStream_t st) { return pp->execute(dA, dB, dC, alpha, st); });
+    steps.push_back([=](cudaStream_t st) { return pp->execute(A->d, B->d, C->d, alpha, st); });
     info.push_back({std::string(c) + "[" + lc + "]+=" + a + "[" + la + "]*" + b + "[" + lb + "]", 0, pp->flops,
                     8.0 * (double)(A->L.nelem + B->L.nelem + 2 * C->L.nelem), (int)cplans.size()});
     launches += 4;
     cplans.push_back(std::move(p));
+    plan_operands.push_back({A, B});
     return GBX_OK;
   }
 
@@ -193,10 +206,11 @@ struct gbx_cc_job {
     GBX_TRY(check_labels(C, lc, c));
     GBX_TRY(check_labels(A, la, a));
     std::unique_ptr<SumPlan> p;
-    GBX_TRY(plan_sum(A->L, C->L, labels(la), labels(lc), coef, p));
+    GBX_TRY(plan_sum(A->L, C->L, labels(la), labels(lc), coef, p, /*defer=*/true));
     SumPlan* pp = p.get();
-    double *dA = A->d, *dC = C->d;
-    steps.push_back([=](cudaStream_t st) { return pp->execute(dA, dC, 1.0, st); });
+    dynamic_use.insert(a);
+    dynamic_use.insert(c);
+    steps.push_back([=](cudaStream_t st) { return pp->execute(A->d, C->d, 1.0, st); });
     info.push_back({std::string(c) + "[" + lc + "]+=" + a + "[" + la + "]", 1, 0.0,
                     8.0 * (double)(A->L.nelem + 2 * C->L.nelem)});
     launches += 1;
@@ -206,10 +220,10 @@ struct gbx_cc_job {
 
   int zero(const char* c) {
     CCTensor* C = get(c);
-    double* d = C->d;
     size_t bytes = sizeof(double) * C->L.nelem;
+    dynamic_use.insert(c);
     steps.push_back([=](cudaStream_t st) {
-      GBX_CUDA(cudaMemsetAsync(d, 0, bytes, st));
+      GBX_CUDA(cudaMemsetAsync(C->d, 0, bytes, st));
       return GBX_OK;
     });
     info.push_back({std::string("zero ") + c, 2, 0.0, (double)bytes});
@@ -240,31 +254,32 @@ struct gbx_cc_job {
     return tilesets.back().get();
   }
 
-  int denom(const char* out, const char* in, CCTileSet* ts) {
-    double* dout = get(out)->d;
-    const double* din = get(in)->d;
-    CCDeviceTables tb = tab;
-    steps.push_back([=](cudaStream_t st) { return run_cc_tiles(*ts, CC_OP_DENOM, tb, din, dout, st); });
-    info.push_back({std::string(out) + "=" + in + "/D", 3, 0.0, 16.0 * (double)get(out)->L.nelem});
+  // out = in / D over the tiles of out (the tile set is built with the job)
+  int denom(const char* out, const char* in, CCTileSet** ts) {
+    CCTensor *O = get(out), *I = get(in);
+    dynamic_use.insert(out);
+    dynamic_use.insert(in);
+    steps.push_back([=](cudaStream_t st) { return run_cc_tiles(**ts, CC_OP_DENOM, tab, I->d, O->d, st); });
+    info.push_back({std::string(out) + "=" + in + "/D", 3, 0.0, 16.0 * (double)O->L.nelem});
     launches += 1;
     return GBX_OK;
   }
 
   int energy_step() {
-    const double* V = get("OOVV")->d;
-    const double* tau = get(cfg.method == GBX_CC_CCSD ? "tau" : "t2")->d;
-    int64_t n = get("OOVV")->L.nelem;
-    double* part = d_partial;
-    double* hist = d_hist;
-    int* cnt = d_count;
-    int np = npartial, cap = hist_cap;
-    steps.push_back([=](cudaStream_t st) { return gbx::run_energy(V, tau, n, part, np, hist, cnt, cap, st); });
+    CCTensor *V = get("OOVV"), *tau = get(cfg.method == GBX_CC_CCSD ? "tau" : "t2");
+    dynamic_use.insert("OOVV");
+    int64_t n = V->L.nelem;
+    steps.push_back([=](cudaStream_t st) {
+      return gbx::run_energy(V->d, tau->d, n, d_partial, npartial, d_hist, d_count, hist_cap, st);
+    });
     info.push_back({"energy", 4, 2.0 * (double)n, 16.0 * (double)n});
     launches += 2;
     return GBX_OK;
   }
 
-  int build();
+  int plan_all();
+  int materialize(cudaStream_t st);
+  int footprint(double* resident, double* peak) const;
   int tau_steps();
 };
 
@@ -281,7 +296,7 @@ int gbx_cc_job::tau_steps() {
   return GBX_OK;
 }
 
-int gbx_cc_job::build() {
+int gbx_cc_job::plan_all() {
   const bool sd = cfg.method == GBX_CC_CCSD;
   // amplitudes, residuals, intermediates
   GBX_TRY(tensor("t2", "oovv"));
@@ -289,7 +304,12 @@ int gbx_cc_job::build() {
   GBX_TRY(tensor("Xa", "oovv"));
   GBX_TRY(tensor("Fae", "vv"));
   GBX_TRY(tensor("Fmi", "oo"));
-  GBX_TRY(tensor("Wmnij", "oooo"));
+  // W_mnij is antisymmetric in mn and in ij: canonical tiles only
+  GBX_TRY(tensor("Wmnij", "oooo", {0, 0, 1, 1}));
+  // both ladder-type terms of R2 (tau W_mnij and tau <ab||ef>) are
+  // antisymmetric in ij and in ab: they are formed on canonical tiles (a
+  // quarter of the work) and expanded into R2 once
+  GBX_TRY(tensor("Lad", "oovv", {0, 0, 1, 1}));
   GBX_TRY(tensor("Wmbej", "ovvo"));
   GBX_TRY(tensor("Q", "oovv"));
   for (const char* nm : {"OOOO", "OOVV", "OVVO", "VVVV"}) {
@@ -306,7 +326,7 @@ int gbx_cc_job::build() {
     GBX_TRY(tensor("Fbe", "vv"));
     GBX_TRY(tensor("Fmj", "oo"));
     GBX_TRY(tensor("Xoooo", "oooo"));
-    GBX_TRY(tensor("Zp", "ooov"));
+    GBX_TRY(tensor("Zp", "ooov", {0, 0, -1, -1}));  // antisymmetric in ij
     GBX_TRY(tensor("V3", "oovo"));
     for (const char* nm : {"OOOV", "OVVV", "OOVO", "OVOV", "VVVO", "OVOO"}) {
       std::string sp;
@@ -314,33 +334,16 @@ int gbx_cc_job::build() {
       GBX_TRY(tensor(nm, sp));
     }
   }
-  // integrals on the device
-  cudaStream_t st0 = 0;
-  for (auto& kv : T) {
-    const std::string& nm = kv.first;
-    bool integ = nm.size() == 4 && std::all_of(nm.begin(), nm.end(), [](char c) { return c == 'O' || c == 'V'; });
-    if (!integ) continue;
-    CCTileSet* ts = tileset(kv.second.get());
-    if (!ts) return fail(GBX_ENOMEM, "tile set upload failed");
-    GBX_TRY(run_cc_tiles(*ts, CC_OP_INTEGRAL, tab, nullptr, kv.second->d, st0));
-  }
-  den2 = tileset(get("t2"));
-  if (sd) den1 = tileset(get("t1"));
-  if (!den2 || (sd && !den1)) return fail(GBX_ENOMEM, "tile set upload failed");
-  // MP2 guess t2 = <ij||ab> / D, t1 = 0, energy 0
-  GBX_TRY(run_cc_tiles(*den2, CC_OP_DENOM, tab, get("OOVV")->d, get("t2")->d, st0));
   const char* TAU = sd ? "tau" : "t2";
   const char* TAUT = sd ? "taut" : "t2";
   if (sd) {
-    // initial tau / taut from the guess, run once outside the iteration
+    // initial tau / taut from the guess, run once when the job is built
     size_t first = steps.size();
     GBX_TRY(tau_steps());
-    for (size_t i = first; i < steps.size(); ++i) GBX_TRY(steps[i](st0));
+    init_steps.assign(steps.begin() + first, steps.end());
     steps.resize(first);
     info.resize(first);
   }
-  GBX_TRY(gbx::run_energy(get("OOVV")->d, get(TAU)->d, get("OOVV")->L.nelem, d_partial, npartial, d_hist, d_count,
-                          hist_cap, st0));
   launches = 0;
   flops = 0.0;
   gemm_flops = 0.0;
@@ -415,10 +418,12 @@ int gbx_cc_job::build() {
   GBX_TRY(contract("Xa", "ijab", "t2", "imab", FMJ, "mj", 1.0));
   GBX_TRY(sum("R2", "ijab", "Xa", "ijab", -1.0));
   GBX_TRY(sum("R2", "ijab", "Xa", "jiab", 1.0));
-  // 1/2 tau_mn^ab W_mnij
-  GBX_TRY(contract("R2", "ijab", TAU, "mnab", "Wmnij", "mnij", 0.5));
-  // 1/2 tau_ij^ef <ab||ef>: the ladder, integrals as the (static) A operand
-  GBX_TRY(contract("R2", "ijab", "VVVV", "abef", TAU, "ijef", 0.5));
+  // 1/2 tau_mn^ab W_mnij + 1/2 tau_ij^ef <ab||ef> (the ladder, integrals as
+  // the static A operand), on canonical tiles, then into R2
+  GBX_TRY(zero("Lad"));
+  GBX_TRY(contract("Lad", "ijab", TAU, "mnab", "Wmnij", "mnij", 0.5));
+  GBX_TRY(contract("Lad", "ijab", "VVVV", "abef", TAU, "ijef", 0.5));
+  GBX_TRY(sum("R2", "ijab", "Lad", "ijab", 1.0));
   if (sd) {
     // -1/2 P(ab) t_m^b sum_ef tau_ij^ef <am||ef> = +1/2 P(ab) sum_m t_m^b Z'_ijma
     GBX_TRY(zero("Zp"));
@@ -453,12 +458,137 @@ int gbx_cc_job::build() {
     GBX_TRY(sum("R2", "ijab", "Xa", "ijba", 1.0));
   }
   // Jacobi update and energy
-  GBX_TRY(denom("t2", "R2", den2));
+  GBX_TRY(denom("t2", "R2", &den2));
   if (sd) {
-    GBX_TRY(denom("t1", "R1", den1));
+    GBX_TRY(denom("t1", "R1", &den1));
     GBX_TRY(tau_steps());
   }
   GBX_TRY(energy_step());
+  return GBX_OK;
+}
+
+namespace {
+double up256d(double x) { return std::ceil(x / 256.0) * 256.0; }
+}  // namespace
+
+// An integral tensor read only as constant plan operands: released once those
+// operands are packed and split.
+bool gbx_cc_job_static_only(const gbx_cc_job& j, const std::string& name) {
+  return gbx_cc_job::is_integral(name.c_str()) && !j.dynamic_use.count(name);
+}
+
+// Device bytes of the built job: what stays resident, and the peak while it
+// is being built (integral tiles and constant-operand scratch included).
+int gbx_cc_job::footprint(double* resident, double* peak) const {
+  double keep = 0.0, transient = 0.0, ws = 0.0, scratch = 0.0;
+  for (auto& kv : T) {
+    const double b = up256d(8.0 * (double)std::max<int64_t>(1, kv.second->L.nelem));
+    if (gbx_cc_job_static_only(*this, kv.first)) transient += b; else keep += b;
+  }
+  for (auto& p : cplans) {
+    size_t k = 0, w = 0, sc = 0;
+    GBX_TRY(p->sizes(&k, &w, &sc));
+    keep += (double)k + p->f64_workspace_estimate();
+    ws = std::max(ws, (double)w);
+    scratch = std::max(scratch, (double)sc);
+  }
+  for (auto& p : splans)
+    keep += (double)(p->moves.host.size() * sizeof(MoveDesc) + (p->moves.host.size() + 1) * sizeof(uint32_t));
+  auto tiles_bytes = [](const TensorLayout& L) {
+    return up256d((double)L.tiles.size() * sizeof(CCTile)) + up256d(4.0 * (double)(L.tiles.size() + 1));
+  };
+  keep += tiles_bytes(T.at("t2")->L);
+  if (T.count("t1")) keep += tiles_bytes(T.at("t1")->L);
+  for (auto& kv : T)
+    if (is_integral(kv.first.c_str())) transient += tiles_bytes(kv.second->L);
+  keep += up256d(4.0 * n) + up256d(8.0 * n) + up256d(8.0 * (2 * n + 1)) + up256d(8.0 * npartial) +
+          up256d(8.0 * hist_cap) + 256.0;
+  keep += ws;
+  if (resident) *resident = keep;
+  if (peak) *peak = keep + transient + scratch;
+  return GBX_OK;
+}
+
+// Allocates and fills the job: orbital tables, tensors, integrals, the plan
+// arena, constant operands (packed and split once), the MP2 guess and the
+// initial energy.  Runs on the legacy default stream `st` and waits for it.
+int gbx_cc_job::materialize(cudaStream_t st) {
+  const bool sd = cfg.method == GBX_CC_CCSD;
+  std::vector<double> mag(2 * n + 1);
+  for (size_t d = 0; d < mag.size(); ++d) mag[d] = cfg.v_scale * std::exp(-(double)d / cfg.v_decay);
+  GBX_TRY(dev_alloc((void**)&d_irrep, sizeof(int) * n));
+  GBX_TRY(dev_alloc((void**)&d_eps, sizeof(double) * n));
+  GBX_TRY(dev_alloc((void**)&d_mag, sizeof(double) * mag.size()));
+  GBX_CUDA(cudaMemcpy(d_irrep, irrep.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+  GBX_CUDA(cudaMemcpy(d_eps, eps.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+  GBX_CUDA(cudaMemcpy(d_mag, mag.data(), sizeof(double) * mag.size(), cudaMemcpyHostToDevice));
+  tab.irrep = d_irrep;
+  tab.eps = d_eps;
+  tab.mag = d_mag;
+  tab.norb = n;
+  tab.nocc = o;
+  GBX_TRY(dev_alloc((void**)&d_partial, sizeof(double) * npartial));
+  GBX_TRY(dev_alloc((void**)&d_hist, sizeof(double) * hist_cap));
+  GBX_TRY(dev_alloc((void**)&d_count, sizeof(int)));
+  GBX_CUDA(cudaMemsetAsync(d_count, 0, sizeof(int), st));
+  for (auto& kv : T) {
+    CCTensor* t = kv.second.get();
+    const size_t bytes = sizeof(double) * std::max<int64_t>(1, t->L.nelem);
+    GBX_TRY(dev_alloc((void**)&t->d, bytes));
+    GBX_CUDA(cudaMemsetAsync(t->d, 0, bytes, st));
+  }
+  // integrals on the device (their tile sets are dropped afterwards)
+  std::vector<std::unique_ptr<CCTileSet>> once;
+  for (auto& kv : T) {
+    if (!is_integral(kv.first.c_str())) continue;
+    CCTileSet* ts = tileset(kv.second.get());
+    if (!ts) return fail(GBX_ENOMEM, "tile set upload failed");
+    once.push_back(std::move(tilesets.back()));
+    tilesets.pop_back();
+    GBX_TRY(run_cc_tiles(*ts, CC_OP_INTEGRAL, tab, nullptr, kv.second->d, st));
+  }
+  den2 = tileset(get("t2"));
+  if (sd) den1 = tileset(get("t1"));
+  if (!den2 || (sd && !den1)) return fail(GBX_ENOMEM, "tile set upload failed");
+  // one arena for every plan's per-run buffers (the steps run in order on one
+  // stream); constant operands are packed into scratch, split, and the
+  // scratch is released
+  arena_bytes = 0;
+  size_t scratch_bytes = 0;
+  for (auto& p : cplans) {
+    size_t k = 0, w = 0, sc = 0;
+    GBX_TRY(p->sizes(&k, &w, &sc));
+    arena_bytes = std::max(arena_bytes, w);
+    scratch_bytes = std::max(scratch_bytes, sc);
+  }
+  if (arena_bytes) GBX_TRY(dev_alloc((void**)&d_arena, arena_bytes));
+  unsigned char* d_scratch = nullptr;
+  if (scratch_bytes) GBX_TRY(dev_alloc((void**)&d_scratch, scratch_bytes));
+  for (auto& p : splans) GBX_TRY(p->moves.upload());
+  for (size_t i = 0; i < cplans.size(); ++i) {
+    ContractionPlan* p = cplans[i].get();
+    int rc = p->build(d_arena, d_scratch);
+    if (rc == GBX_OK && (p->a_static || p->b_static))
+      rc = p->prepare_static(plan_operands[i].first->d, plan_operands[i].second->d, st);
+    if (rc != GBX_OK) {
+      cudaStreamSynchronize(st);
+      dev_free(d_scratch);
+      return rc;
+    }
+  }
+  // MP2 guess t2 = <ij||ab> / D, t1 = 0; tau / taut; energy
+  GBX_TRY(run_cc_tiles(*den2, CC_OP_DENOM, tab, get("OOVV")->d, get("t2")->d, st));
+  for (auto& f : init_steps) GBX_TRY(f(st));
+  GBX_TRY(gbx::run_energy(get("OOVV")->d, get(sd ? "tau" : "t2")->d, get("OOVV")->L.nelem, d_partial, npartial,
+                          d_hist, d_count, hist_cap, st));
+  GBX_CUDA(cudaStreamSynchronize(st));
+  dev_free(d_scratch);
+  once.clear();
+  for (auto& kv : T)
+    if (gbx_cc_job_static_only(*this, kv.first)) {
+      dev_free(kv.second->d);
+      kv.second->d = nullptr;
+    }
   return GBX_OK;
 }
 
@@ -484,15 +614,15 @@ void gbx_cc_default_config(gbx_cc_config* c) {
   c->v_decay = 8.0;
 }
 
-int gbx_cc_create(const gbx_cc_config* cfg, void* stream, gbx_cc_job** out) {
-  if (!cfg || !out) return fail(GBX_EINVAL, "null argument");
-  *out = nullptr;
+// Host part of a job: orbitals, blocking and every plan (no device work).
+static int cc_setup(const gbx_cc_config* cfg, std::unique_ptr<gbx_cc_job>& job) {
+  if (!cfg) return fail(GBX_EINVAL, "null argument");
   if (cfg->nocc < 1 || cfg->nvir < 1 || cfg->max_block < 1 ||
       !(cfg->nirrep == 1 || cfg->nirrep == 2 || cfg->nirrep == 4 || cfg->nirrep == 8) ||
       (cfg->method != GBX_CC_CCD && cfg->method != GBX_CC_CCSD) ||
       (cfg->engine != GBX_MODE_FP64 && cfg->engine != GBX_MODE_SPLIT) || cfg->v_decay <= 0)
     return fail(GBX_EINVAL, "bad CC configuration");
-  auto job = std::make_unique<gbx_cc_job>();
+  job = std::make_unique<gbx_cc_job>();
   job->cfg = *cfg;
   job->o = cfg->nocc;
   job->v = cfg->nvir;
@@ -510,55 +640,60 @@ int gbx_cc_create(const gbx_cc_config* cfg, void* stream, gbx_cc_job** out) {
   CCStream eo(cfg->seed, 3), ev(cfg->seed, 4), ei(cfg->seed, 5);
   for (int i = 0; i < job->o; ++i) job->eps.push_back(cfg->eps_occ_lo + (cfg->eps_occ_hi - cfg->eps_occ_lo) * eo.uniform());
   for (int a = 0; a < job->v; ++a) job->eps.push_back(cfg->eps_vir_lo + (cfg->eps_vir_hi - cfg->eps_vir_lo) * ev.uniform());
-  std::vector<double> mag(2 * job->n + 1);
-  for (size_t d = 0; d < mag.size(); ++d) mag[d] = cfg->v_scale * std::exp(-(double)d / cfg->v_decay);
-  GBX_TRY(dev_alloc((void**)&job->d_irrep, sizeof(int) * job->n));
-  GBX_TRY(dev_alloc((void**)&job->d_eps, sizeof(double) * job->n));
-  GBX_TRY(dev_alloc((void**)&job->d_mag, sizeof(double) * mag.size()));
-  GBX_CUDA(cudaMemcpy(job->d_irrep, job->irrep.data(), sizeof(int) * job->n, cudaMemcpyHostToDevice));
-  GBX_CUDA(cudaMemcpy(job->d_eps, job->eps.data(), sizeof(double) * job->n, cudaMemcpyHostToDevice));
-  GBX_CUDA(cudaMemcpy(job->d_mag, mag.data(), sizeof(double) * mag.size(), cudaMemcpyHostToDevice));
-  job->tab.irrep = job->d_irrep;
-  job->tab.eps = job->d_eps;
-  job->tab.mag = job->d_mag;
-  job->tab.norb = job->n;
-  job->tab.nocc = job->o;
   job->tab.seed_int = ei.next();
-  GBX_TRY(dev_alloc((void**)&job->d_partial, sizeof(double) * job->npartial));
-  GBX_TRY(dev_alloc((void**)&job->d_hist, sizeof(double) * job->hist_cap));
-  GBX_TRY(dev_alloc((void**)&job->d_count, sizeof(int)));
-  GBX_CUDA(cudaMemset(job->d_count, 0, sizeof(int)));
-  GBX_TRY(job->build());
-  GBX_CUDA(cudaDeviceSynchronize());
+  return job->plan_all();
+}
+
+int gbx_cc_footprint(const gbx_cc_config* cfg, double* resident_bytes, double* peak_bytes, double* flops_per_iter) {
+  std::unique_ptr<gbx_cc_job> job;
+  GBX_TRY(cc_setup(cfg, job));
+  if (flops_per_iter) *flops_per_iter = job->flops;
+  return job->footprint(resident_bytes, peak_bytes);
+}
+
+int gbx_cc_create(const gbx_cc_config* cfg, void* stream, gbx_cc_job** out) {
+  if (!out) return fail(GBX_EINVAL, "null argument");
+  *out = nullptr;
+  std::unique_ptr<gbx_cc_job> job;
+  GBX_TRY(cc_setup(cfg, job));
+  {
+    AllocAccount acct(&job->account);
+    GBX_TRY(job->materialize(0));
+  }
   job->nenergies = 1;
   (void)stream;
   *out = job.release();
   return GBX_OK;
 }
 
+int gbx_cc_capture(gbx_cc_job* job) {
+  if (!job) return fail(GBX_EINVAL, "null job");
+  if (!job->cfg.use_graph || job->exec) return GBX_OK;
+  cudaStream_t cap;
+  GBX_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+  GBX_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+  int rc = GBX_OK;
+  for (auto& s : job->steps) {
+    rc = s(cap);
+    if (rc != GBX_OK) break;
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(cap, &g);
+  cudaStreamDestroy(cap);
+  if (rc != GBX_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+  job->graph = g;
+  GBX_CUDA(cudaGraphInstantiate(&job->exec, g, 0));
+  return GBX_OK;
+}
+
 int gbx_cc_enqueue(gbx_cc_job* job, int niter, void* stream) {
   if (!job || niter < 0) return fail(GBX_EINVAL, "bad arguments");
   cudaStream_t st = (cudaStream_t)stream;
-  if (job->cfg.use_graph && !job->exec && niter > 0) {
-    cudaStream_t cap;
-    GBX_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
-    GBX_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-    int rc = GBX_OK;
-    for (auto& s : job->steps) {
-      rc = s(cap);
-      if (rc != GBX_OK) break;
-    }
-    cudaGraph_t g = nullptr;
-    cudaError_t e = cudaStreamEndCapture(cap, &g);
-    cudaStreamDestroy(cap);
-    if (rc != GBX_OK) {
-      if (g) cudaGraphDestroy(g);
-      return rc;
-    }
-    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture", __FILE__, __LINE__);
-    job->graph = g;
-    GBX_CUDA(cudaGraphInstantiate(&job->exec, g, 0));
-  }
+  if (niter > 0) GBX_TRY(gbx_cc_capture(job));
   for (int it = 0; it < niter; ++it) {
     if (job->exec) {
       GBX_CUDA(cudaGraphLaunch(job->exec, st));
@@ -570,13 +705,19 @@ int gbx_cc_enqueue(gbx_cc_job* job, int niter, void* stream) {
   return GBX_OK;
 }
 
-int gbx_cc_iterate(gbx_cc_job* job, int niter, double* energies, void* stream) {
-  GBX_TRY(gbx_cc_enqueue(job, niter, stream));
-  GBX_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+int gbx_cc_check(gbx_cc_job* job) {
+  if (!job) return fail(GBX_EINVAL, "null job");
   for (auto& p : job->cplans) {
     int err = split_plan_error(p->split);
     if (err != 0) return fail(GBX_ETIMEOUT, "split GEMM: a bounded device wait ran out (stage %d)", err);
   }
+  return GBX_OK;
+}
+
+int gbx_cc_iterate(gbx_cc_job* job, int niter, double* energies, void* stream) {
+  GBX_TRY(gbx_cc_enqueue(job, niter, stream));
+  GBX_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  GBX_TRY(gbx_cc_check(job));
   if (energies && niter > 0) {
     int first = job->nenergies - niter;
     if (first + niter > job->hist_cap) return fail(GBX_EUNSUPPORTED, "energy history full");
@@ -599,10 +740,7 @@ int gbx_cc_stats_get(const gbx_cc_job* job, gbx_cc_stats* s) {
   std::memset(s, 0, sizeof(*s));
   s->flops_per_iter = job->flops;
   s->gemm_flops_per_iter = job->gemm_flops;
-  double bytes = 0;
-  for (auto& kv : job->T) bytes += 8.0 * kv.second->L.nelem;
-  for (auto& p : job->cplans) bytes += 8.0 * (p->a_elems + p->b_elems + p->c_elems) + split_plan_bytes(p->split);
-  s->resident_bytes = bytes;
+  s->resident_bytes = (double)job->account.load();
   s->ncontractions = (int)job->cplans.size() - job->iter_plan_begin;
   s->nsums = (int)job->splans.size();
   s->nblocks_occ = (int)job->occ->ext.size();
@@ -751,7 +889,9 @@ int gbx_cc_time_gemm(gbx_cc_job* job, int contraction, int reps, float* ms, doub
   cudaEvent_t e0, e1;
   GBX_CUDA(cudaEventCreate(&e0));
   GBX_CUDA(cudaEventCreate(&e1));
-  // operands are already packed and split by the last iteration: time only the GEMM launches
+  // the arena is shared by every plan: pack and split this plan's operands
+  // again, then time only the GEMM launches
+  GBX_TRY(p->stage(job->plan_operands[contraction].first->d, job->plan_operands[contraction].second->d, st));
   GBX_CUDA(cudaEventRecord(e0, st));
   for (int r = 0; r < reps; ++r) {
     if (p->split) GBX_TRY(run_split_plan(p->split, false, false, st));

@@ -4,6 +4,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -138,6 +139,9 @@ struct F64Gemm {
   void release();
   ~F64Gemm() { release(); }
 };
+// Split-K partial-sum elements F64Gemm::build allocates for these problems
+// (model tile shapes).
+int64_t f64_partial_elems(const std::vector<GemmProblem>& probs);
 // Tile shapes shared by the host planner and the kernels.
 int f64_variant(int m, int n);
 int f64_variant(int m, int n, int k);
@@ -149,5 +153,22 @@ int f64_tiles(int m, int n);
 // through these so that OOM surfaces as GBX_ENOMEM).
 int dev_alloc(void** p, size_t bytes);
 void dev_free(void* p);
+// While alive, library allocations made on this thread are counted in *acc
+// (and subtracted again when freed, on any thread).
+struct AllocAccount {
+  explicit AllocAccount(std::atomic<int64_t>* acc);
+  ~AllocAccount();
+  std::atomic<int64_t>* prev;
+};
+// While alive, library allocations made on this thread come from the
+// stream-ordered allocator on `st` and are later freed on it (cudaFreeAsync),
+// so releasing them does not wait for the whole device as cudaFree does.  The
+// caller must ensure no work still uses memory it frees.
+struct StreamOrderedAlloc {
+  explicit StreamOrderedAlloc(cudaStream_t st);
+  ~StreamOrderedAlloc();
+  bool prev_on;
+  cudaStream_t prev;
+};
 
 }  // namespace gbx

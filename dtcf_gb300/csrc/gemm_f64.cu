@@ -297,7 +297,7 @@ __global__ void __launch_bounds__(kRedThreads) splitk_reduce_kernel(const GemmPr
 void F64Gemm::release() {
   auto fr = [&](void* q) {
     if (!q) return;
-    if (async_stream_set) cudaFreeAsync(q, async_stream); else cudaFree(q);
+    if (async_stream_set) cudaFreeAsync(q, async_stream); else dev_free(q);
   };
   for (auto& sb : subs) {
     fr(sb.d_probs);
@@ -315,6 +315,36 @@ void F64Gemm::release() {
   d_red_first = nullptr;
   nprob = nred = 0;
   red_chunks = 0;
+}
+
+namespace {
+// K split of a DMMA problem: only when the output tiles of the whole launch
+// leave the GPU idle; ranges are multiples of the K step.
+void f64_ksplit(int k, int64_t out_tiles, int* ks_out, int* chunk_out) {
+  int ks = 1;
+  if (out_tiles < kFillTiles && k > 2 * kMinChunk) {
+    int want = (int)((kFillTiles + out_tiles - 1) / out_tiles);
+    ks = std::max(1, std::min(want, (k + kMinChunk - 1) / kMinChunk));
+  }
+  int chunk = (k + ks - 1) / ks;
+  chunk = ((chunk + BK - 1) / BK) * BK;
+  ks = std::max(1, (k + chunk - 1) / chunk);
+  *ks_out = ks;
+  *chunk_out = chunk;
+}
+}  // namespace
+
+int64_t f64_partial_elems(const std::vector<GemmProblem>& probs) {
+  int64_t out_tiles = 0, part = 0;
+  for (auto& q : probs)
+    if (q.m > 0 && q.n > 0) out_tiles += f64_tiles(q.m, q.n);
+  for (auto& q : probs) {
+    if (q.m <= 0 || q.n <= 0 || f64_variant(q.m, q.n, q.k) >= 4) continue;
+    int ks = 1, chunk = 0;
+    f64_ksplit(q.k, out_tiles, &ks, &chunk);
+    if (ks > 1) part += (int64_t)ks * q.m * q.n;
+  }
+  return part;
 }
 
 int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t st, const std::vector<int>* variants) {
@@ -354,13 +384,8 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
       q.pad_ = thin;
       continue;
     }
-    if (out_tiles < kFillTiles && q.k > 2 * kMinChunk) {
-      int want = (int)((kFillTiles + out_tiles - 1) / out_tiles);
-      ks = std::max(1, std::min(want, (q.k + kMinChunk - 1) / kMinChunk));
-    }
-    int chunk = (q.k + ks - 1) / ks;
-    chunk = ((chunk + BK - 1) / BK) * BK;
-    ks = std::max(1, (q.k + chunk - 1) / chunk);
+    int chunk = 0;
+    f64_ksplit(q.k, out_tiles, &ks, &chunk);
     q.ksplit = ks;
     q.kchunk = std::max(chunk, BK);
     q.partial = nullptr;

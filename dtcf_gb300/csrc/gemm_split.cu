@@ -764,6 +764,11 @@ __global__ void __launch_bounds__(256) digits_kernel(const SplitRowSet* __restri
       }
       dst[k] = __int2bfloat16_rn((int)X);
     }
+    // the row's last chunk also clears its K padding (the slice buffers may be
+    // an arena shared with other plans, so nothing else keeps it zero)
+    if (k1 == rs.K)
+      for (int64_t k = rs.K + threadIdx.x; k < rs.Kp; k += 256)
+        for (int s = 0; s < S; ++s) dst[s * rs.slice_stride + k] = __int2bfloat16_rn(0);
   }
 }
 
@@ -806,6 +811,8 @@ __global__ void __launch_bounds__(256) split_short_rows_kernel(const SplitRowSet
       }
       dst[k] = __int2bfloat16_rn((int)X);
     }
+    for (int64_t k = rs.K + lane; k < rs.Kp; k += 32)
+      for (int s = 0; s < S; ++s) dst[s * rs.slice_stride + k] = __int2bfloat16_rn(0);
   }
 }
 
@@ -877,8 +884,8 @@ struct SplitPlan {
   std::vector<SplitProblem> host;
   std::vector<int> width;  // per problem
   std::vector<bool> thin;  // per problem: thin-K kernel
-  __nv_bfloat16* d_slices = nullptr;  // all A and B slices
-  int* d_exps = nullptr;
+  unsigned char* d_persist = nullptr;    // slices and exponents of constant plan operands
+  unsigned char* d_own_arena = nullptr;  // the per-run region when no arena was given
   SplitRowSet* d_sets_a = nullptr;  // long rows from the plan's packed A
   SplitRowSet* d_sets_b = nullptr;  // long rows from the plan's packed B
   SplitRowSet* d_short_a = nullptr;  // short rows (first_row counts rows)
@@ -891,18 +898,16 @@ struct SplitPlan {
   std::vector<SplitLaunch> launches;
   DevProblem* d_all = nullptr;  // every problem, for the split-K reduction
   int* d_err = nullptr;
-  double* d_partial = nullptr;
   int* d_red_prob = nullptr;
   int64_t* d_red_first = nullptr;
   int nred = 0;
   int64_t red_total = 0;
   double bytes = 0.0;
   ~SplitPlan() {
-    dev_free(d_partial);
     dev_free(d_red_prob);
     dev_free(d_red_first);
-    dev_free(d_slices);
-    dev_free(d_exps);
+    dev_free(d_persist);
+    dev_free(d_own_arena);
     dev_free(d_sets_a);
     dev_free(d_sets_b);
     dev_free(d_short_a);
@@ -924,7 +929,105 @@ int set_smem_attr() {
   return GBX_OK;
 }
 
-int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitPlan** out) {
+namespace {
+
+size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+// Where every buffer of a split plan lives.  Region 0 persists with the plan
+// (slices and exponents of constant plan operands, split once); region 1 is
+// rewritten by every run (the other operands' slices and exponents, split-K
+// partial sums) and may be an arena shared with other plans.  Offsets are in
+// elements of each region's slice, exponent and partial-sum sub-buffers.
+struct SplitLayout {
+  struct Prob {
+    int bn = 0;
+    bool thin = false;
+    int64_t Mp = 0, Np = 0, Kp = 0;
+    int ra = 0, rb = 0;      // region of the GEMM's A and B slices
+    int64_t sa = 0, sb = 0;  // slice offsets
+    int64_t ea = 0, eb = 0;  // exponent offsets
+    int ks = 1, per = 0;     // K split and k-blocks per range
+    int64_t part = -1;       // partial-sum offset (region 1), -1 = none
+  };
+  std::vector<Prob> p;
+  int64_t slices[2] = {0, 0}, exps[2] = {0, 0}, part = 0;
+  size_t exps_at(int r) const { return align256(2 * (size_t)slices[r]); }
+  size_t part_at() const { return exps_at(1) + align256(4 * (size_t)exps[1]); }
+  size_t bytes(int r) const {
+    size_t b = exps_at(r) + align256(4 * (size_t)exps[r]);
+    if (r == 1) b += align256(8 * (size_t)part);
+    return (r == 0 && slices[0] == 0 && exps[0] == 0) || (r == 1 && slices[1] == 0 && exps[1] == 0 && part == 0)
+               ? 0
+               : b;
+  }
+};
+
+int split_layout(const std::vector<SplitProblem>& probs, int S, bool static_a, bool static_b, SplitLayout& L) {
+  L = SplitLayout();
+  int64_t out_tiles = 0;
+  for (auto& q : probs) {
+    if (q.M <= 0 || q.N <= 0 || q.K <= 0) return fail(GBX_EINVAL, "empty split problem");
+    if (q.M >= (1ll << 30) || q.N >= (1ll << 30) || q.K >= (1ll << 30)) return fail(GBX_EUNSUPPORTED, "split problem too large");
+    SplitLayout::Prob o;
+    // thin-K problems (one k-block, at most 32 columns) take the thin kernel
+    o.thin = q.K <= BK && q.N <= kThinBN && S <= 7;
+    o.bn = o.thin ? kThinBN : (q.width ? q.width : choose_width(q.N));
+    if (!o.thin && o.bn != 32 && o.bn != 64 && o.bn != 128 && o.bn != 256)
+      return fail(GBX_EINVAL, "split tile width %d", o.bn);
+    o.Mp = (q.M + BM - 1) / BM * BM;
+    o.Np = (q.N + o.bn - 1) / o.bn * o.bn;
+    o.Kp = (q.K + BK - 1) / BK * BK;
+    // the GEMM's A rows come from plan operand B when swapped
+    const bool a_const = q.a_is_plan_b ? static_b : static_a;
+    const bool b_const = q.a_is_plan_b ? static_a : static_b;
+    o.ra = a_const ? 0 : 1;
+    o.rb = b_const ? 0 : 1;
+    o.sa = L.slices[o.ra];
+    L.slices[o.ra] += S * o.Mp * o.Kp;
+    o.sb = L.slices[o.rb];
+    L.slices[o.rb] += S * o.Np * o.Kp;
+    o.ea = L.exps[o.ra];
+    L.exps[o.ra] += o.Mp;
+    o.eb = L.exps[o.rb];
+    L.exps[o.rb] += o.Np;
+    out_tiles += (o.Mp / BM) * (o.Np / o.bn);
+    L.p.push_back(o);
+  }
+  for (size_t i = 0; i < probs.size(); ++i) {
+    SplitLayout::Prob& o = L.p[i];
+    const int nkb = (int)(o.Kp / BK);
+    // split K when the output tiles of all problems leave SMs idle; ranges are
+    // whole exact-accumulation chunks
+    int ks = 1;
+    if (!o.thin && out_tiles < kSplitFill && nkb > 2 * kChunkKb) {
+      int want = (int)((kSplitFill + out_tiles - 1) / out_tiles);
+      ks = std::max(1, std::min(want, nkb / kChunkKb));
+    }
+    int per = (nkb + ks - 1) / ks;
+    per = (per + kChunkKb - 1) / kChunkKb * kChunkKb;
+    ks = (nkb + per - 1) / per;
+    o.ks = ks;
+    o.per = per;
+    if (ks > 1) {
+      o.part = L.part;
+      L.part += (int64_t)ks * probs[i].M * probs[i].N;
+    }
+  }
+  return GBX_OK;
+}
+
+}  // namespace
+
+int split_plan_sizes(const std::vector<SplitProblem>& probs, int slices, bool static_a, bool static_b,
+                     size_t* persist_bytes, size_t* arena_bytes) {
+  SplitLayout L;
+  GBX_TRY(split_layout(probs, slices > 0 ? slices : 6, static_a, static_b, L));
+  if (persist_bytes) *persist_bytes = L.bytes(0);
+  if (arena_bytes) *arena_bytes = L.bytes(1);
+  return GBX_OK;
+}
+
+int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitPlan** out, const SplitMem* mem) {
   *out = nullptr;
   auto sp = std::make_unique<SplitPlan>();
   sp->S = slices > 0 ? slices : 6;
@@ -932,58 +1035,52 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
   sp->L = sp->S - 1;
   sp->host = probs;
   const int S = sp->S;
-  int64_t slice_elems = 0, exp_elems = 0;
-  struct Off {
-    int64_t a, b, ea, eb, Mp, Np, Kp;
-  };
-  std::vector<Off> offs;
-  for (auto& p : probs) {
-    if (p.M <= 0 || p.N <= 0 || p.K <= 0) return fail(GBX_EINVAL, "empty split problem");
-    if (p.M >= (1ll << 30) || p.N >= (1ll << 30) || p.K >= (1ll << 30)) return fail(GBX_EUNSUPPORTED, "split problem too large");
-    // thin-K problems (one k-block, at most 32 columns) take the thin kernel
-    const bool thin = p.K <= BK && p.N <= kThinBN && S <= 7;
-    const int bn = thin ? kThinBN : (p.width ? p.width : choose_width(p.N));
-    if (!thin && bn != 32 && bn != 64 && bn != 128 && bn != 256) return fail(GBX_EINVAL, "split tile width %d", bn);
-    sp->width.push_back(bn);
-    sp->thin.push_back(thin);
-    Off o;
-    o.Mp = (p.M + BM - 1) / BM * BM;
-    o.Np = (p.N + bn - 1) / bn * bn;
-    o.Kp = (p.K + BK - 1) / BK * BK;
-    o.a = slice_elems;
-    slice_elems += S * o.Mp * o.Kp;
-    o.b = slice_elems;
-    slice_elems += S * o.Np * o.Kp;
-    o.ea = exp_elems;
-    exp_elems += o.Mp;
-    o.eb = exp_elems;
-    exp_elems += o.Np;
-    offs.push_back(o);
+  const bool static_a = mem && mem->static_a, static_b = mem && mem->static_b;
+  SplitLayout lay;
+  GBX_TRY(split_layout(probs, S, static_a, static_b, lay));
+  for (auto& o : lay.p) {
+    sp->width.push_back(o.bn);
+    sp->thin.push_back(o.thin);
   }
-  GBX_TRY(dev_alloc((void**)&sp->d_slices, sizeof(__nv_bfloat16) * std::max<int64_t>(slice_elems, 1)));
-  GBX_TRY(dev_alloc((void**)&sp->d_exps, sizeof(int) * std::max<int64_t>(exp_elems, 1)));
-  GBX_CUDA(cudaMemset(sp->d_slices, 0, sizeof(__nv_bfloat16) * std::max<int64_t>(slice_elems, 1)));
-  GBX_CUDA(cudaMemset(sp->d_exps, 0, sizeof(int) * std::max<int64_t>(exp_elems, 1)));
-  sp->bytes = 2.0 * slice_elems + 4.0 * exp_elems;
+  unsigned char* base[2] = {nullptr, nullptr};
+  const size_t b0 = lay.bytes(0), b1 = lay.bytes(1);
+  if (b0) {
+    // constant operands are split once: their padding must read as zero
+    GBX_TRY(dev_alloc((void**)&sp->d_persist, b0));
+    GBX_CUDA(cudaMemset(sp->d_persist, 0, b0));
+    base[0] = sp->d_persist;
+  }
+  if (b1) {
+    if (mem && mem->arena) {
+      base[1] = mem->arena;
+    } else {
+      GBX_TRY(dev_alloc((void**)&sp->d_own_arena, b1));
+      GBX_CUDA(cudaMemset(sp->d_own_arena, 0, b1));
+      base[1] = sp->d_own_arena;
+    }
+  }
+  auto slice_ptr = [&](int r, int64_t off) { return (__nv_bfloat16*)base[r] + off; };
+  auto exp_ptr = [&](int r, int64_t off) { return (int*)(base[r] + lay.exps_at(r)) + off; };
+  double* part_base = b1 ? (double*)(base[1] + lay.part_at()) : nullptr;
+  sp->bytes = (double)b0 + (double)b1;
   std::vector<SplitRowSet> sa, sb, ssa, ssb;
   int64_t sra = 0, srb = 0;
   std::vector<DevProblem> dp;
   std::vector<CUtensorMap> maps;
   int64_t ra = 0, rb = 0;
-  int64_t out_tiles = 0;
-  for (size_t i = 0; i < probs.size(); ++i) out_tiles += (offs[i].Mp / BM) * (offs[i].Np / sp->width[i]);
-  int64_t part_elems = 0;
   std::vector<int> red;
   std::vector<int64_t> red_first;
   int64_t red_total = 0;
   for (size_t i = 0; i < probs.size(); ++i) {
     const SplitProblem& p = probs[i];
-    const Off& o = offs[i];
-    const int bn = sp->width[i];
+    const SplitLayout::Prob& o = lay.p[i];
+    const int bn = o.bn;
     // row sets are grouped by the plan operand they come from, so constant
     // plan operands can be split once
-    SplitRowSet a{p.A, p.M, p.K, sp->d_slices + o.a, o.Mp * o.Kp, o.Kp, sp->d_exps + o.ea, 0, p.lda ? p.lda : p.K};
-    SplitRowSet b{p.B, p.N, p.K, sp->d_slices + o.b, o.Np * o.Kp, o.Kp, sp->d_exps + o.eb, 0, p.ldb ? p.ldb : p.K};
+    SplitRowSet a{p.A, p.M, p.K, slice_ptr(o.ra, o.sa), o.Mp * o.Kp, o.Kp, exp_ptr(o.ra, o.ea), 0,
+                  p.lda ? p.lda : p.K};
+    SplitRowSet b{p.B, p.N, p.K, slice_ptr(o.rb, o.sb), o.Np * o.Kp, o.Kp, exp_ptr(o.rb, o.eb), 0,
+                  p.ldb ? p.ldb : p.K};
     SplitRowSet& to_a = p.a_is_plan_b ? b : a;  // rows that come from plan A
     SplitRowSet& to_b = p.a_is_plan_b ? a : b;
     if (to_a.K <= kShortRow) {
@@ -1013,25 +1110,14 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
     d.nkb = (int)(o.Kp / BK);
     d.tiles_m = (int)(o.Mp / BM);
     d.tiles_n = (int)(o.Np / bn);
-    // split K when the output tiles of all problems leave SMs idle; ranges are
-    // whole exact-accumulation chunks
-    int ks = 1;
-    if (!sp->thin[i] && out_tiles < kSplitFill && d.nkb > 2 * kChunkKb) {
-      int want = (int)((kSplitFill + out_tiles - 1) / out_tiles);
-      ks = std::max(1, std::min(want, d.nkb / kChunkKb));
-    }
-    int per = (d.nkb + ks - 1) / ks;
-    per = (per + kChunkKb - 1) / kChunkKb * kChunkKb;
-    ks = (d.nkb + per - 1) / per;
-    d.ksplit = ks;
-    d.kb_per_split = per;
-    d.eA = sp->d_exps + o.ea;
-    d.eB = sp->d_exps + o.eb;
+    d.ksplit = o.ks;
+    d.kb_per_split = o.per;
+    d.eA = exp_ptr(o.ra, o.ea);
+    d.eB = exp_ptr(o.rb, o.eb);
     d.C = p.C;
     d.partial = nullptr;
-    if (ks > 1) {
-      d.partial = (double*)(intptr_t)(part_elems + 1);
-      part_elems += (int64_t)ks * p.M * p.N;
+    if (o.ks > 1) {
+      d.partial = part_base + o.part;
       red.push_back((int)i);
       red_first.push_back(red_total);
       red_total += p.M * p.N;
@@ -1039,22 +1125,18 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
     d.ldc = p.ldc ? p.ldc : p.N;
     dp.push_back(d);
     CUtensorMap ma, mb;
-    GBX_TRY(encode_slices(&ma, sp->d_slices + o.a, S, o.Mp, o.Kp, BM));
-    GBX_TRY(encode_slices(&mb, sp->d_slices + o.b, S, o.Np, o.Kp, bn));
+    GBX_TRY(encode_slices(&ma, slice_ptr(o.ra, o.sa), S, o.Mp, o.Kp, BM));
+    GBX_TRY(encode_slices(&mb, slice_ptr(o.rb, o.sb), S, o.Np, o.Kp, bn));
     maps.push_back(ma);
     maps.push_back(mb);
   }
-  if (part_elems > 0) {
-    GBX_TRY(dev_alloc((void**)&sp->d_partial, sizeof(double) * part_elems));
-    for (auto& d : dp)
-      if (d.partial) d.partial = sp->d_partial + ((intptr_t)d.partial - 1);
+  if (!red.empty()) {
     GBX_TRY(dev_alloc((void**)&sp->d_red_prob, sizeof(int) * red.size()));
     GBX_TRY(dev_alloc((void**)&sp->d_red_first, sizeof(int64_t) * red.size()));
     GBX_CUDA(cudaMemcpy(sp->d_red_prob, red.data(), sizeof(int) * red.size(), cudaMemcpyHostToDevice));
     GBX_CUDA(cudaMemcpy(sp->d_red_first, red_first.data(), sizeof(int64_t) * red.size(), cudaMemcpyHostToDevice));
     sp->nred = (int)red.size();
     sp->red_total = red_total;
-    sp->bytes += 8.0 * part_elems;
   }
   sp->nsets = (int)probs.size();
   sp->rows_a = ra;

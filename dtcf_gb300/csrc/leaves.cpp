@@ -4,6 +4,9 @@
 // host and runs them with stream-ordered temporaries, so a call never
 // synchronises the host with the device.
 #include <algorithm>
+#include <atomic>
+#include <mutex>
+#include <unordered_map>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -46,21 +49,75 @@ int cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
   return GBX_ECUDA;
 }
 
+// Every library allocation is recorded with its size and the account that
+// was current on the allocating thread, so a job can report the device bytes
+// it holds.
+namespace {
+struct AllocRec {
+  size_t bytes;
+  std::atomic<int64_t>* account;
+  cudaStream_t stream;  // stream-ordered allocation: freed on this stream
+  bool ordered;
+};
+std::mutex g_alloc_mu;
+std::unordered_map<void*, AllocRec> g_allocs;
+thread_local std::atomic<int64_t>* g_account = nullptr;
+thread_local bool g_ordered = false;
+thread_local cudaStream_t g_order_stream = nullptr;
+}  // namespace
+
+AllocAccount::AllocAccount(std::atomic<int64_t>* acc) : prev(g_account) { g_account = acc; }
+AllocAccount::~AllocAccount() { g_account = prev; }
+
+StreamOrderedAlloc::StreamOrderedAlloc(cudaStream_t st) : prev_on(g_ordered), prev(g_order_stream) {
+  g_ordered = true;
+  g_order_stream = st;
+}
+StreamOrderedAlloc::~StreamOrderedAlloc() {
+  g_ordered = prev_on;
+  g_order_stream = prev;
+}
+
 int dev_alloc(void** p, size_t bytes) {
   *p = nullptr;
   if (bytes == 0) return GBX_OK;
-  cudaError_t e = cudaMalloc(p, bytes);
+  cudaError_t e;
+  if (g_ordered) {
+    // the allocation completes before the memory is handed out, so any
+    // stream (and host-synchronous copies) may use it at once
+    e = cudaMallocAsync(p, bytes, g_order_stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g_order_stream);
+  } else {
+    e = cudaMalloc(p, bytes);
+  }
   if (e != cudaSuccess) {
     cudaGetLastError();
     *p = nullptr;
-    return fail(e == cudaErrorMemoryAllocation ? GBX_ENOMEM : GBX_ECUDA, "cudaMalloc(%zu) failed: %s", bytes,
-                cudaGetErrorString(e));
+    return fail(e == cudaErrorMemoryAllocation ? GBX_ENOMEM : GBX_ECUDA, "device allocation of %zu bytes failed: %s",
+                bytes, cudaGetErrorString(e));
   }
+  std::lock_guard<std::mutex> lk(g_alloc_mu);
+  g_allocs[*p] = AllocRec{bytes, g_account, g_order_stream, g_ordered};
+  if (g_account) g_account->fetch_add((int64_t)bytes);
   return GBX_OK;
 }
 
 void dev_free(void* p) {
-  if (p) cudaFree(p);
+  if (!p) return;
+  bool ordered = false;
+  cudaStream_t st = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_alloc_mu);
+    auto it = g_allocs.find(p);
+    if (it != g_allocs.end()) {
+      if (it->second.account) it->second.account->fetch_sub((int64_t)it->second.bytes);
+      ordered = it->second.ordered;
+      st = it->second.stream;
+      g_allocs.erase(it);
+    }
+  }
+  if (ordered) cudaFreeAsync(p, st);
+  else cudaFree(p);
 }
 
 // Stream-ordered temporary upload of host data (freed on the same stream).

@@ -275,18 +275,16 @@ void choose_engine(GroupBlock& g, bool split_engine, bool split_all, int slices)
 }
 
 ContractionPlan::~ContractionPlan() {
-  if (own_workspace) {
-    dev_free(d_Abig);
-    dev_free(d_Bbig);
-    dev_free(d_Cbig);
-  }
   destroy_split_plan(split);
+  dev_free(d_keepA);
+  dev_free(d_keepB);
+  dev_free(d_own_arena);
 }
 
 int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorLayout& C,
                      const std::vector<std::string>& la, const std::vector<std::string>& lb,
                      const std::vector<std::string>& lc, Engine e, int nslices,
-                     std::unique_ptr<ContractionPlan>& out, bool split_all) {
+                     std::unique_ptr<ContractionPlan>& out, bool split_all, bool defer) {
   if ((int)la.size() != A.rank || (int)lb.size() != B.rank || (int)lc.size() != C.rank)
     return fail(GBX_EINVAL, "index strings do not match tensor ranks (%d/%d, %d/%d, %d/%d)", (int)la.size(), A.rank,
                 (int)lb.size(), B.rank, (int)lc.size(), C.rank);
@@ -465,46 +463,125 @@ int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorL
   GBX_TRY(check_moves(p->packB, B.nelem, p->b_elems, "pack B"));
   GBX_TRY(check_moves(p->unpackC, p->c_elems, C.nelem, "unpack C"));
   p->split_all = split_all;
-  GBX_TRY(p->build(e, nslices));
+  p->engine = e;
+  p->slices = nslices;
+  for (auto& g : p->groups) {
+    if (g.M == 0 || g.N == 0 || g.K == 0) continue;
+    if (g.M >= (1ll << 31) || g.N >= (1ll << 31) || g.K >= (1ll << 31))
+      return fail(GBX_EUNSUPPORTED, "packed block too large");
+    if (g.engine == 1) ++p->n_split_groups; else ++p->n_f64_groups;
+  }
+  if (!defer) GBX_TRY(p->build());
   out = std::move(p);
   return GBX_OK;
 }
 
-int ContractionPlan::build(Engine e, int nslices) {
-  engine = e;
-  slices = nslices;
+namespace {
+size_t up256(size_t x) { return (x + 255) / 256 * 256; }
+size_t move_bytes(const MoveSet& m) {
+  return m.host.empty() ? 0 : m.host.size() * sizeof(MoveDesc) + (m.host.size() + 1) * sizeof(uint32_t);
+}
+}  // namespace
+
+// The split engine's problems over the packed buffers (sizes() only needs
+// their shapes).
+void ContractionPlan::split_problems(std::vector<SplitProblem>& sp) const {
+  sp.clear();
+  for (auto& g : groups) {
+    if (g.M == 0 || g.N == 0 || g.K == 0 || g.engine != 1) continue;
+    SplitProblem q;
+    if (g.swap) {  // C^T = B A^T: rows from B, C block stored N x M
+      q.A = d_Bbig + g.b_off;
+      q.B = d_Abig + g.a_off;
+      q.M = g.N;
+      q.N = g.M;
+      q.a_is_plan_b = true;
+    } else {
+      q.A = d_Abig + g.a_off;
+      q.B = d_Bbig + g.b_off;
+      q.M = g.M;
+      q.N = g.N;
+      q.a_is_plan_b = false;
+    }
+    q.C = d_Cbig + g.c_off;
+    q.K = g.K;
+    sp.push_back(q);
+  }
+}
+
+int ContractionPlan::sizes(size_t* persist, size_t* arena, size_t* static_scratch) const {
+  size_t keep = 0, ws = 0, scratch = 0;
+  const size_t ab = up256(sizeof(double) * a_elems), bb = up256(sizeof(double) * b_elems);
+  if (keeps_a()) keep += ab; else if (a_static) scratch += ab; else ws += ab;
+  if (keeps_b()) keep += bb; else if (b_static) scratch += bb; else ws += bb;
+  ws += up256(sizeof(double) * c_elems);
+  keep += move_bytes(packA) + move_bytes(packB) + move_bytes(unpackC);
+  if (n_split_groups) {
+    std::vector<SplitProblem> sp;
+    split_problems(sp);
+    size_t sp_keep = 0, sp_ws = 0;
+    GBX_TRY(split_plan_sizes(sp, slices, a_static, b_static, &sp_keep, &sp_ws));
+    keep += sp_keep;
+    ws += sp_ws;
+  }
+  if (persist) *persist = keep;
+  if (arena) *arena = ws;
+  if (static_scratch) *static_scratch = scratch;
+  return GBX_OK;
+}
+
+double ContractionPlan::f64_workspace_estimate() const {
+  std::vector<GemmProblem> fp;
+  for (auto& g : groups) {
+    if (g.M == 0 || g.N == 0 || g.K == 0 || g.engine == 1) continue;
+    GemmProblem q;
+    std::memset(&q, 0, sizeof(q));
+    q.m = (int)g.M;
+    q.n = (int)g.N;
+    q.k = (int)g.K;
+    fp.push_back(q);
+  }
+  return 8.0 * (double)f64_partial_elems(fp);
+}
+
+int ContractionPlan::build(unsigned char* arena, unsigned char* static_scratch) {
+  size_t keep = 0, ws = 0, scratch = 0;
+  GBX_TRY(sizes(&keep, &ws, &scratch));
+  if (!arena && (ws || (scratch && !static_scratch))) {
+    GBX_TRY(dev_alloc((void**)&d_own_arena, ws + scratch));
+    arena = d_own_arena;
+  }
   GBX_TRY(packA.upload());
   GBX_TRY(packB.upload());
   GBX_TRY(unpackC.upload());
-  GBX_TRY(dev_alloc((void**)&d_Abig, sizeof(double) * a_elems));
-  GBX_TRY(dev_alloc((void**)&d_Bbig, sizeof(double) * b_elems));
-  GBX_TRY(dev_alloc((void**)&d_Cbig, sizeof(double) * c_elems));
+  size_t off = 0, soff = 0;
+  auto carve = [&](size_t bytes) {
+    unsigned char* q = arena + off;
+    off += up256(bytes);
+    return q;
+  };
+  unsigned char* sbase = static_scratch ? static_scratch : (arena ? arena + ws : nullptr);
+  auto carve_static = [&](size_t bytes) {
+    unsigned char* q = sbase + soff;
+    soff += up256(bytes);
+    return q;
+  };
+  if (keeps_a()) {
+    GBX_TRY(dev_alloc((void**)&d_keepA, std::max<size_t>(8, sizeof(double) * a_elems)));
+    d_Abig = d_keepA;
+  } else {
+    d_Abig = (double*)(a_static ? carve_static(sizeof(double) * a_elems) : carve(sizeof(double) * a_elems));
+  }
+  if (keeps_b()) {
+    GBX_TRY(dev_alloc((void**)&d_keepB, std::max<size_t>(8, sizeof(double) * b_elems)));
+    d_Bbig = d_keepB;
+  } else {
+    d_Bbig = (double*)(b_static ? carve_static(sizeof(double) * b_elems) : carve(sizeof(double) * b_elems));
+  }
+  d_Cbig = (double*)carve(sizeof(double) * c_elems);
   std::vector<GemmProblem> probs;
-  std::vector<SplitProblem> sp;
   for (auto& g : groups) {
-    if (g.M == 0 || g.N == 0 || g.K == 0) continue;
-    if (g.M >= (1ll << 31) || g.N >= (1ll << 31) || g.K >= (1ll << 31))
-      return fail(GBX_EUNSUPPORTED, "packed block too large");
-    if (g.engine == 1) {
-      SplitProblem q;
-      if (g.swap) {  // C^T = B A^T: rows from B, C block stored N x M
-        q.A = d_Bbig + g.b_off;
-        q.B = d_Abig + g.a_off;
-        q.M = g.N;
-        q.N = g.M;
-        q.a_is_plan_b = true;
-      } else {
-        q.A = d_Abig + g.a_off;
-        q.B = d_Bbig + g.b_off;
-        q.M = g.M;
-        q.N = g.N;
-        q.a_is_plan_b = false;
-      }
-      q.C = d_Cbig + g.c_off;
-      q.K = g.K;
-      sp.push_back(q);
-      continue;
-    }
+    if (g.M == 0 || g.N == 0 || g.K == 0 || g.engine == 1) continue;
     GemmProblem q;
     std::memset(&q, 0, sizeof(q));
     q.A = d_Abig + g.a_off;
@@ -522,10 +599,19 @@ int ContractionPlan::build(Engine e, int nslices) {
     q.accumulate = 0;
     probs.push_back(q);
   }
-  n_f64_groups = (int)probs.size();
-  n_split_groups = (int)sp.size();
   GBX_TRY(f64.build(probs));
-  if (!sp.empty()) GBX_TRY(create_split_plan(sp, nslices, &split));
+  if (n_split_groups) {
+    std::vector<SplitProblem> sp;
+    split_problems(sp);
+    SplitMem mem;
+    mem.static_a = a_static;
+    mem.static_b = b_static;
+    mem.arena = ws > off ? arena + off : nullptr;
+    GBX_TRY(create_split_plan(sp, slices, &split, &mem));
+  }
+  // uploads and zero fills above ran on the legacy default stream: finish
+  // them before any other stream touches the plan's buffers
+  GBX_CUDA(cudaStreamSynchronize(cudaStreamLegacy));
   return GBX_OK;
 }
 
@@ -540,6 +626,20 @@ int ContractionPlan::prepare_static(const double* dA, const double* dB, cudaStre
   }
   if (split) GBX_TRY(split_operands(split, a_static, b_static, st));
   static_ready = a_static || b_static;
+  return GBX_OK;
+}
+
+int ContractionPlan::stage(const double* dA, const double* dB, cudaStream_t st) {
+  const bool skipA = a_static && static_ready, skipB = b_static && static_ready;
+  if (!skipA) {
+    if (a_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Abig, 0, sizeof(double) * a_elems, st));
+    GBX_TRY(run_moves(packA, dA, d_Abig, st));
+  }
+  if (!skipB) {
+    if (b_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Bbig, 0, sizeof(double) * b_elems, st));
+    GBX_TRY(run_moves(packB, dB, d_Bbig, st));
+  }
+  if (split) GBX_TRY(split_operands(split, !skipA, !skipB, st));
   return GBX_OK;
 }
 
@@ -564,7 +664,7 @@ int SumPlan::execute(const double* dA, double* dC, double alpha, cudaStream_t st
 }
 
 int plan_sum(const TensorLayout& A, const TensorLayout& C, const std::vector<std::string>& la,
-             const std::vector<std::string>& lc, double coef, std::unique_ptr<SumPlan>& out) {
+             const std::vector<std::string>& lc, double coef, std::unique_ptr<SumPlan>& out, bool defer) {
   if ((int)la.size() != A.rank || (int)lc.size() != C.rank || A.rank != C.rank)
     return fail(GBX_EINVAL, "sum: index strings do not match ranks");
   std::vector<int> a_of_c(C.rank);
@@ -600,7 +700,7 @@ int plan_sum(const TensorLayout& A, const TensorLayout& C, const std::vector<std
     p->moves.host.push_back(make_move(C.rank, ext, sstr, dstr, A.off[id], C.off[t], 1, coef * f));
   }
   GBX_TRY(check_moves(p->moves, A.nelem, C.nelem, "sum"));
-  GBX_TRY(p->moves.upload());
+  if (!defer) GBX_TRY(p->moves.upload());
   out = std::move(p);
   return GBX_OK;
 }

@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "common.h"
+#include "split.h"
 
 namespace gbx {
 
@@ -110,7 +111,6 @@ void choose_engine(GroupBlock& g, bool split_engine, bool split_all, int slices)
 enum class Engine { F64 = 0, Split = 1 };
 
 
-struct SplitPlan;  // the split-precision GEMM state (gemm_split.cu)
 
 struct ContractionPlan {
   TensorLayout A, B, C;
@@ -121,33 +121,57 @@ struct ContractionPlan {
   MoveSet packA, packB, unpackC;
   // F64 engine
   F64Gemm f64;
-  // workspace
+  // Packed operands.  A constant operand read by FP64 groups keeps its own
+  // buffer; every other packed buffer, the split engine's per-run slices and
+  // partial sums live in the workspace arena (the plan's own, or one shared
+  // by plans that never run at the same time).  A constant operand that is
+  // kept only as split slices is packed into scratch that prepare_static
+  // alone reads.
   double *d_Abig = nullptr, *d_Bbig = nullptr, *d_Cbig = nullptr;
-  bool own_workspace = true;
+  double *d_keepA = nullptr, *d_keepB = nullptr;
+  unsigned char* d_own_arena = nullptr;
   Engine engine = Engine::F64;
   int slices = 0;
   SplitPlan* split = nullptr;
   double flops = 0.0;        // algorithmic: 2 * sum over nonzero triples m*n*k
   double gemm_flops = 0.0;   // what the packed GEMMs execute
   // Operands whose values never change (integrals) are packed and split once
-  // by prepare_static and skipped by execute.
+  // by prepare_static and skipped by execute.  Set before build().
   bool a_static = false, b_static = false;
   bool static_ready = false;
   int n_split_groups = 0, n_f64_groups = 0;
   bool split_all = false;
 
   ~ContractionPlan();
-  int build(Engine e, int nslices);
+  // Device bytes the plan keeps for itself, the arena bytes one execute
+  // needs and the scratch bytes prepare_static needs (host arithmetic only;
+  // valid once planned, before build).
+  int sizes(size_t* persist, size_t* arena, size_t* static_scratch = nullptr) const;
+  // FP64 split-K workspace the FP64 groups will allocate (bytes).
+  double f64_workspace_estimate() const;
+  // Allocates the persistent buffers, binds the arena (nullptr: the plan's
+  // own) and the static scratch (nullptr: after the arena), uploads the
+  // launch descriptors.
+  int build(unsigned char* arena = nullptr, unsigned char* static_scratch = nullptr);
   int prepare_static(const double* dA, const double* dB, cudaStream_t st);
+  // Packs and splits the changing operands without running the GEMM (so a
+  // GEMM can be timed alone on current data).
+  int stage(const double* dA, const double* dB, cudaStream_t st);
   // C += alpha * A * B.
   int execute(const double* dA, const double* dB, double* dC, double alpha, cudaStream_t st);
+
+ private:
+  void split_problems(std::vector<SplitProblem>& sp) const;
+  bool keeps_a() const { return a_static && n_f64_groups > 0; }
+  bool keeps_b() const { return b_static && n_f64_groups > 0; }
 };
 
 // split_all: every packed GEMM of a split plan uses the split engine (tests).
+// defer: plan only (host); the caller sets the static flags and calls build().
 int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorLayout& C,
                      const std::vector<std::string>& la, const std::vector<std::string>& lb,
                      const std::vector<std::string>& lc, Engine e, int nslices,
-                     std::unique_ptr<ContractionPlan>& out, bool split_all = false);
+                     std::unique_ptr<ContractionPlan>& out, bool split_all = false, bool defer = false);
 
 // Tile moves accumulating alpha * permuted A into C: C[c] += alpha * A[a],
 // the DLTC Summation (DLTC/task.cc:51-81) over block-sparse layouts.
@@ -158,6 +182,6 @@ struct SumPlan {
 };
 int check_moves(const MoveSet& ms, int64_t src_elems, int64_t dst_elems, const char* what);
 int plan_sum(const TensorLayout& A, const TensorLayout& C, const std::vector<std::string>& la,
-             const std::vector<std::string>& lc, double coef, std::unique_ptr<SumPlan>& out);
+             const std::vector<std::string>& lc, double coef, std::unique_ptr<SumPlan>& out, bool defer = false);
 
 }  // namespace gbx

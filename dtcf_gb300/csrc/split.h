@@ -24,7 +24,19 @@ struct SplitProblem {
 };
 
 struct SplitPlan;
-int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitPlan** out);
+// Memory of a split plan.  Slices of a constant plan operand (static_a /
+// static_b) persist with the plan; everything rewritten by each run (the
+// other operands' slices and exponents, split-K partial sums) lives in
+// `arena` when given (split_plan_sizes bytes, 256-byte aligned, shared by
+// plans that never run at the same time), else in the plan's own buffer.
+struct SplitMem {
+  bool static_a = false, static_b = false;
+  unsigned char* arena = nullptr;
+};
+int split_plan_sizes(const std::vector<SplitProblem>& probs, int slices, bool static_a, bool static_b,
+                     size_t* persist_bytes, size_t* arena_bytes);
+int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitPlan** out,
+                      const SplitMem* mem = nullptr);
 // plan_a / plan_b: re-split the operands that come from the plan's packed A /
 // B (false when unchanged since the last run, e.g. constant integrals).
 int run_split_plan(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st);

@@ -51,9 +51,22 @@ typedef struct gbx_cc_job gbx_cc_job;
  * [-2,-0.5] / [0.2,3.0], v_scale 1e-2, v_decay 8, block 16, CCSD, FP64). */
 GBX_API void gbx_cc_default_config(gbx_cc_config* cfg);
 /* Build the job: orbitals, integrals (on the device), plans, MP2 guess. */
+/* Device bytes a job of this configuration will hold once built
+ * (resident_bytes) and at most while it is being built (peak_bytes), and the
+ * algorithmic flops of one iteration, from host planning alone: no device
+ * memory is touched.  The serving loop admits jobs by resident_bytes.  Any
+ * output pointer may be NULL. */
+GBX_API int gbx_cc_footprint(const gbx_cc_config* cfg, double* resident_bytes, double* peak_bytes,
+                             double* flops_per_iter);
 GBX_API int gbx_cc_create(const gbx_cc_config* cfg, void* stream, gbx_cc_job** job);
 /* Enqueue niter Jacobi iterations on stream without waiting; the energy of
  * each lands in the job's device history. */
+/* Captures one iteration as a CUDA graph now (otherwise the first enqueue
+ * does it); a no-op when use_graph is 0 or the graph exists. */
+GBX_API int gbx_cc_capture(gbx_cc_job* job);
+/* GBX_ETIMEOUT if a bounded device wait of the split engine ran out in any
+ * iteration so far (reads the error words; call after the work finished). */
+GBX_API int gbx_cc_check(gbx_cc_job* job);
 GBX_API int gbx_cc_enqueue(gbx_cc_job* job, int niter, void* stream);
 /* Run niter iterations and return their correlation energies (host array of
  * niter); waits for the stream. */

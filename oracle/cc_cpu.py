@@ -17,7 +17,11 @@ import numpy as np
 
 SPACES = {"t1": "ov", "t2": "oovv", "tau": "oovv", "taut": "oovv", "Xa": "oovv", "Q": "oovv", "R2": "oovv",
           "R1": "ov", "Fae": "vv", "Fbe": "vv", "Fmi": "oo", "Fmj": "oo", "Fme": "ov", "Wmnij": "oooo",
-          "Xoooo": "oooo", "Wmbej": "ovvo", "Zp": "ooov", "V3": "oovo"}
+          "Xoooo": "oooo", "Wmbej": "ovvo", "Zp": "ooov", "V3": "oovo", "Lad": "oovv"}
+
+# Intermediates stored as canonical tiles only (antisymmetric index pairs, as
+# RRR stores unique blocks, tensor.cc:617-640): C positions of each pair.
+CANONICAL = {"Wmnij": [(0, 1), (2, 3)], "Lad": [(0, 1), (2, 3)], "Zp": [(0, 1)]}
 
 
 def spaces(name):
@@ -53,8 +57,8 @@ def contraction_list(method="ccsd"):
               ("Fbe", "be", "t1", "mb", "Fme", "me"), ("Fmj", "mj", "t1", "je", "Fme", "me")]
     L += [("Xa", "ijab", "t2", "ijae", "Fbe" if sd else "Fae", "be"),
           ("Xa", "ijab", "t2", "imab", "Fmj" if sd else "Fmi", "mj"),
-          ("R2", "ijab", tau, "mnab", "Wmnij", "mnij"),
-          ("R2", "ijab", "VVVV", "abef", tau, "ijef")]
+          ("Lad", "ijab", tau, "mnab", "Wmnij", "mnij"),
+          ("Lad", "ijab", "VVVV", "abef", tau, "ijef")]
     if sd:
         L += [("Zp", "ijma", tau, "ijef", "OVVV", "maef"), ("Xa", "ijab", "Zp", "ijma", "t1", "mb")]
     L += [("Xa", "ijab", "t2", "imae", "Wmbej", "mbej")]
@@ -89,16 +93,51 @@ def _conv(counts, sp, nirrep):
     return out
 
 
+def _conv_canonical(system, sp, pairs, nirrep):
+    """_conv over block tuples of the spaces sp whose block indices are
+    non-increasing on every position pair in pairs (element counts)."""
+    blocks = {"o": system.occ_blocks, "v": system.vir_blocks}
+    out = np.zeros(nirrep, dtype=np.int64)
+
+    def rec(pos, idx, h, size):
+        if pos == len(sp):
+            out[h] += size
+            return
+        for b, (ext, irr) in enumerate(blocks[sp[pos]]):
+            ok = all(not (j == pos and i < pos and idx[i] < b) and not (i == pos and j < pos and b < idx[j])
+                     for i, j in pairs)
+            if ok:
+                idx.append(b)
+                rec(pos + 1, idx, h ^ irr, size * ext)
+                idx.pop()
+
+    rec(0, [], 0, 1)
+    return out
+
+
+def _ext_counts(system, counts, nirrep, C, lc, X, lx):
+    """Counts of the external index tuples of operand X (labels lx) that C needs."""
+    sx = spaces(X)
+    pos = [i for i, l in enumerate(lx) if l in lc]
+    sp = "".join(sx[i] for i in pos)
+    ext = [lx[i] for i in pos]
+    pairs = [(ext.index(lc[ci]), ext.index(lc[cj])) for ci, cj in CANONICAL.get(C, [])
+             if lc[ci] in ext and lc[cj] in ext]
+    if not pairs:
+        return _conv(counts, sp, nirrep)
+    return _conv_canonical(system, sp, pairs, nirrep)
+
+
 def gemm_shapes(system, method="ccsd"):
     """Per-irrep (M, N, K) of every contraction of one iteration."""
     nirrep, counts = _irrep_counts(system)
     shapes = []
     for C, lc, A, la, B, lb in contraction_list(method):
-        sa, sb = spaces(A), spaces(B)
-        extA = "".join(sa[i] for i, l in enumerate(la) if l in lc)
-        extB = "".join(sb[i] for i, l in enumerate(lb) if l in lc)
+        sa = spaces(A)
         con = "".join(sa[i] for i, l in enumerate(la) if l in lb)
-        M, N, K = _conv(counts, extA, nirrep), _conv(counts, extB, nirrep), _conv(counts, con, nirrep)
+        M = _ext_counts(system, counts, nirrep, C, lc, A, la)
+        N = _ext_counts(system, counts, nirrep, C, lc, B, lb)
+        K = _conv(counts, con, nirrep)
         for h in range(nirrep):
             if M[h] and N[h] and K[h]:
                 shapes.append((int(M[h]), int(N[h]), int(K[h])))
