@@ -42,6 +42,8 @@ def parse():
     p.add_argument("--min-block", type=int, default=4)
     p.add_argument("--seed", type=int, default=1)
     p.add_argument("--slices", type=int, default=0)
+    p.add_argument("--autotune", type=int, default=1,
+                   help="1: the split job times each contraction's output tile widths when it is built")
     p.add_argument("--profile", action="store_true", help="print the per-step breakdown to stderr")
     p.add_argument("--kernel", choices=["ladder", "thin"], default=None,
                    help="time one split GEMM alone: 'ladder' = one irrep block of the <ab||ef> ladder of "
@@ -68,7 +70,8 @@ def parse():
 def workload(a):
     return {"workload": "ccsd_8irrep_o%d_v%d" % (a.nocc, a.nvir), "method": "CCSD spin-orbital (Jacobi)",
             "nocc": a.nocc, "nvir": a.nvir, "nirrep": a.nirrep, "block_min": a.min_block, "block_max": a.max_block,
-            "seed": a.seed, "l2": "inputs larger than L2 (integrals resident, > 3 GB)", "parallelism": "replicas"}
+            "seed": a.seed, "l2": "inputs larger than L2 (integrals resident, > 3 GB)", "parallelism": "replicas",
+            "split_slices": a.slices or 6, "split_autotune": a.autotune}
 
 
 class Clocks:
@@ -407,13 +410,7 @@ def main():
     primary = None
     clocks = None
     for eng in engines:
-        try:
-            job = Job(engine=eng, **common)
-        except Exception as ex:  # split engine unavailable in this build
-            if eng == "split" and a.engine == "auto":  # noqa: SIM102
-                print("split engine unavailable: %s" % ex, file=sys.stderr)
-                continue
-            raise
+        job = Job(engine=eng, autotune=1 if (a.autotune and eng == "split") else 0, **common)
         st = job.stats()
         steps = a.steps if primary is None else max(2, min(a.steps, 3))
         ck = Clocks(local)
@@ -423,7 +420,11 @@ def main():
         if primary is None:
             clocks = ck.stop()
         ms = max_over_ranks(ms)
-        energies = job.energies()
+        # the per-iteration energies of the first 12 iterations (untimed top-up)
+        have = len(job.energies()) - 1
+        if have < 12:
+            job.iterate(12 - have)
+        energies = job.energies()[1:13]
         results[eng] = dict(ms=ms / steps, steps=steps, stats=st, energies=energies, job=job)
         if primary is None:
             primary = eng
@@ -492,8 +493,10 @@ def main():
         F = results["fp64"]
         line["fp64_iter_s"] = sum_over_ranks(1000.0 / F["ms"])
         line["split_speedup_vs_fp64"] = F["ms"] / P["ms"]
-        m = min(len(F["energies"]), len(P["energies"]))
-        line["energy_err_vs_fp64_eh"] = float(np.max(np.abs(np.array(F["energies"][:m]) - np.array(P["energies"][:m]))))
+        err = np.abs(np.array(F["energies"]) - np.array(P["energies"]))
+        line["energy_err_vs_fp64_eh"] = float(np.max(err))
+        line["energy_err_per_iter_eh"] = [float(x) for x in err]
+        line["energy_iterations_compared"] = int(len(err))
     if rank == 0:
         try:
             cb = cpu_arm(a, 1, 1, "port")

@@ -17,7 +17,8 @@ class Config(ctypes.Structure):
                 ("slices", ctypes.c_int), ("use_graph", ctypes.c_int), ("split_all", ctypes.c_int),
                 ("seed", ctypes.c_uint64),
                 ("eps_occ_lo", ctypes.c_double), ("eps_occ_hi", ctypes.c_double), ("eps_vir_lo", ctypes.c_double),
-                ("eps_vir_hi", ctypes.c_double), ("v_scale", ctypes.c_double), ("v_decay", ctypes.c_double)]
+                ("eps_vir_hi", ctypes.c_double), ("v_scale", ctypes.c_double), ("v_decay", ctypes.c_double),
+                ("autotune", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):

@@ -561,7 +561,10 @@ int gbx_cc_job::materialize(cudaStream_t st) {
     arena_bytes = std::max(arena_bytes, w);
     scratch_bytes = std::max(scratch_bytes, sc);
   }
-  if (arena_bytes) GBX_TRY(dev_alloc((void**)&d_arena, arena_bytes));
+  if (arena_bytes) {
+    GBX_TRY(dev_alloc((void**)&d_arena, arena_bytes));
+    GBX_CUDA(cudaMemsetAsync(d_arena, 0, arena_bytes, st));
+  }
   unsigned char* d_scratch = nullptr;
   if (scratch_bytes) GBX_TRY(dev_alloc((void**)&d_scratch, scratch_bytes));
   for (auto& p : splans) GBX_TRY(p->moves.upload());
@@ -570,6 +573,7 @@ int gbx_cc_job::materialize(cudaStream_t st) {
     int rc = p->build(d_arena, d_scratch);
     if (rc == GBX_OK && (p->a_static || p->b_static))
       rc = p->prepare_static(plan_operands[i].first->d, plan_operands[i].second->d, st);
+    if (rc == GBX_OK && cfg.autotune) rc = p->tune_split(st);
     if (rc != GBX_OK) {
       cudaStreamSynchronize(st);
       dev_free(d_scratch);

@@ -828,11 +828,11 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
   return fn;
 }
 
-int encode_slices(CUtensorMap* map, const __nv_bfloat16* base, int64_t S, int64_t rows_p, int64_t Kp, int box_rows) {
+int encode_slices(CUtensorMap* map, const __nv_bfloat16* base, int64_t S, int64_t rows, int64_t Kp, int box_rows) {
   auto enc = get_encode();
   if (!enc) return fail(GBX_ECUDA, "cuTensorMapEncodeTiled unavailable");
-  cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows_p, (cuuint64_t)S};
-  cuuint64_t strides[2] = {(cuuint64_t)(Kp * 2), (cuuint64_t)(rows_p * Kp * 2)};
+  cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)S};
+  cuuint64_t strides[2] = {(cuuint64_t)(Kp * 2), (cuuint64_t)(rows * Kp * 2)};
   cuuint32_t box[3] = {(cuuint32_t)BK, (cuuint32_t)box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
   CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, (void*)base, dims, strides, box, estr,
@@ -983,9 +983,9 @@ int split_layout(const std::vector<SplitProblem>& probs, int S, bool static_a, b
     o.ra = a_const ? 0 : 1;
     o.rb = b_const ? 0 : 1;
     o.sa = L.slices[o.ra];
-    L.slices[o.ra] += S * o.Mp * o.Kp;
+    L.slices[o.ra] += S * q.M * o.Kp;
     o.sb = L.slices[o.rb];
-    L.slices[o.rb] += S * o.Np * o.Kp;
+    L.slices[o.rb] += S * q.N * o.Kp;
     o.ea = L.exps[o.ra];
     L.exps[o.ra] += o.Mp;
     o.eb = L.exps[o.rb];
@@ -1077,9 +1077,9 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
     const int bn = o.bn;
     // row sets are grouped by the plan operand they come from, so constant
     // plan operands can be split once
-    SplitRowSet a{p.A, p.M, p.K, slice_ptr(o.ra, o.sa), o.Mp * o.Kp, o.Kp, exp_ptr(o.ra, o.ea), 0,
+    SplitRowSet a{p.A, p.M, p.K, slice_ptr(o.ra, o.sa), p.M * o.Kp, o.Kp, exp_ptr(o.ra, o.ea), 0,
                   p.lda ? p.lda : p.K};
-    SplitRowSet b{p.B, p.N, p.K, slice_ptr(o.rb, o.sb), o.Np * o.Kp, o.Kp, exp_ptr(o.rb, o.eb), 0,
+    SplitRowSet b{p.B, p.N, p.K, slice_ptr(o.rb, o.sb), p.N * o.Kp, o.Kp, exp_ptr(o.rb, o.eb), 0,
                   p.ldb ? p.ldb : p.K};
     SplitRowSet& to_a = p.a_is_plan_b ? b : a;  // rows that come from plan A
     SplitRowSet& to_b = p.a_is_plan_b ? a : b;
@@ -1125,8 +1125,10 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
     d.ldc = p.ldc ? p.ldc : p.N;
     dp.push_back(d);
     CUtensorMap ma, mb;
-    GBX_TRY(encode_slices(&ma, slice_ptr(o.ra, o.sa), S, o.Mp, o.Kp, BM));
-    GBX_TRY(encode_slices(&mb, slice_ptr(o.rb, o.sb), S, o.Np, o.Kp, bn));
+    // slices hold only the real rows: a tile's rows past M (or N) lie outside
+    // the tensor and TMA fills them with zeros without reading memory
+    GBX_TRY(encode_slices(&ma, slice_ptr(o.ra, o.sa), S, p.M, o.Kp, BM));
+    GBX_TRY(encode_slices(&mb, slice_ptr(o.rb, o.sb), S, p.N, o.Kp, bn));
     maps.push_back(ma);
     maps.push_back(mb);
   }

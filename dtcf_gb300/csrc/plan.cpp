@@ -505,6 +505,7 @@ void ContractionPlan::split_problems(std::vector<SplitProblem>& sp) const {
     }
     q.C = d_Cbig + g.c_off;
     q.K = g.K;
+    q.width = split_width;
     sp.push_back(q);
   }
 }
@@ -607,12 +608,74 @@ int ContractionPlan::build(unsigned char* arena, unsigned char* static_scratch) 
     mem.static_a = a_static;
     mem.static_b = b_static;
     mem.arena = ws > off ? arena + off : nullptr;
+    split_arena = mem.arena;
+    split_arena_cap = ws > off ? ws - off : 0;
     GBX_TRY(create_split_plan(sp, slices, &split, &mem));
   }
   // uploads and zero fills above ran on the legacy default stream: finish
   // them before any other stream touches the plan's buffers
   GBX_CUDA(cudaStreamSynchronize(cudaStreamLegacy));
   return GBX_OK;
+}
+
+int ContractionPlan::tune_split(cudaStream_t st, int reps) {
+  if (!split) return GBX_OK;
+  cudaEvent_t e0, e1;
+  GBX_CUDA(cudaEventCreate(&e0));
+  GBX_CUDA(cudaEventCreate(&e1));
+  auto time_of = [&](SplitPlan* sp, float* best) -> int {
+    GBX_TRY(run_split_plan(sp, !a_static, !b_static, st));  // warm
+    *best = 1e30f;
+    for (int r = 0; r < reps; ++r) {
+      GBX_CUDA(cudaEventRecord(e0, st));
+      GBX_TRY(run_split_plan(sp, !a_static, !b_static, st));
+      GBX_CUDA(cudaEventRecord(e1, st));
+      GBX_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      GBX_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      *best = std::min(*best, ms);
+    }
+    return GBX_OK;
+  };
+  float best = 0.f;
+  int rc = time_of(split, &best);
+  const int keep_w = split_width;
+  int best_w = keep_w;
+  for (int w : {64, 128, 256}) {
+    if (rc != GBX_OK) break;
+    if (w == keep_w) continue;
+    split_width = w;
+    std::vector<SplitProblem> sp;
+    split_problems(sp);
+    size_t k = 0, ws = 0;
+    rc = split_plan_sizes(sp, slices, a_static, b_static, &k, &ws);
+    if (rc != GBX_OK) break;
+    if (ws > split_arena_cap) continue;  // a candidate must fit the arena the plan was given
+    SplitMem mem;
+    mem.static_a = a_static;
+    mem.static_b = b_static;
+    mem.arena = split_arena;
+    SplitPlan* alt = nullptr;
+    rc = create_split_plan(sp, slices, &alt, &mem);
+    if (rc == GBX_OK && cudaStreamSynchronize(cudaStreamLegacy) != cudaSuccess) rc = fail(GBX_ECUDA, "sync failed");
+    // constant operands: split again from the packed scratch
+    if (rc == GBX_OK && (a_static || b_static)) rc = split_operands(alt, a_static, b_static, st);
+    float ms = 0.f;
+    if (rc == GBX_OK) rc = time_of(alt, &ms);
+    cudaStreamSynchronize(st);
+    if (rc == GBX_OK && ms < 0.97f * best) {
+      destroy_split_plan(split);
+      split = alt;
+      best = ms;
+      best_w = w;
+    } else {
+      destroy_split_plan(alt);
+    }
+  }
+  split_width = best_w;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
 }
 
 int ContractionPlan::prepare_static(const double* dA, const double* dB, cudaStream_t st) {

@@ -141,6 +141,9 @@ struct ContractionPlan {
   bool static_ready = false;
   int n_split_groups = 0, n_f64_groups = 0;
   bool split_all = false;
+  int split_width = 0;  // output tile width of every split problem (0 = the model's choice)
+  unsigned char* split_arena = nullptr;  // the split plan's per-run region and its capacity
+  size_t split_arena_cap = 0;
 
   ~ContractionPlan();
   // Device bytes the plan keeps for itself, the arena bytes one execute
@@ -159,6 +162,11 @@ struct ContractionPlan {
   int stage(const double* dA, const double* dB, cudaStream_t st);
   // C += alpha * A * B.
   int execute(const double* dA, const double* dB, double* dC, double alpha, cudaStream_t st);
+  // Autotuner: times the split GEMMs (with their per-run splits) at output
+  // tile widths 64, 128 and 256 against the current choice and keeps the
+  // fastest.  Call right after prepare_static, while the static scratch
+  // still holds this plan's constant operands; timing runs on st.
+  int tune_split(cudaStream_t st, int reps = 3);
 
  private:
   void split_problems(std::vector<SplitProblem>& sp) const;

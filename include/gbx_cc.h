@@ -35,6 +35,7 @@ typedef struct {
     uint64_t seed;
     double eps_occ_lo, eps_occ_hi, eps_vir_lo, eps_vir_hi;
     double v_scale, v_decay; /* |<pq||rs>| = v_scale * exp(-(|p-q| + |r-s|) / v_decay) */
+    int autotune;        /* time each split contraction's output tile widths when the job is built */
 } gbx_cc_config;
 
 typedef struct {

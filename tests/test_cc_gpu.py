@@ -77,3 +77,19 @@ def test_cc_gemm_shapes_match_oracle_planner():
     got = sorted(map(tuple, job.gemm_shapes().tolist()))
     want = sorted(cc_cpu.gemm_shapes(_system(case), "ccsd"))
     assert got == want
+
+
+def test_cc_split_autotune_keeps_energies():
+    """The width autotuner changes tile shapes only: energies agree with the
+    model-chosen plans to 1e-12 Eh and with the FP64 oracle to 1e-10 Eh."""
+    from dtcf_gb300.cc import Job
+    case = dict(nocc=12, nvir=60, nirrep=4, max_block=10, min_block=1, seed=13)
+    a = Job(method="ccsd", engine="split", split_all=1, **case)
+    b = Job(method="ccsd", engine="split", split_all=1, autotune=1, **case)
+    ea, eb = a.iterate(3), b.iterate(3)
+    assert np.max(np.abs(ea - eb)) <= 1e-12
+    ref = occ.CC(_system(case), "ccsd")
+    e_ref = np.array(ref.iterate(3)[1:])
+    assert np.max(np.abs(eb - e_ref)) <= 1e-10
+    a.close()
+    b.close()
