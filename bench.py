@@ -41,7 +41,9 @@ def parse():
     p.add_argument("--max-block", type=int, default=40)
     p.add_argument("--min-block", type=int, default=4)
     p.add_argument("--seed", type=int, default=1)
-    p.add_argument("--slices", type=int, default=0)
+    p.add_argument("--slices", type=int, default=4,
+                   help="bf16 slices per FP64 operand on the split path (4: energy error ~1e-11 Eh over 12 "
+                        "iterations of the default workload, inside the 1e-10 Eh bound; 6: ~1e-16)")
     p.add_argument("--autotune", type=int, default=1,
                    help="1: the split job times each contraction's output tile widths when it is built")
     p.add_argument("--profile", action="store_true", help="print the per-step breakdown to stderr")
@@ -71,7 +73,7 @@ def workload(a):
     return {"workload": "ccsd_8irrep_o%d_v%d" % (a.nocc, a.nvir), "method": "CCSD spin-orbital (Jacobi)",
             "nocc": a.nocc, "nvir": a.nvir, "nirrep": a.nirrep, "block_min": a.min_block, "block_max": a.max_block,
             "seed": a.seed, "l2": "inputs larger than L2 (integrals resident, > 3 GB)", "parallelism": "replicas",
-            "split_slices": a.slices or 6, "split_autotune": a.autotune}
+            "split_slices": a.slices, "split_autotune": a.autotune}
 
 
 class Clocks:
