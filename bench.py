@@ -118,10 +118,8 @@ class Clocks:
 
 
 def dist_setup():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    from dtcf_gb300.replicas import world
+    return world()
 
 
 def cpu_arm(a, steps, warmup, label_impl):
@@ -371,23 +369,7 @@ def main():
         dist.init_process_group("nccl")
     from dtcf_gb300.cc import Job
 
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
-
-    def max_over_ranks(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
-
-    def sum_over_ranks(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t)
-        return float(t.item())
+    from dtcf_gb300.replicas import barrier, max_over_ranks, sum_over_ranks
 
     common = dict(nocc=a.nocc, nvir=a.nvir, nirrep=a.nirrep, max_block=a.max_block, min_block=a.min_block,
                   seed=a.seed, method="ccsd", slices=a.slices)

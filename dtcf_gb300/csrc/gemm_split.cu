@@ -664,6 +664,227 @@ __global__ void __launch_bounds__(kThinThreads, 1) split_thin_kernel(const GemmP
   }
 }
 
+// ---- k-stationary kernel: S <= 4, 64-column output tiles -----------------
+//
+// The pair-by-pair kernel above streams a k-block's A and B slices once per
+// slice pair that uses them (2 S (S + 1) / 2 tile loads per k-block).  Here
+// every k-block's S A slices and S B slices are loaded once into a ring of
+// (A_s, B_s) slots and all S (S + 1) / 2 products are issued from there into
+// per-level TMEM accumulators (level l at columns l * 64 of a buffer, two
+// buffers).  A level sums at most S products of 64 K-elements per k-block,
+// each below 2^20 in magnitude, so 16 / S k-blocks fit below 2^24 and the
+// FP32 sums are exact; the drain warps then combine the levels into an exact
+// int64 Y = sum_l X_l 2^(8 (L - l)) per output (|Y| <= K 2^(14 + 8 L) < 2^63
+// for L <= 3 and K < 2^24) and scale it to FP64 once per tile.
+constexpr int kKsBN = 64;
+constexpr int kKsSlots = 8;        // (A slice, B slice) pairs, 24 KB each: two k-blocks of 4 slices
+constexpr int kKsDrainWarps = 8;   // 4 TMEM lane quarters x 2 column halves
+constexpr int kKsThreads = 64 + 32 * kKsDrainWarps;
+constexpr int kKsMaxS = 4;
+
+struct KsSmem {
+  alignas(1024) __nv_bfloat16 a[kKsSlots][BM * BK];
+  alignas(1024) __nv_bfloat16 b[kKsSlots][kKsBN * BK];
+  uint64_t full[kKsSlots], empty[kKsSlots], accfull[2], accempty[2], done;
+  uint32_t tmem_base;
+};
+
+__global__ void __launch_bounds__(kKsThreads, 1) split_ks_kernel(const GemmParams P) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  KsSmem& sm = *reinterpret_cast<KsSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int S = P.S, L = P.L;
+  const int D = 16 / S;  // k-blocks per exact accumulation group
+  constexpr uint32_t kTx = (BM + kKsBN) * BK * 2;
+  constexpr uint32_t kCols = 512;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kKsSlots; ++i) {
+      mbar_init(&sm.full[i], 1);
+      mbar_init(&sm.empty[i], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&sm.accfull[b], 1);
+      mbar_init(&sm.accempty[b], kKsDrainWarps);
+    }
+    mbar_init(&sm.done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm.tmem_base)),
+                 "r"(kCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = sm.tmem_base;
+  const uint32_t buf_cols = (uint32_t)(S * kKsBN);
+
+  if (warp == 0) {
+    // ---------------- TMA producer: a k-block's S slice pairs ----------------
+    if (lane == 0) {
+      int slot = 0;
+      uint32_t phase = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < P.total_tiles && ok; tile += gridDim.x) {
+        const TileInfo ti = decode_tile<kKsBN>(P, tile);
+        const CUtensorMap* ma = P.maps + 2 * ti.p;
+        const CUtensorMap* mb = P.maps + 2 * ti.p + 1;
+        for (int kb = ti.kb0; kb < ti.kb0 + ti.nkb && ok; ++kb)
+          for (int s = 0; s < S; ++s) {
+            if (!mbar_wait(&sm.empty[slot], phase ^ 1, P.err, 21)) {
+              ok = false;
+              break;
+            }
+            mbar_expect_tx(&sm.full[slot], kTx);
+            tma_load_3d(sm.a[slot], ma, &sm.full[slot], kb * BK, ti.m0, s);
+            tma_load_3d(sm.b[slot], mb, &sm.full[slot], kb * BK, ti.n0, s);
+            if (++slot == kKsSlots) {
+              slot = 0;
+              phase ^= 1;
+            }
+          }
+      }
+      for (int i = 0; i < kKsSlots; ++i) {
+        if (--slot < 0) {
+          slot = kKsSlots - 1;
+          phase ^= 1;
+        }
+        long long t0 = clock64();
+        while (!mbar_try_wait(&sm.full[slot], phase) && !mbar_try_wait(&sm.empty[slot], phase)) {
+          if (clock64() - t0 > kWaitCycles) {
+            atomicCAS(P.err, 0, 25);
+            break;
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      int slot = 0, buf = 0;
+      uint32_t phase = 0, aphase = 0;
+      bool ok = true;
+      constexpr uint32_t idesc = idesc_bf16<kKsBN>();
+      for (int tile = blockIdx.x; tile < P.total_tiles && ok; tile += gridDim.x) {
+        const int nkb = decode_tile<kKsBN>(P, tile).nkb;
+        for (int g0 = 0; g0 < nkb && ok; g0 += D) {
+          if (!mbar_wait(&sm.accempty[buf], aphase ^ 1, P.err, 22)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const int g1 = min(nkb, g0 + D);
+          for (int kb = g0; kb < g1 && ok; ++kb) {
+            int sl[kKsMaxS];
+            for (int s = 0; s < S; ++s) {
+              sl[s] = slot;
+              if (!mbar_wait(&sm.full[slot], phase, P.err, 23)) {
+                ok = false;
+                break;
+              }
+              if (++slot == kKsSlots) {
+                slot = 0;
+                phase ^= 1;
+              }
+            }
+            if (!ok) break;
+            tc_fence_after();
+            for (int l = 0; l <= L; ++l) {
+              const uint32_t d = tmem + (uint32_t)buf * buf_cols + (uint32_t)(l * kKsBN);
+              bool first = kb == g0;
+              for (int s = max(1, l + 2 - S); s <= min(S, l + 1); ++s) {
+                const int t = l + 2 - s;
+                const uint64_t a0 = sdesc(smem_u32(sm.a[sl[s - 1]]));
+                const uint64_t b0 = sdesc(smem_u32(sm.b[sl[t - 1]]));
+#pragma unroll
+                for (int k = 0; k < BK / 16; ++k) {
+                  umma(d, a0 + (uint64_t)(k * 2), b0 + (uint64_t)(k * 2), idesc, first ? 0u : 1u);
+                  first = false;
+                }
+              }
+            }
+            for (int s = 0; s < S; ++s) umma_commit(&sm.empty[sl[s]]);
+          }
+          if (!ok) break;
+          umma_commit(&sm.accfull[buf]);
+          if (++buf == 2) {
+            buf = 0;
+            aphase ^= 1;
+          }
+        }
+      }
+      umma_commit(&sm.done);
+      mbar_wait(&sm.done, 0, P.err, 26);
+    }
+  } else {
+    // ---------------- drain: exact int64 level recombination ----------------
+    const int quarter = warp & 3;               // TMEM lanes this warp may read
+    const int half = (warp - 2) >> 2;           // which 32 of the 64 columns
+    const uint32_t lane_addr = (uint32_t)(quarter * 32) << 16;
+    int buf = 0;
+    uint32_t aphase = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < P.total_tiles && ok; tile += gridDim.x) {
+      const TileInfo ti = decode_tile<kKsBN>(P, tile);
+      const DevProblem& pr = P.probs[ti.p];
+      long long Y[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) Y[j] = 0;
+      for (int g0 = 0; g0 < ti.nkb; g0 += D) {
+        int w_ok = lane == 0 ? (int)mbar_wait(&sm.accfull[buf], aphase, P.err, 24) : 1;
+        w_ok = __shfl_sync(0xffffffffu, w_ok, 0);
+        if (!w_ok) {
+          ok = false;
+          break;
+        }
+        __syncwarp();
+        tc_fence_after();
+        for (int l = 0; l <= L; ++l) {
+          uint32_t r[2][16];
+          const uint32_t col = (uint32_t)buf * buf_cols + (uint32_t)(l * kKsBN + half * 32);
+          tmem_ld16(tmem + lane_addr + col, r[0]);
+          tmem_ld16(tmem + lane_addr + col + 16, r[1]);
+          tmem_wait_ld();
+          const int sh = 8 * (L - l);
+          const long long w = 1ll << sh;
+#pragma unroll
+          for (int j = 0; j < 32; ++j) Y[j] += (long long)__float2int_rn(__uint_as_float(r[j >> 4][j & 15])) * w;
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sm.accempty[buf]);
+        if (++buf == 2) {
+          buf = 0;
+          aphase ^= 1;
+        }
+      }
+      if (!ok) break;
+      const int row = ti.m0 + quarter * 32 + lane;
+      if (row < pr.M) {
+        const int ea = pr.eA[row];
+        double* crow = pr.ksplit > 1 ? pr.partial + ((int64_t)ti.kc * pr.M + row) * pr.N : pr.C + (int64_t)row * pr.ldc;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int col = ti.n0 + half * 32 + j;
+          if (col < pr.N) {
+            int ex = ea + pr.eB[col] - 2 * 1022 - 14 - 8 * L + 1023;
+            ex = ex < 1 ? 1 : (ex > 2046 ? 2046 : ex);
+            crow[col] = (double)Y[j] * __longlong_as_double((long long)ex << 52);
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols));
+  }
+}
+
 // Fixed-order sum of the split-K partial contributions into C.
 __global__ void __launch_bounds__(256) split_reduce_kernel(const DevProblem* __restrict__ probs,
                                                            const int* __restrict__ red_prob,
@@ -853,8 +1074,11 @@ int encode_slices(CUtensorMap* map, const __nv_bfloat16* base, int64_t S, int64_
 constexpr int kWidths[4] = {32, 64, 128, 256};
 static int g_width_override = 0;
 
-int choose_width(int64_t N) {
+int choose_width(int64_t N, int S) {
   if (g_width_override) return g_width_override;
+  // up to 4 slices the k-stationary kernel (64 columns) loads every slice
+  // once per k-block and keeps its sums in registers
+  if (S <= kKsMaxS) return kKsBN;
   int best = 256;
   double best_cost = 1e300;
   for (int bn : kWidths) {
@@ -971,7 +1195,9 @@ int split_layout(const std::vector<SplitProblem>& probs, int S, bool static_a, b
     SplitLayout::Prob o;
     // thin-K problems (one k-block, at most 32 columns) take the thin kernel
     o.thin = q.K <= BK && q.N <= kThinBN && S <= 7;
-    o.bn = o.thin ? kThinBN : (q.width ? q.width : choose_width(q.N));
+    o.bn = o.thin ? kThinBN : (q.width ? q.width : choose_width(q.N, S));
+    // the k-stationary kernel's exact int64 sums need K < 2^24
+    if (!o.thin && S <= kKsMaxS && o.bn == kKsBN && q.K >= (1 << 24)) o.bn = 128;
     if (!o.thin && o.bn != 32 && o.bn != 64 && o.bn != 128 && o.bn != 256)
       return fail(GBX_EINVAL, "split tile width %d", o.bn);
     o.Mp = (q.M + BM - 1) / BM * BM;
@@ -1190,6 +1416,8 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
   GBX_TRY(set_smem_attr<64>());
   GBX_TRY(set_smem_attr<128>());
   GBX_TRY(set_smem_attr<256>());
+  GBX_CUDA(cudaFuncSetAttribute(split_ks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(sizeof(KsSmem) + 1024)));
   GBX_CUDA(cudaFuncSetAttribute(split_thin_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)(sizeof(ThinSmem) + 1024)));
   *out = sp.release();
@@ -1264,7 +1492,23 @@ int run_split_plan(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st) {
     }
     switch (L.bn) {
       case 32: GBX_TRY(launch_width<32>(sp, L, nsm, st)); break;
-      case 64: GBX_TRY(launch_width<64>(sp, L, nsm, st)); break;
+      case 64:
+        if (sp->S <= kKsMaxS) {
+          GemmParams P;
+          P.probs = L.d_probs;
+          P.tile_first = L.d_tile_first;
+          P.maps = L.d_maps;
+          P.nprob = L.nprob;
+          P.total_tiles = L.total_tiles;
+          P.S = sp->S;
+          P.L = sp->L;
+          P.err = sp->d_err;
+          split_ks_kernel<<<std::min(L.total_tiles, nsm), kKsThreads, sizeof(KsSmem) + 1024, st>>>(P);
+          GBX_CUDA(cudaGetLastError());
+        } else {
+          GBX_TRY(launch_width<64>(sp, L, nsm, st));
+        }
+        break;
       case 128: GBX_TRY(launch_width<128>(sp, L, nsm, st)); break;
       default: GBX_TRY(launch_width<256>(sp, L, nsm, st)); break;
     }

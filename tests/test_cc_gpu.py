@@ -93,3 +93,21 @@ def test_cc_split_autotune_keeps_energies():
     assert np.max(np.abs(eb - e_ref)) <= 1e-10
     a.close()
     b.close()
+
+
+def test_ccd_config2_fp64_and_split_ten_iterations():
+    """CCD at o=32, v=128, block 16 from the MP2 guess, 10 Jacobi iterations:
+    the split path's energies stay within 1e-10 Eh of the FP64 path's at
+    every iteration, and the iteration converges."""
+    from dtcf_gb300.cc import Job
+    case = dict(nocc=32, nvir=128, nirrep=1, max_block=16, min_block=1, seed=1, method="ccd")
+    f = Job(engine="fp64", **case)
+    s = Job(engine="split", slices=4, **case)
+    ef = np.concatenate([f.energies()[:1], f.iterate(10)])
+    es = np.concatenate([s.energies()[:1], s.iterate(10)])
+    assert ef[0] == es[0]  # the MP2 guess is computed identically
+    assert np.max(np.abs(ef - es)) <= 1e-10
+    steps = np.abs(np.diff(ef))
+    assert steps[-1] < steps[0] and np.all(np.isfinite(ef))
+    f.close()
+    s.close()

@@ -79,3 +79,47 @@ def test_split_gemm_thin_k_exact(M, N, K):
     dtcf_gb300.split_gemm(dev(Af), dev(Bf), C, slices=7)
     ref = Af @ Bf.T
     assert np.linalg.norm(C.cpu().numpy() - ref) <= 1e-15 * max(np.linalg.norm(ref), 1e-300) * 10
+
+
+@pytest.mark.parametrize("slices", [2, 3, 4])
+@pytest.mark.parametrize("M,N,K", [(128, 64, 64), (300, 270, 2100), (129, 33, 70), (100, 40, 40000), (257, 190, 4100)])
+def test_split_gemm_k_stationary_exact(slices, M, N, K):
+    """Up to 4 slices the 64-column k-stationary kernel runs (all slice
+    products of a k-block from one load of each slice, exact int64 sums):
+    exact on integers whose digits all fall in the kept slice products
+    (|x| < 2^(8 h - 2) with h = (slices + 1) // 2 leading digits), including
+    several accumulation groups, ragged edges and a split K."""
+    import dtcf_gb300
+    rng = np.random.default_rng(M + N + K + slices)
+    lim = 1 << (8 * ((slices + 1) // 2) - 2)
+    A = rng.integers(-lim, lim, size=(M, K)).astype(np.float64)
+    B = rng.integers(-lim, lim, size=(N, K)).astype(np.float64)
+    want = (A.astype(np.int64) @ B.astype(np.int64).T).astype(np.float64)
+    C = torch.zeros((M, N), dtype=torch.float64, device="cuda")
+    dtcf_gb300.split_gemm(dev(A), dev(B), C, slices=slices)
+    assert np.array_equal(C.cpu().numpy(), want)
+
+
+def test_split_gemm_k_stationary_matches_pairwise_kernel():
+    """Random FP64 at 4 slices: the k-stationary kernel (width 64) and the
+    pair-by-pair kernel (width 128) keep the same slice products, so they
+    agree to FP64 rounding; both are within 2^-28 of the FP64 product."""
+    import dtcf_gb300
+    from dtcf_gb300._lib import lib
+    rng = np.random.default_rng(9)
+    M, N, K = 400, 300, 5000
+    A = rng.uniform(-1, 1, (M, K))
+    B = rng.uniform(-1, 1, (N, K))
+    want = A @ B.T
+    out = []
+    for w in (64, 128):
+        C = torch.zeros((M, N), dtype=torch.float64, device="cuda")
+        assert lib().gbx_split_set_width(w) == 0
+        try:
+            dtcf_gb300.split_gemm(dev(A), dev(B), C, slices=4)
+        finally:
+            lib().gbx_split_set_width(0)
+        out.append(C.cpu().numpy())
+    scale = np.linalg.norm(want)
+    assert np.linalg.norm(out[0] - out[1]) / scale < 1e-14
+    assert np.linalg.norm(out[0] - want) / scale < 2.0 ** -28
