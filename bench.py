@@ -48,8 +48,8 @@ def parse():
                    help="1: the split job times each contraction's output tile widths when it is built")
     p.add_argument("--profile", action="store_true", help="print the per-step breakdown to stderr")
     p.add_argument("--kernel", choices=["ladder", "thin"], default=None,
-                   help="time one split GEMM alone: 'ladder' = one irrep block of the <ab||ef> ladder of "
-                        "this workload (7200 x 288 x 7200); 'thin' = one irrep block of t_i^e <ab||ej> "
+                   help="time one split GEMM alone: 'ladder' = one irrep block of the canonical-tile "
+                        "<ab||ef> ladder of this workload (3600 x 144 x 7200); 'thin' = one irrep block of t_i^e <ab||ej> "
                         "(346174 x 8 x 38, the thin-K kernel)")
     p.add_argument("--rates", action="store_true", help="build and run the arithmetic-rate probe")
     p.add_argument("--grouped", type=int, default=0, metavar="T",
@@ -148,7 +148,7 @@ def kernel_arm(a):
     """One kernel alone, for profiling: the split GEMM on a ladder block."""
     import torch
     import dtcf_gb300
-    M, N, K = (7200, 288, 7200) if a.kernel == "ladder" else (346174, 8, 38)
+    M, N, K = (3600, 144, 7200) if a.kernel == "ladder" else (346174, 8, 38)
     g = torch.Generator(device="cuda").manual_seed(a.seed)
     A = torch.rand(M, K, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
     B = torch.rand(N, K, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
@@ -420,7 +420,11 @@ def main():
     value = sum_over_ranks(iters)
 
     # dominant kernel: per-step breakdown of one iteration (CUDA events on the launching stream)
+    # one eager iteration, step by step, inside an NVTX range so that a
+    # profiler can be pointed at exactly these launches (--nvtx-include iteration/)
+    torch.cuda.nvtx.range_push("iteration")
     prof = P["job"].profile(stream)
+    torch.cuda.nvtx.range_pop()
     if a.profile and rank == 0:
         for s in sorted(prof, key=lambda x: -x["ms"])[:25]:
             print("%9.3f ms  %10.3g fl  %s" % (s["ms"], s["flops"], s["name"]), file=sys.stderr)
@@ -436,7 +440,10 @@ def main():
         # tensor-pipe work of the slice products against the measured bf16 peak
         peak, src = peaks.get("bf16_tflops", 1900.0), "of measured (MEASURED_PEAKS.json bf16_tflops, burst)"
         achieved = kt["tensor_flops"] / (kt["ms"] * 1e-3) / 1e12
-        kname = "split_gemm_kernel (tcgen05 bf16 slices)"
+        pi = P["job"].plan_info(top["plan"])
+        w = pi["split_width"] or (64 if pi["slices"] <= 4 else 0)
+        kname = ("split_ks_kernel (tcgen05 bf16 slices, k-stationary, 64 columns)" if w == 64 and pi["slices"] <= 4
+                 else "split_gemm_kernel<%s> (tcgen05 bf16 slices)" % (w or "model width"))
     else:
         # FP64 tensor-pipe ceiling measured on this GPU (DMMA m8n8k4 throughput probe)
         peak, src = 1.05, "of measured DMMA probe (profiles/)"

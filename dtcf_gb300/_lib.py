@@ -45,6 +45,7 @@ SIGNATURES = {
     "gbx_cc_default_config": (None, [_p]),
     "gbx_cc_footprint": (_i, [_p, ctypes.POINTER(_d), ctypes.POINTER(_d), ctypes.POINTER(_d)]),
     "gbx_cc_capture": (_i, [_p]),
+    "gbx_cc_plan_info": (_i, [_p, _i, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)]),
     "gbx_cc_check": (_i, [_p]),
     "gbx_cc_create": (_i, [_p, _p, ctypes.POINTER(_p)]),
     "gbx_cc_enqueue": (_i, [_p, _i, _p]),

@@ -128,6 +128,12 @@ class Job:
                             plan=int(plan[i])))
         return out
 
+    def plan_info(self, contraction):
+        """dict(split_width, n_split, n_f64, slices) of one contraction's GEMMs."""
+        v = [ctypes.c_int() for _ in range(4)]
+        check(lib().gbx_cc_plan_info(self.handle, contraction, *[ctypes.byref(x) for x in v]))
+        return dict(zip(("split_width", "n_split", "n_f64", "slices"), (x.value for x in v)))
+
     def time_gemm(self, contraction, reps=5, stream=None):
         """GEMM launches of one contraction alone: dict(ms, fp64_flops, tensor_flops, engine)."""
         ms = ctypes.c_float()

@@ -884,6 +884,17 @@ int gbx_cc_profile(gbx_cc_job* job, int cap, float* ms, double* flops, double* b
   return GBX_OK;
 }
 
+int gbx_cc_plan_info(const gbx_cc_job* job, int contraction, int* split_width, int* n_split, int* n_f64,
+                     int* slices) {
+  if (!job || contraction < 0 || contraction >= (int)job->cplans.size()) return fail(GBX_EINVAL, "bad arguments");
+  const ContractionPlan* p = job->cplans[contraction].get();
+  if (split_width) *split_width = p->split_width;
+  if (n_split) *n_split = p->n_split_groups;
+  if (n_f64) *n_f64 = p->n_f64_groups;
+  if (slices) *slices = p->slices > 0 ? p->slices : 6;
+  return GBX_OK;
+}
+
 int gbx_cc_time_gemm(gbx_cc_job* job, int contraction, int reps, float* ms, double* fp64_flops,
                      double* tensor_flops, int* engine, void* stream) {
   if (!job || contraction < 0 || contraction >= (int)job->cplans.size() || reps < 1)

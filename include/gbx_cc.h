@@ -97,8 +97,13 @@ GBX_API int gbx_cc_read_energy(gbx_cc_job* job, double* energy, void* stream);
  * (or -1) and a name of name_len chars.  Counts as one iteration. */
 GBX_API int gbx_cc_profile(gbx_cc_job* job, int cap, float* ms, double* flops, double* bytes, int* kind, int* plan,
                            char* names, int name_len, int* count, void* stream);
-/* Time only the GEMM launches of one contraction (its operands as the last
- * iteration left them), reps times, with CUDA events on stream.  Reports
+/* Kernel choice of one contraction's packed GEMMs: the split output tile
+ * width (64 with at most 4 slices: the k-stationary kernel; 0: the width
+ * model's choice per GEMM), the number of split and FP64 GEMMs, the slices. */
+GBX_API int gbx_cc_plan_info(const gbx_cc_job* job, int contraction, int* split_width, int* n_split, int* n_f64,
+                             int* slices);
+/* Time only the GEMM launches of one contraction (its operands packed and
+ * split again first), reps times, with CUDA events on stream.  Reports
  * ms per run, the FP64 flops of the packed GEMMs, the bf16 tensor flops the
  * split engine issues, and the engine (0 FP64, 1 split, 2 both). */
 GBX_API int gbx_cc_time_gemm(gbx_cc_job* job, int contraction, int reps, float* ms, double* fp64_flops,
