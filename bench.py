@@ -452,6 +452,16 @@ def main():
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                 "traffic": None, "kernel": kname, "contraction": top["name"], "kernel_ms": kt["ms"],
                 "fp64_equiv_tflops": kt["fp64_flops"] / (kt["ms"] * 1e-3) / 1e12, "peak_source": src}
+    # DRAM traffic of the ladder launch from the committed ncu summary of one of
+    # its irrep blocks (scaled by the 8 blocks), when this is that workload
+    prof_md = os.path.join(ROOT, "profiles", "split_ks_kernel_ladder_3600x144x7200.md")
+    if (top["name"].startswith("Lad[ijab]+=VVVV") and "split_ks_kernel" in kname and os.path.exists(prof_md)
+            and (a.nocc, a.nvir, a.nirrep, a.max_block, a.min_block, a.seed, a.slices) == (48, 240, 8, 40, 4, 1, 4)):
+        for ln in open(prof_md):
+            if ln.startswith("traffic_bytes_per_ladder_launch:"):
+                roofline["traffic"] = float(ln.split(":")[1].split()[0])
+                roofline["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one irrep block x 8 "
+                                              "(profiles/split_ks_kernel_ladder_3600x144x7200.md)")
 
     # end to end through the public API with host buffers: every step copies the
     # amplitudes in from pinned host memory and reads the energy back

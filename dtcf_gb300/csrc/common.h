@@ -145,6 +145,8 @@ int64_t f64_partial_elems(const std::vector<GemmProblem>& probs);
 // Tile shapes shared by the host planner and the kernels.
 int f64_variant(int m, int n);
 int f64_variant(int m, int n, int k);
+// As f64_variant, plus variant 7 (at most 16 x 16 outputs, long K) for planned launches.
+int f64_variant_planned(int m, int n, int k);
 int f64_tile_m(int variant);
 int f64_tile_n(int variant);
 int f64_tiles(int m, int n);

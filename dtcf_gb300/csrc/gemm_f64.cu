@@ -32,6 +32,9 @@ constexpr int kRedChunk = 2048;
 constexpr int kThinN = 32, kThinK = 64, kThinMinWide = 16384;
 constexpr int kSmallK = 8;
 constexpr int kSmallKElems = 2048;  // output elements per CTA
+constexpr int kSmallOutDim = 16;    // small outputs: at most 16 x 16 ...
+constexpr int kSmallOutMinK = 4096;  // ... with at least this K
+constexpr int kSmallOutChunk = 4096;  // K per work item
 }  // namespace
 
 // Tile shapes: 64x64 for large problems, 64x16 / 16x64 / 16x16 for skinny ones
@@ -49,6 +52,12 @@ int f64_variant(int m, int n, int k) {
   return (m < 48 ? 2 : 0) + (n < 48 ? 1 : 0);
 }
 int f64_variant(int m, int n) { return (m < 48 ? 2 : 0) + (n < 48 ? 1 : 0); }
+// Planned launches also use variant 7: outputs of at most 16 x 16 with long
+// K, one CTA per K chunk holding the whole output (reduced in a fixed order).
+int f64_variant_planned(int m, int n, int k) {
+  if (m <= kSmallOutDim && n <= kSmallOutDim && k >= kSmallOutMinK) return 7;
+  return f64_variant(m, n, k);
+}
 int f64_tile_m(int variant) { return (variant & 2) ? 16 : 64; }
 int f64_tile_n(int variant) { return (variant & 1) ? 16 : 64; }
 int f64_tiles(int m, int n) {
@@ -267,6 +276,63 @@ __global__ void __launch_bounds__(256) small_k_gemm_f64_kernel(const GemmProblem
   }
 }
 
+// Small output, long K (variant 7): work item = one K chunk of one problem;
+// the CTA stages 64-wide K slices of all m rows of A and n rows of B in
+// shared memory, thread t accumulates output t % (m n) over every
+// (256 / (m n))-th k of the slice, and the lanes of an output are summed in
+// a fixed order into the chunk's partial (or C when there is one chunk).
+__global__ void __launch_bounds__(256) small_out_gemm_f64_kernel(const GemmProblem* __restrict__ probs, int nprob,
+                                                                 const int* __restrict__ item_first, int total) {
+  __shared__ double As[kSmallOutDim][65];
+  __shared__ double Bs[kSmallOutDim][65];
+  __shared__ double red[256];
+  const int tid = threadIdx.x;
+  for (int item = blockIdx.x; item < total; item += gridDim.x) {
+    int lo = 0, hi = nprob - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (item_first[mid] <= item) lo = mid; else hi = mid - 1;
+    }
+    const GemmProblem& p = probs[lo];
+    const int c = item - item_first[lo];
+    const int P = p.m * p.n, lanes = 256 / P;
+    const int out = tid % P, lane = tid / P;
+    const bool active = lane < lanes;
+    const int i = out / p.n, j = out - i * p.n;
+    const int k0 = c * p.kchunk, k1 = min(p.k, k0 + p.kchunk);
+    double acc = 0.0;
+    for (int kk = k0; kk < k1; kk += 64) {
+      const int kc = min(64, k1 - kk);
+      __syncthreads();
+      for (int e = tid; e < p.m * 64; e += 256) {
+        const int r = e >> 6, q = e & 63;
+        As[r][q] = q < kc ? __ldg(p.A + (int64_t)r * p.a_rs + (int64_t)(kk + q) * p.a_cs) : 0.0;
+      }
+      for (int e = tid; e < p.n * 64; e += 256) {
+        const int r = e >> 6, q = e & 63;
+        Bs[r][q] = q < kc ? __ldg(p.B + (int64_t)r * p.b_rs + (int64_t)(kk + q) * p.b_cs) : 0.0;
+      }
+      __syncthreads();
+      if (active)
+        for (int q = lane; q < kc; q += lanes) acc = fma(As[i][q], Bs[j][q], acc);
+    }
+    __syncthreads();
+    red[tid] = active ? acc : 0.0;
+    __syncthreads();
+    if (tid < P) {
+      double sum = 0.0;
+      for (int l = 0; l < lanes; ++l) sum = __dadd_rn(sum, red[l * P + tid]);
+      if (p.ksplit > 1) {
+        p.partial[(int64_t)c * P + tid] = sum;
+      } else {
+        double* cp = p.C + (int64_t)i * p.c_rs + j;
+        const double v = __dmul_rn(p.alpha, sum);
+        *cp = p.accumulate ? __dadd_rn(*cp, v) : v;
+      }
+    }
+  }
+}
+
 // Fixed-order reduction of split-K partials into C.
 __global__ void __launch_bounds__(kRedThreads) splitk_reduce_kernel(const GemmProblem* __restrict__ probs,
                                                                     const int* __restrict__ red_prob,
@@ -339,7 +405,14 @@ int64_t f64_partial_elems(const std::vector<GemmProblem>& probs) {
   for (auto& q : probs)
     if (q.m > 0 && q.n > 0) out_tiles += f64_tiles(q.m, q.n);
   for (auto& q : probs) {
-    if (q.m <= 0 || q.n <= 0 || f64_variant(q.m, q.n, q.k) >= 4) continue;
+    if (q.m <= 0 || q.n <= 0) continue;
+    const int v = f64_variant_planned(q.m, q.n, q.k);
+    if (v == 7) {
+      const int64_t ks7 = (q.k + kSmallOutChunk - 1) / kSmallOutChunk;
+      if (ks7 > 1) part += ks7 * q.m * q.n;
+      continue;
+    }
+    if (v >= 4) continue;
     int ks = 1, chunk = 0;
     f64_ksplit(q.k, out_tiles, &ks, &chunk);
     if (ks > 1) part += (int64_t)ks * q.m * q.n;
@@ -358,9 +431,10 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
     if (q.m <= 0 || q.n <= 0) continue;
     probs.push_back(q);
     int v = variants && i < variants->size() ? (*variants)[i] : -1;
-    if (v < -1 || v > 6) return fail(GBX_EINVAL, "FP64 tile variant %d", v);
+    if (v < -1 || v > 7) return fail(GBX_EINVAL, "FP64 tile variant %d", v);
     // the thin kernels need their shape limits
-    if ((v == 4 && q.n > kThinN) || (v == 5 && q.m > kThinN) || (v == 6 && q.k > kSmallK))
+    if ((v == 4 && q.n > kThinN) || (v == 5 && q.m > kThinN) || (v == 6 && q.k > kSmallK) ||
+        (v == 7 && (q.m > kSmallOutDim || q.n > kSmallOutDim)))
       return fail(GBX_EINVAL, "FP64 tile variant %d does not fit %d x %d x %d", v, q.m, q.n, q.k);
     want.push_back(v);
   }
@@ -376,7 +450,22 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
   for (int i = 0; i < nprob; ++i) {
     GemmProblem& q = probs[i];
     int ks = 1;
-    const int thin = want[i] >= 0 ? want[i] : f64_variant(q.m, q.n, q.k);
+    const int thin = want[i] >= 0 ? want[i] : f64_variant_planned(q.m, q.n, q.k);
+    if (thin == 7) {  // small output: one work item per K chunk, fixed-order reduction
+      ks = std::max(1, (q.k + kSmallOutChunk - 1) / kSmallOutChunk);
+      q.ksplit = ks;
+      q.kchunk = kSmallOutChunk;
+      q.partial = nullptr;
+      q.pad_ = 7;
+      if (ks > 1) {
+        q.partial = (double*)(intptr_t)(part_elems + 1);  // offset + 1, patched below
+        part_elems += (int64_t)ks * q.m * q.n;
+        red.push_back(i);
+        red_first.push_back((uint32_t)rc);
+        rc += ((uint64_t)q.m * q.n + kRedChunk - 1) / kRedChunk;
+      }
+      continue;
+    }
     if (thin >= 4) {  // thin and small-K kernels: no split-K
       q.ksplit = 1;
       q.kchunk = std::max(q.k, BK);
@@ -421,7 +510,7 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
   for (auto& q : probs)
     if (q.partial) q.partial = d_partial + ((intptr_t)q.partial - 1);
   // one launch per tile shape
-  for (int v = 0; v < 7; ++v) {
+  for (int v = 0; v < 8; ++v) {
     std::vector<GemmProblem> vp;
     std::vector<int> first;
     int64_t tiles = 0;
@@ -432,6 +521,7 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
       if (v == 4) tiles += (q.m + 255) / 256;
       else if (v == 5) tiles += (q.n + 255) / 256;
       else if (v == 6) tiles += ((int64_t)q.m * q.n + kSmallKElems - 1) / kSmallKElems;
+      else if (v == 7) tiles += q.ksplit;
       else tiles += (int64_t)((q.m + f64_tile_m(v) - 1) / f64_tile_m(v)) * ((q.n + f64_tile_n(v) - 1) / f64_tile_n(v)) * q.ksplit;
     }
     if (vp.empty()) continue;
@@ -491,6 +581,10 @@ int F64Gemm::run(cudaStream_t st) const {
         small_k_gemm_f64_kernel<<<std::min(sb.total_tiles, 152 * 8), 256, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first,
                                                                                    sb.total_tiles);
         break;
+      case 7:
+        small_out_gemm_f64_kernel<<<std::min(sb.total_tiles, 152 * 8), 256, 0, st>>>(sb.d_probs, sb.nprob,
+                                                                                     sb.d_first, sb.total_tiles);
+        break;
       default:
         thin_gemm_f64_kernel<false><<<std::min(sb.total_tiles, 152 * 8), 256, 0, st>>>(sb.d_probs, sb.nprob,
                                                                                        sb.d_first, sb.total_tiles);
@@ -518,6 +612,7 @@ int launch_one(int v, const GemmProblem* prob, const int* zero, int tiles, cudaS
     case 3: grouped_gemm_f64_kernel<16, 16><<<grid, kThreads, 0, st>>>(prob, 1, zero, tiles, nullptr); break;
     case 4: thin_gemm_f64_kernel<true><<<tgrid, 256, 0, st>>>(prob, 1, zero, tiles); break;
     case 6: small_k_gemm_f64_kernel<<<tgrid, 256, 0, st>>>(prob, 1, zero, tiles); break;
+    case 7: small_out_gemm_f64_kernel<<<tgrid, 256, 0, st>>>(prob, 1, zero, tiles); break;
     default: thin_gemm_f64_kernel<false><<<tgrid, 256, 0, st>>>(prob, 1, zero, tiles); break;
   }
   GBX_CUDA(cudaGetLastError());

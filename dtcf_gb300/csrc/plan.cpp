@@ -259,12 +259,14 @@ void choose_engine(GroupBlock& g, bool split_engine, bool split_all, int slices)
   const double t_split = split_cost(g.M, g.N);
   const double t_split_sw = split_cost(g.N, g.M);
   const int mi = (int)std::min<int64_t>(g.M, 1 << 30), ni = (int)std::min<int64_t>(g.N, 1 << 30);
-  const int v = f64_variant(mi, ni, (int)std::min<int64_t>(g.K, 1 << 30));
+  const int v = f64_variant_planned(mi, ni, (int)std::min<int64_t>(g.K, 1 << 30));
   // thin FP64: exact flops, or streaming the wide operand once, whichever binds
   const double wide = (double)std::max(g.M, g.N) * (double)g.K * 8.0;
   const double outs = (double)g.M * (double)g.N * 8.0;
   const double t_f64 =
-      v == 6 ? std::max(2.0 * (double)g.M * (double)g.N * (double)g.K / 0.9e12, outs / 5e12) + 2e-6
+      v == 7 ? std::max(2.0 * (double)g.M * (double)g.N * (double)g.K / 0.9e12,
+                        (double)(g.M + g.N) * (double)g.K * 8.0 / 5e12) + 4e-6
+      : v == 6 ? std::max(2.0 * (double)g.M * (double)g.N * (double)g.K / 0.9e12, outs / 5e12) + 2e-6
       : v >= 4 ? std::max(2.0 * (double)g.M * (double)g.N * (double)g.K / 0.9e12, wide / 5e12) + 2e-6
                : 2.0 * up(g.M, f64_tile_m(v)) * up(g.N, f64_tile_n(v)) * up(g.K, 16) / 0.95e12;
   const double best_split = std::min(t_split, t_split_sw) + 4e-6;  // + split and launch overhead

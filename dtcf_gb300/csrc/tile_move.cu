@@ -119,27 +119,42 @@ __global__ void __launch_bounds__(kMoveThreads) tile_move_kernel(const MoveDesc*
     const double scale = op == 0 ? md.scale : __dmul_rn(md.scale, alpha);
     const double* __restrict__ s = src + md.src;
     double* __restrict__ t = dst + md.dst;
-#pragma unroll 2
-    for (int k = 0; k < kMoveChunk / kMoveThreads; ++k) {
-      uint32_t e = base + (uint32_t)(k * kMoveThreads) + threadIdx.x;
-      if (e >= n) break;
-      int64_t so = 0, to = 0;
-      uint32_t rem = e;
+    // all addresses first, then every load, then every store: eight
+    // independent loads in flight per thread
+    constexpr int kPer = kMoveChunk / kMoveThreads;
+    int64_t so[kPer], to[kPer];
+    bool in[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+      const uint32_t e = base + (uint32_t)(k * kMoveThreads) + threadIdx.x;
+      in[k] = e < n;
+      so[k] = 0;
+      to[k] = 0;
+      uint32_t rem = in[k] ? e : 0;
       for (int d = rank - 1; d > 0; --d) {
-        uint32_t q = md.div[d].div(rem);
-        uint32_t i = rem - q * md.ext[d];
-        so += (int64_t)i * md.sstr[d];
-        to += (int64_t)i * md.dstr[d];
+        const uint32_t q = md.div[d].div(rem);
+        const uint32_t i = rem - q * md.ext[d];
+        so[k] += (int64_t)i * md.sstr[d];
+        to[k] += (int64_t)i * md.dstr[d];
         rem = q;
       }
-      so += (int64_t)rem * md.sstr[0];
-      to += (int64_t)rem * md.dstr[0];
-      double x = __ldg(s + so);
-      if (op == 0) {
-        t[to] = (scale == 1.0) ? x : __dmul_rn(scale, x);
-      } else {
-        t[to] = __dadd_rn(t[to], __dmul_rn(scale, x));
-      }
+      so[k] += (int64_t)rem * md.sstr[0];
+      to[k] += (int64_t)rem * md.dstr[0];
+    }
+    double x[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) x[k] = in[k] ? __ldg(s + so[k]) : 0.0;
+    if (op == 0) {
+#pragma unroll
+      for (int k = 0; k < kPer; ++k)
+        if (in[k]) t[to[k]] = (scale == 1.0) ? x[k] : __dmul_rn(scale, x[k]);
+    } else {
+      double y[kPer];
+#pragma unroll
+      for (int k = 0; k < kPer; ++k) y[k] = in[k] ? t[to[k]] : 0.0;
+#pragma unroll
+      for (int k = 0; k < kPer; ++k)
+        if (in[k]) t[to[k]] = __dadd_rn(y[k], __dmul_rn(scale, x[k]));
     }
   }
 }

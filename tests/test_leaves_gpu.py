@@ -221,3 +221,21 @@ def test_grouped_gemm_small_k(gbx, m, n, k):
     dA, dB, dC = dev(A), dev(B), dev(C)
     gbx.grouped_gemm_f64([Triple(dA.data_ptr(), dB.data_ptr(), dC.data_ptr(), k, 1, k, 1, n, m, n, k, 0.5, 1)])
     np.testing.assert_allclose(host(dC).reshape(m, n), C + 0.5 * A @ B.T, rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.parametrize("m,n,k,acc", [(6, 6, 20000, 1), (16, 16, 8192, 0), (3, 11, 5000, 1), (16, 1, 4096, 0)])
+def test_grouped_gemm_small_output_long_k(gbx, m, n, k, acc):
+    """Outputs of at most 16 x 16 with K >= 4096: one CTA per K chunk holds the
+    whole output, chunks reduced in a fixed order."""
+    from dtcf_gb300.leaves import Triple
+    rng = np.random.default_rng(m * n + k)
+    A, B, C = rng.standard_normal((m, k)), rng.standard_normal((n, k)), rng.standard_normal((m, n))
+    dA, dB, dC = dev(A), dev(B), dev(C)
+    gbx.grouped_gemm_f64([Triple(dA.data_ptr(), dB.data_ptr(), dC.data_ptr(), k, 1, k, 1, n, m, n, k, -0.75, acc)])
+    want = (C if acc else 0.0) - 0.75 * A @ B.T
+    np.testing.assert_allclose(host(dC).reshape(m, n), want, rtol=1e-12, atol=1e-12 * np.sqrt(k))
+    # and through the leaf entry point with a transposed A (strided operand reads)
+    dC2 = dev(C)
+    At = np.ascontiguousarray(A.T)
+    gbx.local_contraction(m, n, k, dev(At), dB, dC2, 1, 1, -0.75)
+    np.testing.assert_allclose(host(dC2).reshape(m, n), C - 0.75 * A @ B.T, rtol=1e-12, atol=1e-12 * np.sqrt(k))
