@@ -295,7 +295,7 @@ def serve_arm(a):
     out, energies = {}, {}
     for eng in a.serve_engines.split(","):
         s = Server(budget_bytes=a.serve_budget_gb * 1e9, slots=a.serve_slots)
-        ids = [s.add_job(config(engine=eng, **j)) for j in jobs]
+        ids = [s.add_job(config(engine=eng, slices=a.slices if eng == "split" else 0, **j)) for j in jobs]
         for job, t in stream:
             s.submit(ids[job], t)
         clocks = Clocks(0)
@@ -323,6 +323,7 @@ def serve_arm(a):
                       "workload": "cc_serving_%djobs_o16-%d_v4-6o_halfsym" % (a.serve, a.serve_o_max),
                       "jobs": a.serve, "requests_per_job": a.serve_requests, "arrival_rate_per_s": a.serve_rate,
                       "budget_gb": a.serve_budget_gb, "slots": a.serve_slots, "time_limit_s": a.serve_limit,
+                      "split_slices": a.slices,
                       "seed": a.seed, "engines": out, "energy_max_diff_split_vs_fp64_eh": diff,
                       "data": "synthetic (seeded)"}))
     return 0

@@ -254,13 +254,15 @@ struct gbx_cc_job {
     return tilesets.back().get();
   }
 
-  // out = in / D over the tiles of out (the tile set is built with the job)
-  int denom(const char* out, const char* in, CCTileSet** ts) {
-    CCTensor *O = get(out), *I = get(in);
+  // out = in * (1/D), the inverse orbital-energy denominators computed once
+  // when the job is built (out, in and the inverse share one tile layout)
+  int denom(const char* out, const char* in, const char* dinv) {
+    CCTensor *O = get(out), *I = get(in), *Dv = get(dinv);
     dynamic_use.insert(out);
     dynamic_use.insert(in);
-    steps.push_back([=](cudaStream_t st) { return run_cc_tiles(**ts, CC_OP_DENOM, tab, I->d, O->d, st); });
-    info.push_back({std::string(out) + "=" + in + "/D", 3, 0.0, 16.0 * (double)O->L.nelem});
+    const int64_t n = O->L.nelem;
+    steps.push_back([=](cudaStream_t st) { return run_mul(I->d, Dv->d, O->d, n, st); });
+    info.push_back({std::string(out) + "=" + in + "/D", 3, 0.0, 24.0 * (double)O->L.nelem});
     launches += 1;
     return GBX_OK;
   }
@@ -300,8 +302,11 @@ int gbx_cc_job::plan_all() {
   const bool sd = cfg.method == GBX_CC_CCSD;
   // amplitudes, residuals, intermediates
   GBX_TRY(tensor("t2", "oovv"));
+  GBX_TRY(tensor("Dinv2", "oovv"));  // 1 / (e_i + e_j - e_a - e_b)
   GBX_TRY(tensor("R2", "oovv"));
   GBX_TRY(tensor("Xa", "oovv"));
+  GBX_TRY(tensor("Xb", "oovv"));
+  GBX_TRY(tensor("Xj", "oovv"));
   GBX_TRY(tensor("Fae", "vv"));
   GBX_TRY(tensor("Fmi", "oo"));
   // W_mnij is antisymmetric in mn and in ij: canonical tiles only
@@ -319,6 +324,7 @@ int gbx_cc_job::plan_all() {
   }
   if (sd) {
     GBX_TRY(tensor("t1", "ov"));
+    GBX_TRY(tensor("Dinv1", "ov"));
     GBX_TRY(tensor("R1", "ov"));
     GBX_TRY(tensor("tau", "oovv"));
     GBX_TRY(tensor("taut", "oovv"));
@@ -408,16 +414,15 @@ int gbx_cc_job::plan_all() {
     FBE = "Fbe";
     FMJ = "Fmj";
   }
+  // Terms under the same antisymmetriser share one intermediate, expanded
+  // into R2 once: Xb under P(ab), Xj under P(ij), Xa under P(ij)P(ab).
+  GBX_TRY(zero("Xb"));
+  GBX_TRY(zero("Xj"));
+  GBX_TRY(zero("Xa"));
   // P(ab) t_ij^ae F'_be
-  GBX_TRY(zero("Xa"));
-  GBX_TRY(contract("Xa", "ijab", "t2", "ijae", FBE, "be", 1.0));
-  GBX_TRY(sum("R2", "ijab", "Xa", "ijab", 1.0));
-  GBX_TRY(sum("R2", "ijab", "Xa", "ijba", -1.0));
+  GBX_TRY(contract("Xb", "ijab", "t2", "ijae", FBE, "be", 1.0));
   // -P(ij) t_im^ab F'_mj
-  GBX_TRY(zero("Xa"));
-  GBX_TRY(contract("Xa", "ijab", "t2", "imab", FMJ, "mj", 1.0));
-  GBX_TRY(sum("R2", "ijab", "Xa", "ijab", -1.0));
-  GBX_TRY(sum("R2", "ijab", "Xa", "jiab", 1.0));
+  GBX_TRY(contract("Xj", "ijab", "t2", "imab", FMJ, "mj", -1.0));
   // 1/2 tau_mn^ab W_mnij + 1/2 tau_ij^ef <ab||ef> (the ladder, integrals as
   // the static A operand), on canonical tiles, then into R2
   GBX_TRY(zero("Lad"));
@@ -428,39 +433,31 @@ int gbx_cc_job::plan_all() {
     // -1/2 P(ab) t_m^b sum_ef tau_ij^ef <am||ef> = +1/2 P(ab) sum_m t_m^b Z'_ijma
     GBX_TRY(zero("Zp"));
     GBX_TRY(contract("Zp", "ijma", TAU, "ijef", "OVVV", "maef", 1.0));
-    GBX_TRY(zero("Xa"));
-    GBX_TRY(contract("Xa", "ijab", "Zp", "ijma", "t1", "mb", 1.0));
-    GBX_TRY(sum("R2", "ijab", "Xa", "ijab", 0.5));
-    GBX_TRY(sum("R2", "ijab", "Xa", "ijba", -0.5));
+    GBX_TRY(contract("Xb", "ijab", "Zp", "ijma", "t1", "mb", 0.5));
   }
   // P(ij)P(ab) (t_im^ae W_mbej - t_i^e t_m^a <mb||ej>)
-  GBX_TRY(zero("Xa"));
   GBX_TRY(contract("Xa", "ijab", "t2", "imae", "Wmbej", "mbej", 1.0));
   if (sd) {
     GBX_TRY(zero("V3"));
     GBX_TRY(contract("V3", "imbj", "t1", "ie", "OVVO", "mbej", 1.0));
     GBX_TRY(contract("Xa", "ijab", "t1", "ma", "V3", "imbj", -1.0));
+    // P(ij) t_i^e <ab||ej>
+    GBX_TRY(contract("Xj", "ijab", "t1", "ie", "VVVO", "abej", 1.0));
+    // -P(ab) t_m^a <mb||ij>
+    GBX_TRY(contract("Xb", "ijab", "t1", "ma", "OVOO", "mbij", -1.0));
   }
+  GBX_TRY(sum("R2", "ijab", "Xb", "ijab", 1.0));
+  GBX_TRY(sum("R2", "ijab", "Xb", "ijba", -1.0));
+  GBX_TRY(sum("R2", "ijab", "Xj", "ijab", 1.0));
+  GBX_TRY(sum("R2", "ijab", "Xj", "jiab", -1.0));
   GBX_TRY(sum("R2", "ijab", "Xa", "ijab", 1.0));
   GBX_TRY(sum("R2", "ijab", "Xa", "jiab", -1.0));
   GBX_TRY(sum("R2", "ijab", "Xa", "ijba", -1.0));
   GBX_TRY(sum("R2", "ijab", "Xa", "jiba", 1.0));
-  if (sd) {
-    // P(ij) t_i^e <ab||ej>
-    GBX_TRY(zero("Xa"));
-    GBX_TRY(contract("Xa", "ijab", "t1", "ie", "VVVO", "abej", 1.0));
-    GBX_TRY(sum("R2", "ijab", "Xa", "ijab", 1.0));
-    GBX_TRY(sum("R2", "ijab", "Xa", "jiab", -1.0));
-    // -P(ab) t_m^a <mb||ij>
-    GBX_TRY(zero("Xa"));
-    GBX_TRY(contract("Xa", "ijab", "t1", "ma", "OVOO", "mbij", 1.0));
-    GBX_TRY(sum("R2", "ijab", "Xa", "ijab", -1.0));
-    GBX_TRY(sum("R2", "ijab", "Xa", "ijba", 1.0));
-  }
   // Jacobi update and energy
-  GBX_TRY(denom("t2", "R2", &den2));
+  GBX_TRY(denom("t2", "R2", "Dinv2"));
   if (sd) {
-    GBX_TRY(denom("t1", "R1", &den1));
+    GBX_TRY(denom("t1", "R1", "Dinv1"));
     GBX_TRY(tau_steps());
   }
   GBX_TRY(energy_step());
@@ -497,8 +494,8 @@ int gbx_cc_job::footprint(double* resident, double* peak) const {
   auto tiles_bytes = [](const TensorLayout& L) {
     return up256d((double)L.tiles.size() * sizeof(CCTile)) + up256d(4.0 * (double)(L.tiles.size() + 1));
   };
-  keep += tiles_bytes(T.at("t2")->L);
-  if (T.count("t1")) keep += tiles_bytes(T.at("t1")->L);
+  transient += tiles_bytes(T.at("t2")->L);
+  if (T.count("t1")) transient += tiles_bytes(T.at("t1")->L);
   for (auto& kv : T)
     if (is_integral(kv.first.c_str())) transient += tiles_bytes(kv.second->L);
   keep += up256d(4.0 * n) + up256d(8.0 * n) + up256d(8.0 * (2 * n + 1)) + up256d(8.0 * npartial) +
@@ -581,13 +578,18 @@ int gbx_cc_job::materialize(cudaStream_t st) {
     }
   }
   // MP2 guess t2 = <ij||ab> / D, t1 = 0; tau / taut; energy
-  GBX_TRY(run_cc_tiles(*den2, CC_OP_DENOM, tab, get("OOVV")->d, get("t2")->d, st));
+  GBX_TRY(run_cc_tiles(*den2, CC_OP_INVDENOM, tab, nullptr, get("Dinv2")->d, st));
+  if (sd) GBX_TRY(run_cc_tiles(*den1, CC_OP_INVDENOM, tab, nullptr, get("Dinv1")->d, st));
+  GBX_TRY(run_mul(get("OOVV")->d, get("Dinv2")->d, get("t2")->d, get("t2")->L.nelem, st));
   for (auto& f : init_steps) GBX_TRY(f(st));
   GBX_TRY(gbx::run_energy(get("OOVV")->d, get(sd ? "tau" : "t2")->d, get("OOVV")->L.nelem, d_partial, npartial,
                           d_hist, d_count, hist_cap, st));
   GBX_CUDA(cudaStreamSynchronize(st));
   dev_free(d_scratch);
   once.clear();
+  // the tile sets only served the build
+  tilesets.clear();
+  den1 = den2 = nullptr;
   for (auto& kv : T)
     if (gbx_cc_job_static_only(*this, kv.first)) {
       dev_free(kv.second->d);

@@ -55,7 +55,7 @@ struct CCDeviceTables {
   uint64_t seed_int;
 };
 
-enum { CC_OP_INTEGRAL = 0, CC_OP_DENOM = 1 };
+enum { CC_OP_INTEGRAL = 0, CC_OP_DENOM = 1, CC_OP_INVDENOM = 2 };
 
 struct CCTileSet {
   CCTile* d_tiles = nullptr;
@@ -74,6 +74,8 @@ int run_dot(const double* x, const double* y, int64_t n, double scale, double* p
 
 // E = 1/4 sum V * tau appended to the device history hist[*count++] (fixed
 // summation order, so repeated runs give identical energies).
+// out[i] = a[i] * b[i] over n elements.
+int run_mul(const double* a, const double* b, double* out, int64_t n, cudaStream_t st);
 int run_energy(const double* V, const double* tau, int64_t n, double* partial, int npartial, double* hist, int* count,
                int cap, cudaStream_t st);
 

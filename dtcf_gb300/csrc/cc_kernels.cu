@@ -79,10 +79,16 @@ __global__ void __launch_bounds__(kThreads) cc_tile_kernel(const CCTile* __restr
           double ev = tab.eps[g[d]];
           dnm = (g[d] < tab.nocc) ? __dadd_rn(dnm, ev) : __dsub_rn(dnm, ev);
         }
-        out[o] = __ddiv_rn(in[o], dnm);
+        out[o] = op == CC_OP_DENOM ? __ddiv_rn(in[o], dnm) : __ddiv_rn(1.0, dnm);
       }
     }
   }
+}
+
+__global__ void __launch_bounds__(kThreads) mul_kernel(const double* __restrict__ a, const double* __restrict__ b,
+                                                       double* __restrict__ out, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kThreads)
+    out[i] = __dmul_rn(a[i], b[i]);
 }
 
 // Per-CTA partial sums of x*y over n elements, in a fixed order.
@@ -157,6 +163,14 @@ void CCTileSet::release() {
   d_first = nullptr;
   ntiles = 0;
   nchunks = 0;
+}
+
+int run_mul(const double* a, const double* b, double* out, int64_t n, cudaStream_t st) {
+  if (n <= 0) return GBX_OK;
+  const int grid = (int)std::min<int64_t>((n + kThreads - 1) / kThreads, 152 * 16);
+  mul_kernel<<<grid, kThreads, 0, st>>>(a, b, out, n);
+  GBX_CUDA(cudaGetLastError());
+  return GBX_OK;
 }
 
 int run_cc_tiles(const CCTileSet& ts, int op, const CCDeviceTables& tab, const double* in, double* out,
