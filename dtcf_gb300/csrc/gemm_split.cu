@@ -689,12 +689,15 @@ struct KsSmem {
   uint32_t tmem_base;
 };
 
+// S is a template parameter so that the slice-pair loops of the MMA issuer
+// (one thread issuing every tcgen05.mma) unroll completely.
+template <int S>
 __global__ void __launch_bounds__(kKsThreads, 1) split_ks_kernel(const GemmParams P) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   KsSmem& sm = *reinterpret_cast<KsSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int S = P.S, L = P.L;
-  const int D = 16 / S;  // k-blocks per exact accumulation group
+  constexpr int L = S - 1;
+  constexpr int D = 16 / S;  // k-blocks per exact accumulation group
   constexpr uint32_t kTx = (BM + kKsBN) * BK * 2;
   constexpr uint32_t kCols = 512;
   if (threadIdx.x == 0) {
@@ -766,6 +769,10 @@ __global__ void __launch_bounds__(kKsThreads, 1) split_ks_kernel(const GemmParam
       uint32_t phase = 0, aphase = 0;
       bool ok = true;
       constexpr uint32_t idesc = idesc_bf16<kKsBN>();
+      // slot descriptors: slot 0's plus the slot offset in 16-byte units
+      // (the address field holds shared-memory address / 16, below 2^14)
+      const uint64_t ad0 = sdesc(smem_u32(sm.a[0])), bd0 = sdesc(smem_u32(sm.b[0]));
+      constexpr uint64_t kAStep = (uint64_t)(BM * BK * 2) >> 4, kBStep = (uint64_t)(kKsBN * BK * 2) >> 4;
       for (int tile = blockIdx.x; tile < P.total_tiles && ok; tile += gridDim.x) {
         const int nkb = decode_tile<kKsBN>(P, tile).nkb;
         for (int g0 = 0; g0 < nkb && ok; g0 += D) {
@@ -776,7 +783,8 @@ __global__ void __launch_bounds__(kKsThreads, 1) split_ks_kernel(const GemmParam
           tc_fence_after();
           const int g1 = min(nkb, g0 + D);
           for (int kb = g0; kb < g1 && ok; ++kb) {
-            int sl[kKsMaxS];
+            int sl[S];
+#pragma unroll
             for (int s = 0; s < S; ++s) {
               sl[s] = slot;
               if (!mbar_wait(&sm.full[slot], phase, P.err, 23)) {
@@ -790,20 +798,22 @@ __global__ void __launch_bounds__(kKsThreads, 1) split_ks_kernel(const GemmParam
             }
             if (!ok) break;
             tc_fence_after();
+            const uint32_t fresh = kb == g0 ? 0u : 1u;
+#pragma unroll
             for (int l = 0; l <= L; ++l) {
               const uint32_t d = tmem + (uint32_t)buf * buf_cols + (uint32_t)(l * kKsBN);
-              bool first = kb == g0;
-              for (int s = max(1, l + 2 - S); s <= min(S, l + 1); ++s) {
-                const int t = l + 2 - s;
-                const uint64_t a0 = sdesc(smem_u32(sm.a[sl[s - 1]]));
-                const uint64_t b0 = sdesc(smem_u32(sm.b[sl[t - 1]]));
 #pragma unroll
-                for (int k = 0; k < BK / 16; ++k) {
-                  umma(d, a0 + (uint64_t)(k * 2), b0 + (uint64_t)(k * 2), idesc, first ? 0u : 1u);
-                  first = false;
-                }
+              for (int s = (l + 2 - S > 1 ? l + 2 - S : 1); s <= (S < l + 1 ? S : l + 1); ++s) {
+                const int t = l + 2 - s;
+                const uint64_t a0 = ad0 + (uint64_t)sl[s - 1] * kAStep;
+                const uint64_t b0 = bd0 + (uint64_t)sl[t - 1] * kBStep;
+                const bool lead = s == (l + 2 - S > 1 ? l + 2 - S : 1);  // first product of the level
+#pragma unroll
+                for (int k = 0; k < BK / 16; ++k)
+                  umma(d, a0 + (uint64_t)(k * 2), b0 + (uint64_t)(k * 2), idesc, (lead && k == 0) ? fresh : 1u);
               }
             }
+#pragma unroll
             for (int s = 0; s < S; ++s) umma_commit(&sm.empty[sl[s]]);
           }
           if (!ok) break;
@@ -1416,7 +1426,11 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
   GBX_TRY(set_smem_attr<64>());
   GBX_TRY(set_smem_attr<128>());
   GBX_TRY(set_smem_attr<256>());
-  GBX_CUDA(cudaFuncSetAttribute(split_ks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  GBX_CUDA(cudaFuncSetAttribute(split_ks_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(sizeof(KsSmem) + 1024)));
+  GBX_CUDA(cudaFuncSetAttribute(split_ks_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(sizeof(KsSmem) + 1024)));
+  GBX_CUDA(cudaFuncSetAttribute(split_ks_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)(sizeof(KsSmem) + 1024)));
   GBX_CUDA(cudaFuncSetAttribute(split_thin_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)(sizeof(ThinSmem) + 1024)));
@@ -1503,7 +1517,11 @@ int run_split_plan(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st) {
           P.S = sp->S;
           P.L = sp->L;
           P.err = sp->d_err;
-          split_ks_kernel<<<std::min(L.total_tiles, nsm), kKsThreads, sizeof(KsSmem) + 1024, st>>>(P);
+          const int g = std::min(L.total_tiles, nsm);
+          const size_t sh = sizeof(KsSmem) + 1024;
+          if (sp->S == 2) split_ks_kernel<2><<<g, kKsThreads, sh, st>>>(P);
+          else if (sp->S == 3) split_ks_kernel<3><<<g, kKsThreads, sh, st>>>(P);
+          else split_ks_kernel<4><<<g, kKsThreads, sh, st>>>(P);
           GBX_CUDA(cudaGetLastError());
         } else {
           GBX_TRY(launch_width<64>(sp, L, nsm, st));
