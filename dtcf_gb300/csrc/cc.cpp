@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <set>
 
@@ -85,10 +86,16 @@ struct gbx_cc_job {
   std::map<std::string, std::unique_ptr<CCTensor>> T;
   std::vector<std::unique_ptr<ContractionPlan>> cplans;
   std::vector<std::unique_ptr<SumPlan>> splans;
+  std::vector<std::unique_ptr<FusedSumPlan>> fplans;
+  // tau / taut / Q from t2 and t1 (CCSD): per-tile t1 offsets and work items
+  std::vector<CCAmpTile> amp_tiles;
+  std::vector<CCAmpItem> amp_items;
+  CCAmpSet amp;
   std::vector<std::function<int(cudaStream_t)>> steps;       // one iteration
   std::vector<std::function<int(cudaStream_t)>> init_steps;  // once, after the MP2 guess
   std::set<std::string> dynamic_use;  // tensors read or written outside constant plan operands
   std::vector<std::pair<CCTensor*, CCTensor*>> plan_operands;  // A, B of each contraction plan
+  std::vector<CCTensor*> plan_outputs;                         // C of each contraction plan
   unsigned char* d_arena = nullptr;  // packed operands and split slices, shared by every plan
   size_t arena_bytes = 0;
   std::atomic<int64_t> account{0};  // device bytes the job's allocations hold
@@ -118,6 +125,8 @@ struct gbx_cc_job {
     if (graph) cudaGraphDestroy(graph);
     cplans.clear();
     splans.clear();
+    fplans.clear();
+    amp.release();
     T.clear();
     tilesets.clear();
     dev_free(d_arena);
@@ -183,8 +192,9 @@ struct gbx_cc_job {
     GBX_TRY(plan_contraction(A->L, B->L, C->L, labels(la), labels(lb), labels(lc), e, cfg.slices, p,
                              cfg.split_all != 0, /*defer=*/true));
     // integrals never change: packed and split once, when the job is built
-    p->a_static = is_integral(a);
-    p->b_static = is_integral(b);
+    // (a direct plan reads them where they are stored, so they stay resident)
+    p->a_static = is_integral(a) && !p->direct;
+    p->b_static = is_integral(b) && !p->direct;
     if (!p->a_static) dynamic_use.insert(a);
     if (!p->b_static) dynamic_use.insert(b);
     dynamic_use.insert(c);
@@ -194,9 +204,10 @@ struct gbx_cc_job {
     steps.push_back([=](cudaStream_t st) { return pp->execute(A->d, B->d, C->d, alpha, st); });
     info.push_back({std::string(c) + "[" + lc + "]+=" + a + "[" + la + "]*" + b + "[" + lb + "]", 0, pp->flops,
                     8.0 * (double)(A->L.nelem + B->L.nelem + 2 * C->L.nelem), (int)cplans.size()});
-    launches += 4;
+    launches += pp->direct ? 1 : 4;
     cplans.push_back(std::move(p));
     plan_operands.push_back({A, B});
+    plan_outputs.push_back(C);
     return GBX_OK;
   }
 
@@ -215,6 +226,99 @@ struct gbx_cc_job {
                     8.0 * (double)(A->L.nelem + 2 * C->L.nelem)});
     launches += 1;
     splans.push_back(std::move(p));
+    return GBX_OK;
+  }
+
+  // out[lc] = (sum of coef * A[la] over the terms, in order) [* scale]: one
+  // pass that replaces zeroing out and running the terms as separate sums
+  struct Term {
+    const char* a;
+    const char* la;
+    double coef;
+  };
+  int fused(const char* out, const char* lc, const std::vector<Term>& terms, const char* scale = nullptr) {
+    CCTensor* C = get(out);
+    GBX_TRY(check_labels(C, lc, out));
+    std::vector<FusedTermSpec> specs;
+    std::vector<CCTensor*> src;
+    std::string name = std::string(out) + "[" + lc + "]=";
+    double bytes = 8.0 * (double)C->L.nelem;
+    for (const Term& t : terms) {
+      CCTensor* A = get(t.a);
+      GBX_TRY(check_labels(A, t.la, t.a));
+      int slot = -1;
+      for (size_t i = 0; i < src.size(); ++i)
+        if (src[i] == A) slot = (int)i;
+      if (slot < 0) {
+        slot = (int)src.size();
+        src.push_back(A);
+        bytes += 8.0 * (double)A->L.nelem;
+      }
+      if (slot >= kFsMaxSlots) return fail(GBX_EUNSUPPORTED, "fused sum: too many sources");
+      specs.push_back({&A->L, labels(t.la), t.coef, slot});
+      dynamic_use.insert(t.a);
+      char buf[64];
+      std::snprintf(buf, sizeof buf, "%s%s%s[%s]", &t == &terms[0] ? "" : (t.coef < 0 ? "-" : "+"),
+                    (t.coef == 1.0 || t.coef == -1.0) ? "" : (std::to_string(std::fabs(t.coef)).substr(0, 4) + "*").c_str(),
+                    t.a, t.la);
+      name += buf;
+    }
+    CCTensor* S = scale ? get(scale) : nullptr;
+    if (S) {
+      if (S->L.nelem != C->L.nelem) return fail(GBX_EINVAL, "fused sum: scale layout differs");
+      name += std::string(" *") + scale;
+      bytes += 8.0 * (double)S->L.nelem;
+      dynamic_use.insert(scale);
+    }
+    dynamic_use.insert(out);
+    std::unique_ptr<FusedSumPlan> p;
+    GBX_TRY(plan_fused_sum(C->L, labels(lc), specs, p));
+    FusedSumPlan* pp = p.get();
+    steps.push_back([=](cudaStream_t st) {
+      const double* ptr[kFsMaxSlots] = {};
+      for (size_t i = 0; i < src.size(); ++i) ptr[i] = src[i]->d;
+      return pp->execute(ptr, S ? S->d : nullptr, C->d, st);
+    });
+    info.push_back({name, 1, 0.0, bytes});
+    launches += 1;
+    fplans.push_back(std::move(p));
+    return GBX_OK;
+  }
+
+  // tau, taut and Q from t2 and t1 (CCSD), one pass over t2's tiles
+  int amp_step() {
+    CCTensor *t2 = get("t2"), *t1 = get("t1"), *tau = get("tau"), *taut = get("taut"), *Q = get("Q");
+    for (CCTensor* x : {tau, taut, Q})
+      if (x->L.tiles != t2->L.tiles) return fail(GBX_EINVAL, "tau family: layout differs from t2");
+    if (amp_tiles.empty()) {
+      const TensorLayout& L = t2->L;
+      for (size_t t = 0; t < L.tiles.size(); ++t) {
+        const Coords& c = L.tiles[t];
+        CCAmpTile at;
+        std::memset(&at, 0, sizeof(at));
+        at.off = L.off[t];
+        const int pairs[4][2] = {{c[0], c[2]}, {c[1], c[3]}, {c[0], c[3]}, {c[1], c[2]}};
+        for (int k = 0; k < 4; ++k) {
+          const int cc2[2] = {pairs[k][0], pairs[k][1]};
+          const int id = t1->L.find(cc2);
+          at.t1[k] = id < 0 ? -1 : t1->L.off[id];
+        }
+        const int64_t ei = L.dims[0]->ext[c[0]], ej = L.dims[1]->ext[c[1]], ea = L.dims[2]->ext[c[2]],
+                      eb = L.dims[3]->ext[c[3]];
+        at.fj = FastDiv::make((uint32_t)ej);
+        at.fa = FastDiv::make((uint32_t)ea);
+        at.fb = FastDiv::make((uint32_t)eb);
+        const int64_t n = ei * ej * ea * eb;
+        if (n >= ((int64_t)1 << 31)) return fail(GBX_EUNSUPPORTED, "amplitude tile too large");
+        for (int64_t f0 = 0; f0 < n; f0 += 2048)
+          amp_items.push_back({(uint32_t)t, (uint32_t)f0, (uint32_t)std::min<int64_t>(2048, n - f0), 0u});
+        amp_tiles.push_back(at);
+      }
+    }
+    for (const char* nm : {"t2", "t1", "tau", "taut", "Q"}) dynamic_use.insert(nm);
+    steps.push_back([=](cudaStream_t st) { return run_cc_amp(amp, t1->d, t2->d, tau->d, taut->d, Q->d, st); });
+    info.push_back({"tau,taut,Q[ijab]=t2+t1*t1", 1, 0.0, 32.0 * (double)t2->L.nelem});
+    launches += 1;
     return GBX_OK;
   }
 
@@ -285,25 +389,15 @@ struct gbx_cc_job {
   int tau_steps();
 };
 
-// tau = t2 + t1 t1 - t1 t1 (i<->j), taut = t2 + (t1 t1 - t1 t1) / 2
-int gbx_cc_job::tau_steps() {
-  GBX_TRY(zero("tau"));
-  GBX_TRY(sum("tau", "ijab", "t2", "ijab", 1.0));
-  GBX_TRY(contract("tau", "ijab", "t1", "ia", "t1", "jb", 1.0));
-  GBX_TRY(contract("tau", "ijab", "t1", "ib", "t1", "ja", -1.0));
-  GBX_TRY(zero("taut"));
-  GBX_TRY(sum("taut", "ijab", "t2", "ijab", 1.0));
-  GBX_TRY(contract("taut", "ijab", "t1", "ia", "t1", "jb", 0.5));
-  GBX_TRY(contract("taut", "ijab", "t1", "ib", "t1", "ja", -0.5));
-  return GBX_OK;
-}
+// tau = t2 + t1 t1 - t1 t1 (i<->j), taut = t2 + (t1 t1 - t1 t1) / 2 and
+// Q = t2 / 2 + t1 t1, all from the current t1 and t2 (CCSD)
+int gbx_cc_job::tau_steps() { return amp_step(); }
 
 int gbx_cc_job::plan_all() {
   const bool sd = cfg.method == GBX_CC_CCSD;
   // amplitudes, residuals, intermediates
   GBX_TRY(tensor("t2", "oovv"));
   GBX_TRY(tensor("Dinv2", "oovv"));  // 1 / (e_i + e_j - e_a - e_b)
-  GBX_TRY(tensor("R2", "oovv"));
   GBX_TRY(tensor("Xa", "oovv"));
   GBX_TRY(tensor("Xb", "oovv"));
   GBX_TRY(tensor("Xj", "oovv"));
@@ -356,7 +450,8 @@ int gbx_cc_job::plan_all() {
   iter_plan_begin = (int)cplans.size();
 
   // ---- one iteration --------------------------------------------------------
-  if (sd) GBX_TRY(tau_steps());
+  // (tau, taut and Q of the current amplitudes exist: formed at the end of
+  // the previous iteration, by the initial guess or by set_amplitudes)
   // F_ae, F_mi, F_me
   GBX_TRY(zero("Fae"));
   if (sd) GBX_TRY(contract("Fae", "ae", "t1", "mf", "OVVV", "mafe", 1.0));
@@ -369,25 +464,22 @@ int gbx_cc_job::plan_all() {
     GBX_TRY(contract("Fme", "me", "t1", "nf", "OOVV", "mnef", 1.0));
   }
   // W_mnij (with the ladder's 1/8 tau <mn||ef> tau term folded in: 1/2 instead of 1/4)
-  GBX_TRY(zero("Wmnij"));
-  GBX_TRY(sum("Wmnij", "mnij", "OOOO", "mnij", 1.0));
   if (sd) {
     GBX_TRY(zero("Xoooo"));
     GBX_TRY(contract("Xoooo", "mnij", "t1", "je", "OOOV", "mnie", 1.0));
-    GBX_TRY(sum("Wmnij", "mnij", "Xoooo", "mnij", 1.0));
-    GBX_TRY(sum("Wmnij", "mnij", "Xoooo", "mnji", -1.0));
+    GBX_TRY(fused("Wmnij", "mnij", {{"OOOO", "mnij", 1.0}, {"Xoooo", "mnij", 1.0}, {"Xoooo", "mnji", -1.0}}));
+  } else {
+    GBX_TRY(fused("Wmnij", "mnij", {{"OOOO", "mnij", 1.0}}));
   }
   GBX_TRY(contract("Wmnij", "mnij", TAU, "ijef", "OOVV", "mnef", 0.5));
   // W_mbej
-  GBX_TRY(zero("Wmbej"));
-  GBX_TRY(sum("Wmbej", "mbej", "OVVO", "mbej", 1.0));
+  GBX_TRY(fused("Wmbej", "mbej", {{"OVVO", "mbej", 1.0}}));
   if (sd) {
     GBX_TRY(contract("Wmbej", "mbej", "t1", "jf", "OVVV", "mbef", 1.0));
     GBX_TRY(contract("Wmbej", "mbej", "t1", "nb", "OOVO", "mnej", -1.0));
   }
-  GBX_TRY(zero("Q"));
-  GBX_TRY(sum("Q", "jnfb", "t2", "jnfb", 0.5));
-  if (sd) GBX_TRY(contract("Q", "jnfb", "t1", "jf", "t1", "nb", 1.0));
+  // Q = t2 / 2 (+ t1 t1, formed with tau at the end of the previous iteration for CCSD)
+  if (!sd) GBX_TRY(fused("Q", "jnfb", {{"t2", "jnfb", 0.5}}));
   GBX_TRY(contract("Wmbej", "mbej", "Q", "jnfb", "OOVV", "mnef", -1.0));
   // T1 residual
   if (sd) {
@@ -400,16 +492,12 @@ int gbx_cc_job::plan_all() {
     GBX_TRY(contract("R1", "ia", "t2", "mnae", "OOVO", "nmei", -0.5));
   }
   // T2 residual
-  GBX_TRY(zero("R2"));
-  GBX_TRY(sum("R2", "ijab", "OOVV", "ijab", 1.0));
   const char* FBE = "Fae";
   const char* FMJ = "Fmi";
   if (sd) {
-    GBX_TRY(zero("Fbe"));
-    GBX_TRY(sum("Fbe", "be", "Fae", "be", 1.0));
+    GBX_TRY(fused("Fbe", "be", {{"Fae", "be", 1.0}}));
     GBX_TRY(contract("Fbe", "be", "t1", "mb", "Fme", "me", -0.5));
-    GBX_TRY(zero("Fmj"));
-    GBX_TRY(sum("Fmj", "mj", "Fmi", "mj", 1.0));
+    GBX_TRY(fused("Fmj", "mj", {{"Fmi", "mj", 1.0}}));
     GBX_TRY(contract("Fmj", "mj", "t1", "je", "Fme", "me", 0.5));
     FBE = "Fbe";
     FMJ = "Fmj";
@@ -428,7 +516,6 @@ int gbx_cc_job::plan_all() {
   GBX_TRY(zero("Lad"));
   GBX_TRY(contract("Lad", "ijab", TAU, "mnab", "Wmnij", "mnij", 0.5));
   GBX_TRY(contract("Lad", "ijab", "VVVV", "abef", TAU, "ijef", 0.5));
-  GBX_TRY(sum("R2", "ijab", "Lad", "ijab", 1.0));
   if (sd) {
     // -1/2 P(ab) t_m^b sum_ef tau_ij^ef <am||ef> = +1/2 P(ab) sum_m t_m^b Z'_ijma
     GBX_TRY(zero("Zp"));
@@ -446,16 +533,14 @@ int gbx_cc_job::plan_all() {
     // -P(ab) t_m^a <mb||ij>
     GBX_TRY(contract("Xb", "ijab", "t1", "ma", "OVOO", "mbij", -1.0));
   }
-  GBX_TRY(sum("R2", "ijab", "Xb", "ijab", 1.0));
-  GBX_TRY(sum("R2", "ijab", "Xb", "ijba", -1.0));
-  GBX_TRY(sum("R2", "ijab", "Xj", "ijab", 1.0));
-  GBX_TRY(sum("R2", "ijab", "Xj", "jiab", -1.0));
-  GBX_TRY(sum("R2", "ijab", "Xa", "ijab", 1.0));
-  GBX_TRY(sum("R2", "ijab", "Xa", "jiab", -1.0));
-  GBX_TRY(sum("R2", "ijab", "Xa", "ijba", -1.0));
-  GBX_TRY(sum("R2", "ijab", "Xa", "jiba", 1.0));
-  // Jacobi update and energy
-  GBX_TRY(denom("t2", "R2", "Dinv2"));
+  // Jacobi update of T2: the residual R2 = <ij||ab> + ladder + the three
+  // antisymmetrised intermediates, times 1 / D, in one pass (R2 itself is
+  // never stored); then T1, the tau family and the energy
+  GBX_TRY(fused("t2", "ijab",
+                {{"OOVV", "ijab", 1.0}, {"Lad", "ijab", 1.0}, {"Xb", "ijab", 1.0}, {"Xb", "ijba", -1.0},
+                 {"Xj", "ijab", 1.0}, {"Xj", "jiab", -1.0}, {"Xa", "ijab", 1.0}, {"Xa", "jiab", -1.0},
+                 {"Xa", "ijba", -1.0}, {"Xa", "jiba", 1.0}},
+                "Dinv2"));
   if (sd) {
     GBX_TRY(denom("t1", "R1", "Dinv1"));
     GBX_TRY(tau_steps());
@@ -491,6 +576,8 @@ int gbx_cc_job::footprint(double* resident, double* peak) const {
   }
   for (auto& p : splans)
     keep += (double)(p->moves.host.size() * sizeof(MoveDesc) + (p->moves.host.size() + 1) * sizeof(uint32_t));
+  for (auto& p : fplans) keep += up256d((double)(p->items.size() * sizeof(FsItem))) + up256d((double)(p->terms.size() * sizeof(FsTerm)));
+  keep += up256d((double)(amp_tiles.size() * sizeof(CCAmpTile))) + up256d((double)(amp_items.size() * sizeof(CCAmpItem)));
   auto tiles_bytes = [](const TensorLayout& L) {
     return up256d((double)L.tiles.size() * sizeof(CCTile)) + up256d(4.0 * (double)(L.tiles.size() + 1));
   };
@@ -565,6 +652,8 @@ int gbx_cc_job::materialize(cudaStream_t st) {
   unsigned char* d_scratch = nullptr;
   if (scratch_bytes) GBX_TRY(dev_alloc((void**)&d_scratch, scratch_bytes));
   for (auto& p : splans) GBX_TRY(p->moves.upload());
+  for (auto& p : fplans) GBX_TRY(p->upload());
+  if (!amp_items.empty()) GBX_TRY(amp.upload(amp_tiles, amp_items));
   for (size_t i = 0; i < cplans.size(); ++i) {
     ContractionPlan* p = cplans[i].get();
     int rc = p->build(d_arena, d_scratch);
@@ -843,6 +932,10 @@ int gbx_cc_set_amplitudes(gbx_cc_job* job, const double* t1, const double* t2, v
   if (t1 && job->T.count("t1"))
     GBX_CUDA(cudaMemcpyAsync(job->get("t1")->d, t1, sizeof(double) * job->get("t1")->L.nelem, cudaMemcpyHostToDevice,
                              st));
+  // the iteration reads tau, taut and Q of these amplitudes
+  if (job->T.count("t1"))
+    GBX_TRY(run_cc_amp(job->amp, job->get("t1")->d, job->get("t2")->d, job->get("tau")->d, job->get("taut")->d,
+                       job->get("Q")->d, st));
   return GBX_OK;
 }
 
@@ -907,10 +1000,18 @@ int gbx_cc_time_gemm(gbx_cc_job* job, int contraction, int reps, float* ms, doub
   GBX_CUDA(cudaEventCreate(&e0));
   GBX_CUDA(cudaEventCreate(&e1));
   // the arena is shared by every plan: pack and split this plan's operands
-  // again, then time only the GEMM launches
-  GBX_TRY(p->stage(job->plan_operands[contraction].first->d, job->plan_operands[contraction].second->d, st));
+  // again, then time only the GEMM launches (a direct plan: its one launch
+  // with alpha = 0, which leaves C as it is)
+  const double* dA = job->plan_operands[contraction].first->d;
+  const double* dB = job->plan_operands[contraction].second->d;
+  double* dC = job->plan_outputs[contraction]->d;
+  GBX_TRY(p->stage(dA, dB, st));
   GBX_CUDA(cudaEventRecord(e0, st));
   for (int r = 0; r < reps; ++r) {
+    if (p->direct) {
+      GBX_TRY(p->execute(dA, dB, dC, 0.0, st));
+      continue;
+    }
     if (p->split) GBX_TRY(run_split_plan(p->split, false, false, st));
     GBX_TRY(p->f64.run(st));
   }
@@ -921,9 +1022,9 @@ int gbx_cc_time_gemm(gbx_cc_job* job, int contraction, int reps, float* ms, doub
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (ms) *ms = t / reps;
-  if (fp64_flops) *fp64_flops = p->gemm_flops;
+  if (fp64_flops) *fp64_flops = p->direct ? p->flops : p->gemm_flops;
   if (tensor_flops) *tensor_flops = split_plan_tensor_flops(p->split);
-  if (engine) *engine = p->split ? (p->f64.nprob ? 2 : 1) : 0;
+  if (engine) *engine = p->direct ? 3 : p->split ? (p->f64.nprob ? 2 : 1) : 0;
   return GBX_OK;
 }
 

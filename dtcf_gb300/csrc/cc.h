@@ -69,6 +69,34 @@ struct CCTileSet {
 
 int run_cc_tiles(const CCTileSet& ts, int op, const CCDeviceTables& tab, const double* in, double* out,
                  cudaStream_t st);
+
+// The amplitude combinations of one CCSD iteration that need no contraction,
+// formed in one pass over t2 (each from the t2 and t1 of the same iteration):
+//   tau  = t2 + t1_ia t1_jb - t1_ib t1_ja
+//   taut = t2 + (t1_ia t1_jb - t1_ib t1_ja) / 2
+//   Q    = t2 / 2 + t1_ia t1_jb            (Q_jn^fb of W_mbej)
+// element by element as 0 + t2, then each present product added with its
+// coefficient, products and sums separately rounded.  A product is present
+// when both t1 tiles are stored (irrep of i equals that of a, and so on).
+struct CCAmpTile {
+  int64_t off;    // tile offset in t2, tau, taut and Q (one layout)
+  int64_t t1[4];  // t1 tiles (i,a), (j,b), (i,b), (j,a); -1 when not stored
+  FastDiv fj, fa, fb;
+};
+struct CCAmpItem {
+  uint32_t tile, f0, n, pad;  // elements [f0, f0 + n) of one tile
+};
+struct CCAmpSet {
+  CCAmpTile* d_tiles = nullptr;
+  CCAmpItem* d_items = nullptr;
+  int nitems = 0;
+  size_t bytes = 0;
+  int upload(const std::vector<CCAmpTile>& tiles, const std::vector<CCAmpItem>& items);
+  void release();
+  ~CCAmpSet() { release(); }
+};
+int run_cc_amp(const CCAmpSet& s, const double* t1, const double* t2, double* tau, double* taut, double* Q,
+               cudaStream_t st);
 int run_dot(const double* x, const double* y, int64_t n, double scale, double* partial, int npartial, double* out,
             cudaStream_t st);
 

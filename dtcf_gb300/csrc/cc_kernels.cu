@@ -1,6 +1,7 @@
 // Element-wise kernels of the coupled-cluster driver: synthetic integral
-// generation, orbital-energy denominators (MP2 guess, Jacobi update) and the
-// deterministic FP64 dot product behind the correlation energy.
+// generation, orbital-energy denominators (MP2 guess, Jacobi update), the
+// amplitude combinations tau / taut / Q and the deterministic FP64 dot
+// product behind the correlation energy.
 //
 // All of them walk a list of tiles; a tile carries its element offset, rank,
 // extents and the global orbital index of the first orbital of each block.
@@ -163,6 +164,88 @@ void CCTileSet::release() {
   d_first = nullptr;
   ntiles = 0;
   nchunks = 0;
+}
+
+__global__ void __launch_bounds__(kThreads) cc_amp_kernel(const CCAmpTile* __restrict__ tiles,
+                                                         const CCAmpItem* __restrict__ items, int nitems,
+                                                         const double* __restrict__ t1,
+                                                         const double* __restrict__ t2, double* __restrict__ tau,
+                                                         double* __restrict__ taut, double* __restrict__ Q) {
+  constexpr int kPer = kChunk / kThreads;
+  for (int i = blockIdx.x; i < nitems; i += gridDim.x) {
+    const CCAmpItem it = items[i];
+    const CCAmpTile& tl = tiles[it.tile];
+    const uint32_t ej = tl.fj.d, ea = tl.fa.d, eb = tl.fb.d;
+    const int64_t o_ia = tl.t1[0], o_jb = tl.t1[1], o_ib = tl.t1[2], o_ja = tl.t1[3];
+    const bool h1 = o_ia >= 0 && o_jb >= 0, h2 = o_ib >= 0 && o_ja >= 0;
+    double x[kPer], p1[kPer], p2[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+      const uint32_t e = min((uint32_t)(threadIdx.x + k * kThreads), it.n - 1);
+      const uint32_t f = it.f0 + e;
+      const uint32_t r1 = tl.fb.div(f), b = f - r1 * eb;
+      const uint32_t r2 = tl.fa.div(r1), a = r1 - r2 * ea;
+      const uint32_t ii = tl.fj.div(r2), j = r2 - ii * ej;
+      x[k] = __ldg(t2 + tl.off + f);
+      p1[k] = h1 ? __dmul_rn(__ldg(t1 + o_ia + (int64_t)ii * ea + a), __ldg(t1 + o_jb + (int64_t)j * eb + b)) : 0.0;
+      p2[k] = h2 ? __dmul_rn(__ldg(t1 + o_ib + (int64_t)ii * eb + b), __ldg(t1 + o_ja + (int64_t)j * ea + a)) : 0.0;
+    }
+    // seven FP64 instructions per element (the FP64 pipe, not HBM, bounds
+    // element-wise FP64 work on this part): the products p1, p2; tau as
+    // (t2 + p1) - p2; taut and Q with fused multiply-adds by 1/2 -- each the
+    // separately rounded product and sum, 0.5 x being exact
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+      const uint32_t e = threadIdx.x + k * kThreads;
+      if (e >= it.n) continue;
+      const int64_t at = tl.off + it.f0 + e;
+      // 0 + t2 (turns -0 into +0) on the bits
+      const unsigned long long xb = (unsigned long long)__double_as_longlong(x[k]);
+      const double x0 = __longlong_as_double((long long)(xb == 0x8000000000000000ull ? 0ull : xb));
+      double a1 = x0, a2 = x0;
+      double q = __fma_rn(0.5, x[k], h1 ? p1[k] : 0.0);
+      if (h1) {
+        a1 = __dadd_rn(a1, p1[k]);
+        a2 = __fma_rn(0.5, p1[k], a2);
+      }
+      if (h2) {
+        a1 = __dsub_rn(a1, p2[k]);
+        a2 = __fma_rn(-0.5, p2[k], a2);
+      }
+      tau[at] = a1;
+      taut[at] = a2;
+      Q[at] = q;
+    }
+  }
+}
+
+int CCAmpSet::upload(const std::vector<CCAmpTile>& tiles, const std::vector<CCAmpItem>& items) {
+  release();
+  nitems = (int)items.size();
+  if (!nitems) return GBX_OK;
+  GBX_TRY(dev_alloc((void**)&d_tiles, sizeof(CCAmpTile) * tiles.size()));
+  GBX_TRY(dev_alloc((void**)&d_items, sizeof(CCAmpItem) * items.size()));
+  GBX_CUDA(cudaMemcpy(d_tiles, tiles.data(), sizeof(CCAmpTile) * tiles.size(), cudaMemcpyHostToDevice));
+  GBX_CUDA(cudaMemcpy(d_items, items.data(), sizeof(CCAmpItem) * items.size(), cudaMemcpyHostToDevice));
+  bytes = sizeof(CCAmpTile) * tiles.size() + sizeof(CCAmpItem) * items.size();
+  return GBX_OK;
+}
+
+void CCAmpSet::release() {
+  dev_free(d_tiles);
+  dev_free(d_items);
+  d_tiles = nullptr;
+  d_items = nullptr;
+  nitems = 0;
+}
+
+int run_cc_amp(const CCAmpSet& s, const double* t1, const double* t2, double* tau, double* taut, double* Q,
+               cudaStream_t st) {
+  if (s.nitems == 0) return GBX_OK;
+  const int grid = std::min(s.nitems, 152 * 8);
+  cc_amp_kernel<<<grid, kThreads, 0, st>>>(s.d_tiles, s.d_items, s.nitems, t1, t2, tau, taut, Q);
+  GBX_CUDA(cudaGetLastError());
+  return GBX_OK;
 }
 
 int run_mul(const double* a, const double* b, double* out, int64_t n, cudaStream_t st) {

@@ -55,9 +55,12 @@ struct FastDiv {
 
 // One strided tile move: for every index tuple idx over ext[0..rank-1],
 //   dst[dst + sum idx_d * dstr_d]  (op)=  scale * src[src + sum idx_d * sstr_d]
-// op 0 stores (a plain copy when scale == 1, bit-exact), op 1 accumulates with
-// a separately rounded multiply and add, dst + (scale * x).  The host orders
-// the dimensions so that the last one has the smallest destination stride.
+// op 0 stores (a plain copy when scale == 1, bit-exact), op 1 accumulates
+// dst + scale * x with one fused multiply-add: the separately rounded product
+// and sum whenever scale * x is exact (scale = +-2^k), one FP64 instruction
+// instead of two (the FP64 pipe, not HBM, bounds element-wise FP64 work on
+// this part).  The host orders the dimensions so that the last one has the
+// smallest destination stride.
 struct MoveDesc {
   int64_t src, dst;
   int64_t sstr[kMaxDims];
@@ -93,6 +96,75 @@ struct MoveSet {
 // scale * alpha.
 int run_moves(const MoveSet& ms, const double* src, double* dst, cudaStream_t st);
 int run_moves_scaled(const MoveSet& ms, const double* src, double* dst, double alpha, cudaStream_t st);
+
+// Fused permuted sum over one destination layout of rank 2..4: every
+// destination element is formed in one pass as
+//   out = (0 + coef_0 * x_0 + coef_1 * x_1 + ...) [* scale]
+// in term order, each term added with one fused multiply-add (the separately
+// rounded product and sum whenever coef * x is exact, as for coef = +-2^k),
+// x_t the element of source term t under that term's permutation.  A destination tile is walked
+// as rows of slabs: a slab is its last two dimensions (extents ea x eb,
+// contiguous), a row the slabs of one index o0 of its first dimension.
+constexpr int kFsMaxSlots = 8;     // distinct source buffers of one plan
+constexpr int kFsMaxTerms = 16;    // terms of one plan
+constexpr int kFsItemElems = 2048; // destination elements per work item
+
+// One (destination tile, term) pair.
+struct FsTerm {
+  int64_t off;       // source offset of the destination tile's first element
+  int64_t so0, so1;  // source strides of the destination's two outer dimensions
+  int64_t sa, sb;    // source strides of the slab dimensions
+  double coef;       // coefficient with the layout's sign factor
+  int32_t slot;      // source buffer
+  int32_t mode;      // 0 slabs contiguous in order, 1 slabs contiguous transposed, 2 gather
+};
+
+// A run of destination elements inside one row of one tile.
+struct FsItem {
+  int64_t dst;          // destination (and scale) offset of the first element
+  FastDiv fE, fea, feb; // slab size ea * eb and the slab extents
+  uint32_t f0;          // index of the first element within the row
+  uint32_t n;           // elements (<= kFsItemElems)
+  uint32_t o0;          // row
+  uint32_t term0, nterm;
+  uint32_t whole;       // whole slabs only (transposed slabs staged in shared memory)
+};
+
+struct FsSrc {
+  const double* p[kFsMaxSlots];
+};
+
+int run_fused_sum(const FsItem* items, int nitems, const FsTerm* terms, const FsSrc& src, const double* scale,
+                  double* out, cudaStream_t st);
+
+// Direct FP64 contraction (no packing): for a contraction whose contracted
+// extent per output element is small, every output element is formed in
+// place from the stored operand tiles,
+//   C[c] = alpha * acc + C[c],  acc = sum over tile pairs p and contracted
+//   indices k of (+-) A[offA_p + c . sA_p + k . sAk_p] * B[offB_p + ...]
+// with one fused multiply-add per product (FP64 instructions are the bound
+// on this part, so no separate pack, GEMM and unpack passes).
+constexpr int kDirMaxPairs = 32;     // operand tile pairs of one output tile
+constexpr int kDirItemElems = 2048;  // output elements per work item
+
+struct DirPair {
+  int64_t offA, offB;      // stored operand tiles
+  int64_t sA[4], sB[4];    // strides of the output tile's dims (rank padded to 4 in front; 0 = not in operand)
+  int64_t sAk[2], sBk[2];  // strides of the contracted dims
+  uint32_t ek[2];          // contracted extents (1 when unused)
+  int32_t neg;             // sign factor of the pair is -1
+  int32_t pad;
+};
+
+struct DirItem {
+  int64_t coff;           // C offset of the item's first element
+  FastDiv f1, f2, f3;     // extents of output dims 1..3
+  uint32_t f0, n;         // first element within the tile, count
+  uint32_t pair0, npair;
+};
+
+int run_direct(const DirItem* items, int nitems, const DirPair* pairs, const double* A, const double* B, double* C,
+               double alpha, cudaStream_t st);
 
 // One FP64 GEMM problem of a grouped launch (element strides).
 struct GemmProblem {

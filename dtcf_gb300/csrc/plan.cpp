@@ -5,6 +5,7 @@
 #include <cstring>
 #include <map>
 #include <set>
+#include <tuple>
 
 #include "split.h"
 
@@ -278,6 +279,8 @@ void choose_engine(GroupBlock& g, bool split_engine, bool split_all, int slices)
 
 ContractionPlan::~ContractionPlan() {
   destroy_split_plan(split);
+  dev_free(d_dir_items);
+  dev_free(d_dir_pairs);
   dev_free(d_keepA);
   dev_free(d_keepB);
   dev_free(d_own_arena);
@@ -461,6 +464,108 @@ int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorL
   }
   p->flops = fl;
   p->gemm_flops = gf;
+  // direct engine: few products per output element, at most two contracted
+  // dims, at most kDirMaxPairs operand tile pairs per output tile
+  // (tiny contractions too, whose four packed launches cost more than the work)
+  const bool few = fl <= 2.0 * kDirectMaxK * (double)C.nelem || (fl <= 4e6 && fl <= 2.0 * 64.0 * (double)C.nelem);
+  if (!split_all && fl > 0.0 && few && s.contrA.size() <= 2 && C.rank <= 4 && C.rank >= 1) {
+    bool ok = true;
+    std::vector<DirItem> items;
+    std::vector<DirPair> pairs;
+    const int pad = 4 - C.rank;
+    for (size_t t = 0; t < C.tiles.size() && ok; ++t) {
+      const Coords& cc = C.tiles[t];
+      int64_t e4[4] = {1, 1, 1, 1};
+      for (int i = 0; i < C.rank; ++i) e4[pad + i] = C.dims[i]->ext[cc[i]];
+      const int64_t ntile = e4[0] * e4[1] * e4[2] * e4[3];
+      if (ntile >= ((int64_t)1 << 31)) ok = false;
+      const int hr = tuple_irrep(dA, c_row[t]);
+      const uint32_t pair0 = (uint32_t)pairs.size();
+      if (ok && ks.count(hr)) {
+        for (auto& kv : ks[hr].off) {
+          int v[kMaxDims], w[kMaxDims], sdA[kMaxDims], sdB[kMaxDims];
+          double fA, fB;
+          for (size_t i = 0; i < s.extA.size(); ++i) v[s.extA[i]] = c_row[t][i];
+          for (size_t i = 0; i < s.contrA.size(); ++i) v[s.contrA[i]] = kv.first[i];
+          for (size_t i = 0; i < s.extB.size(); ++i) w[s.extB[i]] = c_col[t][i];
+          for (size_t i = 0; i < s.contrB.size(); ++i) w[s.contrB[i]] = kv.first[i];
+          const int idA = A.resolve(v, sdA, &fA);
+          if (idA < 0) continue;
+          const int idB = B.resolve(w, sdB, &fB);
+          if (idB < 0) continue;
+          // strides of the operands' virtual dims inside their stored tiles
+          auto vstrides = [](const TensorLayout& T, int id, const int* sd, int64_t* out) {
+            const Coords& sc = T.tiles[id];
+            int64_t st[kMaxDims];
+            st[T.rank - 1] = 1;
+            for (int d = T.rank - 2; d >= 0; --d) st[d] = st[d + 1] * T.dims[d + 1]->ext[sc[d + 1]];
+            for (int d = 0; d < T.rank; ++d) out[d] = st[sd[d]];
+          };
+          int64_t vsA[kMaxDims], vsB[kMaxDims];
+          vstrides(A, idA, sdA, vsA);
+          vstrides(B, idB, sdB, vsB);
+          DirPair pr;
+          std::memset(&pr, 0, sizeof(pr));
+          pr.offA = A.off[idA];
+          pr.offB = B.off[idB];
+          for (int i = 0; i < C.rank; ++i) {
+            if (s.c_from[i] >= 0) pr.sA[pad + i] = vsA[s.extA[s.c_from[i]]];
+            else pr.sB[pad + i] = vsB[s.extB[-1 - s.c_from[i]]];
+          }
+          pr.ek[0] = pr.ek[1] = 1;
+          for (size_t j = 0; j < s.contrA.size(); ++j) {
+            pr.sAk[j] = vsA[s.contrA[j]];
+            pr.sBk[j] = vsB[s.contrB[j]];
+            pr.ek[j] = (uint32_t)A.dims[s.contrA[j]]->ext[kv.first[j]];
+          }
+          pr.neg = fA * fB < 0.0 ? 1 : 0;
+          // every read stays inside the stored tiles
+          int64_t ma = 0, mb = 0;
+          for (int d = 0; d < 4; ++d) {
+            ma += (e4[d] - 1) * pr.sA[d];
+            mb += (e4[d] - 1) * pr.sB[d];
+          }
+          const int64_t ta = A.tile_size(A.tiles[idA].data()), tb = B.tile_size(B.tiles[idB].data());
+          if (ta >= ((int64_t)1 << 31) || tb >= ((int64_t)1 << 31)) {  // tile-local offsets are 32-bit
+            ok = false;
+            break;
+          }
+          if (ma >= ta || mb >= tb) return fail(GBX_EINVAL, "direct plan: operand read outside its tile");
+          for (int j = 0; j < 2; ++j) {
+            ma += (int64_t)(pr.ek[j] - 1) * pr.sAk[j];
+            mb += (int64_t)(pr.ek[j] - 1) * pr.sBk[j];
+          }
+          if (ma >= ta || mb >= tb) return fail(GBX_EINVAL, "direct plan: operand read outside its tile");
+          pairs.push_back(pr);
+        }
+      }
+      const uint32_t npair = (uint32_t)pairs.size() - pair0;
+      if (npair > (uint32_t)kDirMaxPairs) ok = false;
+      if (!ok || npair == 0) continue;  // C += alpha * 0: nothing to do for this tile
+      for (int64_t f0 = 0; f0 < ntile; f0 += kDirItemElems) {
+        DirItem it;
+        std::memset(&it, 0, sizeof(it));
+        it.coff = C.off[t] + f0;
+        it.f1 = FastDiv::make((uint32_t)e4[1]);
+        it.f2 = FastDiv::make((uint32_t)e4[2]);
+        it.f3 = FastDiv::make((uint32_t)e4[3]);
+        it.f0 = (uint32_t)f0;
+        it.n = (uint32_t)std::min<int64_t>(kDirItemElems, ntile - f0);
+        it.pair0 = pair0;
+        it.npair = npair;
+        items.push_back(it);
+      }
+    }
+    if (ok && items.size() < ((size_t)1 << 31)) {
+      p->direct = true;
+      p->dir_items = std::move(items);
+      p->dir_pairs = std::move(pairs);
+      p->packA.host.clear();
+      p->packB.host.clear();
+      p->unpackC.host.clear();
+      p->a_needs_zero = p->b_needs_zero = false;
+    }
+  }
   GBX_TRY(check_moves(p->packA, A.nelem, p->a_elems, "pack A"));
   GBX_TRY(check_moves(p->packB, B.nelem, p->b_elems, "pack B"));
   GBX_TRY(check_moves(p->unpackC, p->c_elems, C.nelem, "unpack C"));
@@ -468,7 +573,7 @@ int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorL
   p->engine = e;
   p->slices = nslices;
   for (auto& g : p->groups) {
-    if (g.M == 0 || g.N == 0 || g.K == 0) continue;
+    if (g.M == 0 || g.N == 0 || g.K == 0 || p->direct) continue;
     if (g.M >= (1ll << 31) || g.N >= (1ll << 31) || g.K >= (1ll << 31))
       return fail(GBX_EUNSUPPORTED, "packed block too large");
     if (g.engine == 1) ++p->n_split_groups; else ++p->n_f64_groups;
@@ -514,6 +619,12 @@ void ContractionPlan::split_problems(std::vector<SplitProblem>& sp) const {
 
 int ContractionPlan::sizes(size_t* persist, size_t* arena, size_t* static_scratch) const {
   size_t keep = 0, ws = 0, scratch = 0;
+  if (direct) {
+    if (persist) *persist = up256(dir_items.size() * sizeof(DirItem)) + up256(dir_pairs.size() * sizeof(DirPair));
+    if (arena) *arena = 0;
+    if (static_scratch) *static_scratch = 0;
+    return GBX_OK;
+  }
   const size_t ab = up256(sizeof(double) * a_elems), bb = up256(sizeof(double) * b_elems);
   if (keeps_a()) keep += ab; else if (a_static) scratch += ab; else ws += ab;
   if (keeps_b()) keep += bb; else if (b_static) scratch += bb; else ws += bb;
@@ -534,6 +645,7 @@ int ContractionPlan::sizes(size_t* persist, size_t* arena, size_t* static_scratc
 }
 
 double ContractionPlan::f64_workspace_estimate() const {
+  if (direct) return 0.0;
   std::vector<GemmProblem> fp;
   for (auto& g : groups) {
     if (g.M == 0 || g.N == 0 || g.K == 0 || g.engine == 1) continue;
@@ -548,6 +660,15 @@ double ContractionPlan::f64_workspace_estimate() const {
 }
 
 int ContractionPlan::build(unsigned char* arena, unsigned char* static_scratch) {
+  if (direct) {
+    if (!dir_items.empty()) {
+      GBX_TRY(dev_alloc((void**)&d_dir_items, sizeof(DirItem) * dir_items.size()));
+      GBX_TRY(dev_alloc((void**)&d_dir_pairs, sizeof(DirPair) * dir_pairs.size()));
+      GBX_CUDA(cudaMemcpy(d_dir_items, dir_items.data(), sizeof(DirItem) * dir_items.size(), cudaMemcpyHostToDevice));
+      GBX_CUDA(cudaMemcpy(d_dir_pairs, dir_pairs.data(), sizeof(DirPair) * dir_pairs.size(), cudaMemcpyHostToDevice));
+    }
+    return GBX_OK;
+  }
   size_t keep = 0, ws = 0, scratch = 0;
   GBX_TRY(sizes(&keep, &ws, &scratch));
   if (!arena && (ws || (scratch && !static_scratch))) {
@@ -681,6 +802,7 @@ int ContractionPlan::tune_split(cudaStream_t st, int reps) {
 }
 
 int ContractionPlan::prepare_static(const double* dA, const double* dB, cudaStream_t st) {
+  if (direct) return GBX_OK;  // reads its operands where they are stored
   if (a_static) {
     if (a_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Abig, 0, sizeof(double) * a_elems, st));
     GBX_TRY(run_moves(packA, dA, d_Abig, st));
@@ -695,6 +817,7 @@ int ContractionPlan::prepare_static(const double* dA, const double* dB, cudaStre
 }
 
 int ContractionPlan::stage(const double* dA, const double* dB, cudaStream_t st) {
+  if (direct) return GBX_OK;
   const bool skipA = a_static && static_ready, skipB = b_static && static_ready;
   if (!skipA) {
     if (a_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Abig, 0, sizeof(double) * a_elems, st));
@@ -709,6 +832,7 @@ int ContractionPlan::stage(const double* dA, const double* dB, cudaStream_t st) 
 }
 
 int ContractionPlan::execute(const double* dA, const double* dB, double* dC, double alpha, cudaStream_t st) {
+  if (direct) return run_direct(d_dir_items, (int)dir_items.size(), d_dir_pairs, dA, dB, dC, alpha, st);
   if (f64.nprob == 0 && !split) return GBX_OK;
   const bool skipA = a_static && static_ready, skipB = b_static && static_ready;
   if (!skipA) {
@@ -766,6 +890,137 @@ int plan_sum(const TensorLayout& A, const TensorLayout& C, const std::vector<std
   }
   GBX_TRY(check_moves(p->moves, A.nelem, C.nelem, "sum"));
   if (!defer) GBX_TRY(p->moves.upload());
+  out = std::move(p);
+  return GBX_OK;
+}
+
+
+int FusedSumPlan::upload() {
+  release();
+  if (items.empty()) return GBX_OK;
+  GBX_TRY(dev_alloc((void**)&d_items, sizeof(FsItem) * items.size()));
+  GBX_CUDA(cudaMemcpy(d_items, items.data(), sizeof(FsItem) * items.size(), cudaMemcpyHostToDevice));
+  if (!terms.empty()) {
+    GBX_TRY(dev_alloc((void**)&d_terms, sizeof(FsTerm) * terms.size()));
+    GBX_CUDA(cudaMemcpy(d_terms, terms.data(), sizeof(FsTerm) * terms.size(), cudaMemcpyHostToDevice));
+  }
+  return GBX_OK;
+}
+
+void FusedSumPlan::release() {
+  dev_free(d_items);
+  dev_free(d_terms);
+  d_items = nullptr;
+  d_terms = nullptr;
+}
+
+int FusedSumPlan::execute(const double* const* src, const double* scale, double* out, cudaStream_t st) const {
+  if (items.empty()) return GBX_OK;
+  if (!d_items) return fail(GBX_EINVAL, "fused sum: plan not uploaded");
+  FsSrc s;
+  for (int i = 0; i < kFsMaxSlots; ++i) s.p[i] = i < nslots ? src[i] : nullptr;
+  for (int i = 0; i < nslots; ++i)
+    if (!s.p[i]) return fail(GBX_EINVAL, "fused sum: source %d missing", i);
+  return run_fused_sum(d_items, (int)items.size(), d_terms, s, scale, out, st);
+}
+
+int plan_fused_sum(const TensorLayout& C, const std::vector<std::string>& lc, const std::vector<FusedTermSpec>& specs,
+                   std::unique_ptr<FusedSumPlan>& out) {
+  const int r = C.rank;
+  if (r < 2 || r > 4 || (int)lc.size() != r) return fail(GBX_EUNSUPPORTED, "fused sum: destination rank %d", r);
+  if (C.nelem >= (int64_t)1 << 40) return fail(GBX_EUNSUPPORTED, "fused sum: destination too large");
+  const int nt = (int)specs.size();
+  if (nt > kFsMaxTerms) return fail(GBX_EUNSUPPORTED, "fused sum: %d terms (at most %d)", nt, kFsMaxTerms);
+  std::vector<std::vector<int>> a_of_c(nt, std::vector<int>(r, -1));
+  int nslots = 0;
+  for (int t = 0; t < nt; ++t) {
+    const FusedTermSpec& sp = specs[t];
+    if (!sp.A || sp.A->rank != r || (int)sp.la.size() != r)
+      return fail(GBX_EINVAL, "fused sum: term %d rank differs from the destination", t);
+    if (sp.slot < 0 || sp.slot >= kFsMaxSlots) return fail(GBX_EINVAL, "fused sum: term %d slot %d", t, sp.slot);
+    nslots = std::max(nslots, sp.slot + 1);
+    for (int i = 0; i < r; ++i) {
+      for (int j = 0; j < r; ++j)
+        if (sp.la[j] == lc[i]) a_of_c[t][i] = j;
+      if (a_of_c[t][i] < 0) return fail(GBX_EINVAL, "fused sum: index %s missing in term %d", lc[i].c_str(), t);
+      if (!C.dims[i]->same_as(*sp.A->dims[a_of_c[t][i]]))
+        return fail(GBX_EINVAL, "fused sum: blocking differs for %s in term %d", lc[i].c_str(), t);
+    }
+  }
+  auto p = std::make_unique<FusedSumPlan>();
+  p->C = C;
+  p->nslots = nslots;
+  std::vector<int> order(C.tiles.size());
+  for (size_t t = 0; t < order.size(); ++t) order[t] = (int)t;
+  if (r == 4) {
+    auto key = [&](int t) {
+      const Coords& c = C.tiles[t];
+      return std::make_tuple(std::min(c[0], c[1]), std::max(c[0], c[1]), std::min(c[2], c[3]), std::max(c[2], c[3]));
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return key(x) < key(y); });
+  }
+  for (int t : order) {
+    const Coords& cc = C.tiles[t];
+    int64_t ext[4];
+    for (int i = 0; i < r; ++i) ext[i] = C.dims[i]->ext[cc[i]];
+    const int64_t ea = ext[r - 2], eb = ext[r - 1], E = ea * eb;
+    const int64_t O0 = r == 4 ? ext[0] : 1, O1 = r >= 3 ? ext[r - 3] : 1;
+    if (E == 0 || O0 == 0 || O1 == 0) continue;
+    if (O1 * E >= ((int64_t)1 << 31)) return fail(GBX_EUNSUPPORTED, "fused sum: tile row too large");
+    const uint32_t term0 = (uint32_t)p->terms.size();
+    for (int k = 0; k < nt; ++k) {
+      const TensorLayout& A = *specs[k].A;
+      int v[kMaxDims];
+      for (int i = 0; i < r; ++i) v[a_of_c[k][i]] = cc[i];
+      int src_dim[kMaxDims];
+      double f;
+      const int id = A.resolve(v, src_dim, &f);
+      if (id < 0) continue;  // zero tile: the term adds nothing here
+      const Coords& sc = A.tiles[id];
+      int64_t sst[kMaxDims];
+      sst[r - 1] = 1;
+      for (int d = r - 2; d >= 0; --d) sst[d] = sst[d + 1] * A.dims[d + 1]->ext[sc[d + 1]];
+      int64_t sstr[4];
+      for (int i = 0; i < r; ++i) sstr[i] = sst[src_dim[a_of_c[k][i]]];
+      FsTerm tm;
+      std::memset(&tm, 0, sizeof(tm));
+      tm.off = A.off[id];
+      tm.so0 = r == 4 ? sstr[0] : 0;
+      tm.so1 = r >= 3 ? sstr[r - 3] : 0;
+      tm.sa = sstr[r - 2];
+      tm.sb = sstr[r - 1];
+      tm.coef = specs[k].coef * f;
+      tm.slot = specs[k].slot;
+      tm.mode = (tm.sb == 1 && tm.sa == eb) ? 0 : (tm.sa == 1 && tm.sb == ea) ? 1 : 2;
+      const int64_t smax = tm.off + (O0 - 1) * tm.so0 + (O1 - 1) * tm.so1 + (ea - 1) * tm.sa + (eb - 1) * tm.sb;
+      if (tm.off < 0 || smax >= A.nelem) return fail(GBX_EINVAL, "fused sum: term %d reads outside its source", k);
+      p->terms.push_back(tm);
+    }
+    const uint32_t nterm = (uint32_t)p->terms.size() - term0;
+    // items: whole slabs up to kFsItemElems elements, else pieces of a row
+    const int64_t row = O1 * E;
+    for (int64_t o0 = 0; o0 < O0; ++o0) {
+      const int64_t step = E <= kFsItemElems ? (kFsItemElems / E) * E : kFsItemElems;
+      for (int64_t f0 = 0; f0 < row; f0 += step) {
+        FsItem it;
+        std::memset(&it, 0, sizeof(it));
+        const int64_t n = std::min(step, row - f0);
+        it.dst = C.off[t] + o0 * row + f0;
+        it.fE = FastDiv::make((uint32_t)E);
+        it.fea = FastDiv::make((uint32_t)ea);
+        it.feb = FastDiv::make((uint32_t)eb);
+        it.f0 = (uint32_t)f0;
+        it.n = (uint32_t)n;
+        it.o0 = (uint32_t)o0;
+        it.term0 = term0;
+        it.nterm = nterm;
+        it.whole = (f0 % E == 0 && n % E == 0) ? 1u : 0u;
+        if (it.dst < 0 || it.dst + n > C.nelem) return fail(GBX_EINVAL, "fused sum: item outside the destination");
+        p->items.push_back(it);
+      }
+    }
+  }
+  if (p->items.size() >= ((size_t)1 << 31)) return fail(GBX_EUNSUPPORTED, "fused sum: too many items");
   out = std::move(p);
   return GBX_OK;
 }

@@ -144,6 +144,14 @@ struct ContractionPlan {
   int split_width = 0;  // output tile width of every split problem (0 = the model's choice)
   unsigned char* split_arena = nullptr;  // the split plan's per-run region and its capacity
   size_t split_arena_cap = 0;
+  // Direct engine (no packing): chosen when the contracted extent per output
+  // element is small.  The packed GEMM shapes (groups) are still planned and
+  // reported; nothing is packed, split or allocated for them.
+  bool direct = false;
+  std::vector<DirItem> dir_items;
+  std::vector<DirPair> dir_pairs;
+  DirItem* d_dir_items = nullptr;
+  DirPair* d_dir_pairs = nullptr;
 
   ~ContractionPlan();
   // Device bytes the plan keeps for itself, the arena bytes one execute
@@ -174,7 +182,12 @@ struct ContractionPlan {
   bool keeps_b() const { return b_static && n_f64_groups > 0; }
 };
 
-// split_all: every packed GEMM of a split plan uses the split engine (tests).
+// Largest average number of products per output element (flops / (2 * C
+// elements)) for which a contraction runs on the direct engine.
+constexpr double kDirectMaxK = 16.0;
+
+// split_all: every packed GEMM of a split plan uses the split engine (tests),
+// and no contraction takes the direct engine.
 // defer: plan only (host); the caller sets the static flags and calls build().
 int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorLayout& C,
                      const std::vector<std::string>& la, const std::vector<std::string>& lb,
@@ -189,6 +202,40 @@ struct SumPlan {
   int execute(const double* dA, double* dC, double alpha, cudaStream_t st);
 };
 int check_moves(const MoveSet& ms, int64_t src_elems, int64_t dst_elems, const char* what);
+
+// Several Summations (DLTC/task.cc:51-81) into one destination, fused:
+//   out[c] = (sum_t coef_t * A_t[perm_t(c)]) [* scale[c]]
+// in one pass over the destination, each element formed as 0 + c_0 x_0 +
+// c_1 x_1 + ... in term order, one fused multiply-add per term -- for
+// coefficients +-2^k the result of zeroing C, running the terms as separate
+// sums in that order and multiplying by scale.  A term may read a layout that stores canonical
+// tiles only (sign factors applied).  out must not alias a source.
+struct FusedTermSpec {
+  const TensorLayout* A;
+  std::vector<std::string> la;
+  double coef;
+  int slot;  // index of the term's source buffer in execute's src
+};
+
+struct FusedSumPlan {
+  TensorLayout C;
+  int nslots = 0;
+  std::vector<FsItem> items;
+  std::vector<FsTerm> terms;
+  FsItem* d_items = nullptr;
+  FsTerm* d_terms = nullptr;
+  int upload();
+  void release();
+  ~FusedSumPlan() { release(); }
+  size_t device_bytes() const { return items.size() * sizeof(FsItem) + terms.size() * sizeof(FsTerm); }
+  int execute(const double* const* src, const double* scale, double* out, cudaStream_t st) const;
+};
+// lc: labels of C; each term's la names the same labels in its own order.
+// Destination tiles that differ by a swap of their first two or last two
+// block coordinates are scheduled together, so that the permuted reads of
+// one source tile by its partner tiles hit L2.
+int plan_fused_sum(const TensorLayout& C, const std::vector<std::string>& lc, const std::vector<FusedTermSpec>& terms,
+                   std::unique_ptr<FusedSumPlan>& out);
 int plan_sum(const TensorLayout& A, const TensorLayout& C, const std::vector<std::string>& la,
              const std::vector<std::string>& lc, double coef, std::unique_ptr<SumPlan>& out, bool defer = false);
 

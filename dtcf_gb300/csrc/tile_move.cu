@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(kMoveThreads) tile_move_kernel(const MoveDesc*
       for (int k = 0; k < kPer; ++k) y[k] = in[k] ? t[to[k]] : 0.0;
 #pragma unroll
       for (int k = 0; k < kPer; ++k)
-        if (in[k]) t[to[k]] = __dadd_rn(y[k], __dmul_rn(scale, x[k]));
+        if (in[k]) t[to[k]] = __fma_rn(scale, x[k], y[k]);
     }
   }
 }
@@ -169,6 +169,139 @@ int run_moves_scaled(const MoveSet& ms, const double* src, double* dst, double a
 
 int run_moves(const MoveSet& ms, const double* src, double* dst, cudaStream_t st) {
   return run_moves_scaled(ms, src, dst, 1.0, st);
+}
+
+namespace {
+constexpr int kFsThreads = 256;
+constexpr int kFsPer = kFsItemElems / kFsThreads;
+// transposed slabs of one item, rows padded to an odd length: a whole-slab
+// item of n elements needs at most n + n / ea <= 2n doubles
+constexpr int kFsStage = 2 * kFsItemElems;
+static_assert(kFsPer * kFsThreads == kFsItemElems, "item size");
+}  // namespace
+
+// One CTA per work item (grid-stride over items).  Threads hold kFsPer
+// destination elements each, in destination order, and add the terms one
+// after the other: rows of slabs that are contiguous in the source's own
+// order are read directly (coalesced); slabs stored transposed are first
+// copied into shared memory in source order and read back transposed, so
+// both sides stay coalesced; anything else is gathered.  Stores are
+// coalesced along the destination.
+__global__ void __launch_bounds__(kFsThreads, 3)
+    fused_sum_kernel(const FsItem* __restrict__ items, int nitems, const FsTerm* __restrict__ terms, FsSrc src,
+                     const double* __restrict__ scale, double* __restrict__ out) {
+  __shared__ double stage[kFsStage];
+  __shared__ const double* base[kFsMaxSlots];  // indexed by the term's slot
+  // the item and its terms, read field by field (keeps registers free for
+  // the elements in flight)
+  __shared__ FsItem s_item;
+  __shared__ FsTerm s_terms[kFsMaxTerms];
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < kFsMaxSlots; ++k) base[k] = src.p[k];
+  }
+  for (int i = blockIdx.x; i < nitems; i += gridDim.x) {
+    __syncthreads();  // the previous item is finished with s_item, s_terms and stage
+    if (threadIdx.x == 0) s_item = items[i];
+    __syncthreads();
+    const FsItem& it = s_item;
+    if (threadIdx.x < it.nterm) s_terms[threadIdx.x] = terms[it.term0 + threadIdx.x];
+    __syncthreads();
+    const uint32_t E = it.fE.d, ea = it.fea.d, eb = it.feb.d;
+    double acc[kFsPer];
+#pragma unroll
+    for (int k = 0; k < kFsPer; ++k) acc[k] = 0.0;
+    // element k of this thread: e = tid + k * threads (lanes past the end
+    // repeat the last element: valid addresses, no store); its slab sg and
+    // index q within the slab are recomputed per term to save registers
+#define FS_ELEM(k, sg, q)                                                                  \
+  const uint32_t f_ = it.f0 + min((uint32_t)(threadIdx.x + (k) * kFsThreads), it.n - 1); \
+  const uint32_t sg = it.fE.div(f_);                                                     \
+  const uint32_t q = f_ - sg * E
+    for (uint32_t t = 0; t < it.nterm; ++t) {
+      const FsTerm& tm = s_terms[t];
+      const double* __restrict__ p = base[tm.slot] + tm.off + (int64_t)it.o0 * tm.so0;
+      double x[kFsPer];
+      if (tm.mode == 1 && it.whole) {
+        const uint32_t pa = ea | 1u, sp = eb * pa;
+        const uint32_t s_first = it.fE.div(it.f0);
+        __syncthreads();  // earlier reads of stage are done
+#pragma unroll
+        for (int k = 0; k < kFsPer; ++k) {
+          const uint32_t e = min((uint32_t)(threadIdx.x + k * kFsThreads), it.n - 1);
+          const uint32_t sl = it.fE.div(e);
+          x[k] = __ldg(p + (int64_t)(s_first + sl) * tm.so1 + (e - sl * E));
+        }
+#pragma unroll
+        for (int k = 0; k < kFsPer; ++k) {
+          const uint32_t e = threadIdx.x + k * kFsThreads;
+          if (e < it.n) {
+            const uint32_t sl = it.fE.div(e);
+            const uint32_t qq = e - sl * E;  // source order within the slab: b * ea + a
+            const uint32_t b = it.fea.div(qq);
+            stage[sl * sp + b * pa + (qq - b * ea)] = x[k];
+          }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kFsPer; ++k) {
+          FS_ELEM(k, sg, q);
+          const uint32_t a = it.feb.div(q);
+          x[k] = stage[(sg - s_first) * sp + (q - a * eb) * pa + a];
+        }
+      } else if (tm.mode == 0) {
+#pragma unroll
+        for (int k = 0; k < kFsPer; ++k) {
+          FS_ELEM(k, sg, q);
+          x[k] = __ldg(p + (int64_t)sg * tm.so1 + q);
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < kFsPer; ++k) {
+          FS_ELEM(k, sg, q);
+          const uint32_t a = it.feb.div(q);
+          x[k] = __ldg(p + (int64_t)sg * tm.so1 + (int64_t)a * tm.sa + (int64_t)(q - a * eb) * tm.sb);
+        }
+      }
+      // FP64 instructions are the scarce resource here (the FP64 pipe issues
+      // about 1.6 per clock per SM, fewer than the elements HBM delivers):
+      // the first term of a +-1 coefficient is a sign flip on the bits
+      // (0 + c x with -0 turned into +0), every later term one fused
+      // multiply-add -- the separately rounded product and sum whenever c x
+      // is exact, as it is for c = +-2^k
+      const unsigned long long cbits = (unsigned long long)__double_as_longlong(tm.coef);
+      if (t == 0 && (cbits & 0x7FFFFFFFFFFFFFFFull) == 0x3FF0000000000000ull) {
+        const unsigned long long sign = cbits & 0x8000000000000000ull;
+#pragma unroll
+        for (int k = 0; k < kFsPer; ++k) {
+          const unsigned long long b = (unsigned long long)__double_as_longlong(x[k]) ^ sign;
+          acc[k] = __longlong_as_double((long long)(b == 0x8000000000000000ull ? 0ull : b));
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < kFsPer; ++k) acc[k] = __fma_rn(tm.coef, x[k], acc[k]);
+      }
+    }
+#undef FS_ELEM
+#pragma unroll
+    for (int k = 0; k < kFsPer; ++k) {
+      const uint32_t e = threadIdx.x + k * kFsThreads;
+      if (e < it.n) {
+        double v = acc[k];
+        if (scale) v = __dmul_rn(v, __ldg(scale + it.dst + e));
+        out[it.dst + e] = v;
+      }
+    }
+  }
+}
+
+int run_fused_sum(const FsItem* items, int nitems, const FsTerm* terms, const FsSrc& src, const double* scale,
+                  double* out, cudaStream_t st) {
+  if (nitems == 0) return GBX_OK;
+  const int grid = std::min(nitems, 152 * 6);
+  fused_sum_kernel<<<grid, kFsThreads, 0, st>>>(items, nitems, terms, src, scale, out);
+  GBX_CUDA(cudaGetLastError());
+  return GBX_OK;
 }
 
 }  // namespace gbx

@@ -51,7 +51,6 @@ typedef struct gbx_cc_job gbx_cc_job;
 /* Fill cfg with the defaults of the synthetic system (seed 1, eps ranges
  * [-2,-0.5] / [0.2,3.0], v_scale 1e-2, v_decay 8, block 16, CCSD, FP64). */
 GBX_API void gbx_cc_default_config(gbx_cc_config* cfg);
-/* Build the job: orbitals, integrals (on the device), plans, MP2 guess. */
 /* Device bytes a job of this configuration will hold once built
  * (resident_bytes) and at most while it is being built (peak_bytes), and the
  * algorithmic flops of one iteration, from host planning alone: no device
@@ -59,15 +58,16 @@ GBX_API void gbx_cc_default_config(gbx_cc_config* cfg);
  * output pointer may be NULL. */
 GBX_API int gbx_cc_footprint(const gbx_cc_config* cfg, double* resident_bytes, double* peak_bytes,
                              double* flops_per_iter);
+/* Build the job: orbitals, integrals (on the device), plans, MP2 guess. */
 GBX_API int gbx_cc_create(const gbx_cc_config* cfg, void* stream, gbx_cc_job** job);
-/* Enqueue niter Jacobi iterations on stream without waiting; the energy of
- * each lands in the job's device history. */
 /* Captures one iteration as a CUDA graph now (otherwise the first enqueue
  * does it); a no-op when use_graph is 0 or the graph exists. */
 GBX_API int gbx_cc_capture(gbx_cc_job* job);
 /* GBX_ETIMEOUT if a bounded device wait of the split engine ran out in any
  * iteration so far (reads the error words; call after the work finished). */
 GBX_API int gbx_cc_check(gbx_cc_job* job);
+/* Enqueue niter Jacobi iterations on stream without waiting; the energy of
+ * each lands in the job's device history. */
 GBX_API int gbx_cc_enqueue(gbx_cc_job* job, int niter, void* stream);
 /* Run niter iterations and return their correlation energies (host array of
  * niter); waits for the stream. */
@@ -86,8 +86,8 @@ GBX_API int gbx_cc_gemm_shapes(const gbx_cc_job* job, int64_t* mnk, int* count);
 /* Element counts of the amplitude tensors in their tile storage. */
 GBX_API int gbx_cc_amplitude_elems(const gbx_cc_job* job, int64_t* n1, int64_t* n2);
 /* Enqueue host -> device copies of the amplitudes (tile storage order) on
- * stream; the next iteration starts from them.  Pinned host memory keeps the
- * copies asynchronous. */
+ * stream, and the tau / taut / Q combinations of them; the next iteration
+ * starts from them.  Pinned host memory keeps the copies asynchronous. */
 GBX_API int gbx_cc_set_amplitudes(gbx_cc_job* job, const double* t1, const double* t2, void* stream);
 /* Enqueue a device -> host copy of the latest energy on stream. */
 GBX_API int gbx_cc_read_energy(gbx_cc_job* job, double* energy, void* stream);
@@ -99,13 +99,16 @@ GBX_API int gbx_cc_profile(gbx_cc_job* job, int cap, float* ms, double* flops, d
                            char* names, int name_len, int* count, void* stream);
 /* Kernel choice of one contraction's packed GEMMs: the split output tile
  * width (64 with at most 4 slices: the k-stationary kernel; 0: the width
- * model's choice per GEMM), the number of split and FP64 GEMMs, the slices. */
+ * model's choice per GEMM), the number of split and FP64 GEMMs (both 0 for a
+ * contraction on the direct engine), the slices. */
 GBX_API int gbx_cc_plan_info(const gbx_cc_job* job, int contraction, int* split_width, int* n_split, int* n_f64,
                              int* slices);
 /* Time only the GEMM launches of one contraction (its operands packed and
  * split again first), reps times, with CUDA events on stream.  Reports
  * ms per run, the FP64 flops of the packed GEMMs, the bf16 tensor flops the
- * split engine issues, and the engine (0 FP64, 1 split, 2 both). */
+ * split engine issues, and the engine (0 FP64, 1 split, 2 both, 3 direct:
+ * the unpacked FP64 kernel of contractions with few products per output
+ * element, timed with alpha = 0 so that C keeps its values). */
 GBX_API int gbx_cc_time_gemm(gbx_cc_job* job, int contraction, int reps, float* ms, double* fp64_flops,
                              double* tensor_flops, int* engine, void* stream);
 GBX_API int gbx_cc_destroy(gbx_cc_job* job);

@@ -31,13 +31,15 @@ def spaces(name):
 
 
 def contraction_list(method="ccsd"):
-    """(C, lc, A, la, B, lb) of one iteration, in execution order."""
+    """(C, lc, A, la, B, lb) of one iteration, in execution order.
+
+    Only contractions over at least one index are dgemms: the outer products
+    t1 (x) t1 inside tau, taut and Q (no contracted index) are formed element
+    by element together with those tensors, as are all permuted sums."""
     sd = method == "ccsd"
     L = []
     tau, taut = ("tau", "taut") if sd else ("t2", "t2")
     if sd:
-        L += [("tau", "ijab", "t1", "ia", "t1", "jb"), ("tau", "ijab", "t1", "ib", "t1", "ja"),
-              ("taut", "ijab", "t1", "ia", "t1", "jb"), ("taut", "ijab", "t1", "ib", "t1", "ja")]
         L += [("Fae", "ae", "t1", "mf", "OVVV", "mafe")]
     L += [("Fae", "ae", taut, "mnaf", "OOVV", "mnef")]
     if sd:
@@ -47,8 +49,7 @@ def contraction_list(method="ccsd"):
         L += [("Fme", "me", "t1", "nf", "OOVV", "mnef"), ("Xoooo", "mnij", "t1", "je", "OOOV", "mnie")]
     L += [("Wmnij", "mnij", tau, "ijef", "OOVV", "mnef")]
     if sd:
-        L += [("Wmbej", "mbej", "t1", "jf", "OVVV", "mbef"), ("Wmbej", "mbej", "t1", "nb", "OOVO", "mnej"),
-              ("Q", "jnfb", "t1", "jf", "t1", "nb")]
+        L += [("Wmbej", "mbej", "t1", "jf", "OVVV", "mbef"), ("Wmbej", "mbej", "t1", "nb", "OOVO", "mnej")]
     L += [("Wmbej", "mbej", "Q", "jnfb", "OOVV", "mnef")]
     if sd:
         L += [("R1", "ia", "t1", "ie", "Fae", "ae"), ("R1", "ia", "t1", "ma", "Fmi", "mi"),
@@ -65,8 +66,6 @@ def contraction_list(method="ccsd"):
     if sd:
         L += [("V3", "imbj", "t1", "ie", "OVVO", "mbej"), ("Xa", "ijab", "t1", "ma", "V3", "imbj"),
               ("Xa", "ijab", "t1", "ie", "VVVO", "abej"), ("Xa", "ijab", "t1", "ma", "OVOO", "mbij")]
-        L += [("tau", "ijab", "t1", "ia", "t1", "jb"), ("tau", "ijab", "t1", "ib", "t1", "ja"),
-              ("taut", "ijab", "t1", "ia", "t1", "jb"), ("taut", "ijab", "t1", "ib", "t1", "ja")]
     return L
 
 
