@@ -574,8 +574,7 @@ int gbx_cc_job::footprint(double* resident, double* peak) const {
     ws = std::max(ws, (double)w);
     scratch = std::max(scratch, (double)sc);
   }
-  for (auto& p : splans)
-    keep += (double)(p->moves.host.size() * sizeof(MoveDesc) + (p->moves.host.size() + 1) * sizeof(uint32_t));
+  for (auto& p : splans) keep += (double)p->moves.device_bytes();
   for (auto& p : fplans) keep += up256d((double)(p->items.size() * sizeof(FsItem))) + up256d((double)(p->terms.size() * sizeof(FsTerm)));
   keep += up256d((double)(amp_tiles.size() * sizeof(CCAmpTile))) + up256d((double)(amp_items.size() * sizeof(CCAmpItem)));
   auto tiles_bytes = [](const TensorLayout& L) {

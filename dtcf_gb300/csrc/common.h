@@ -80,15 +80,32 @@ struct MoveDesc {
 MoveDesc make_move(int rank, const int64_t* ext, const int64_t* sstr, const int64_t* dstr, int64_t src,
                    int64_t dst, int op, double scale);
 
-// A set of moves uploaded to the device with its launch schedule.
+// Compact form of a move of at most four dimensions (padded in front with
+// unit extents), with the first chunk of its launch schedule.
+struct MoveDesc4 {
+  int64_t src, dst;
+  int64_t sstr[4], dstr[4];
+  FastDiv div[4];
+  uint32_t ext[4];
+  uint32_t n, first;
+  int32_t op, pad;
+  double scale;
+};
+
+// A set of moves uploaded to the device with its launch schedule.  When every
+// move has at most four dimensions the compact descriptors and a chunk ->
+// descriptor table are uploaded instead of the general ones.
 struct MoveSet {
   std::vector<MoveDesc> host;
   MoveDesc* d_desc = nullptr;
   uint32_t* d_first = nullptr;  // first chunk of each descriptor (prefix sum)
+  MoveDesc4* d_desc4 = nullptr;
+  uint32_t* d_chunk_desc = nullptr;  // descriptor of each chunk
   uint32_t nchunks = 0;
   int ndesc = 0;
   int upload();   // copies host -> device (allocates)
   void release();
+  size_t device_bytes() const;  // what upload() allocates
   ~MoveSet() { release(); }
 };
 
@@ -102,9 +119,10 @@ int run_moves_scaled(const MoveSet& ms, const double* src, double* dst, double a
 //   out = (0 + coef_0 * x_0 + coef_1 * x_1 + ...) [* scale]
 // in term order, each term added with one fused multiply-add (the separately
 // rounded product and sum whenever coef * x is exact, as for coef = +-2^k),
-// x_t the element of source term t under that term's permutation.  A destination tile is walked
-// as rows of slabs: a slab is its last two dimensions (extents ea x eb,
-// contiguous), a row the slabs of one index o0 of its first dimension.
+// x_t the element of source term t under that term's permutation.  A
+// destination tile is a sequence of slabs: a slab is its last two dimensions
+// (extents ea x eb, contiguous), slab s sits at outer indices (o0, o1) =
+// (s / O1, s % O1) of its first two dimensions (padded with unit extents).
 constexpr int kFsMaxSlots = 8;     // distinct source buffers of one plan
 constexpr int kFsMaxTerms = 16;    // terms of one plan
 constexpr int kFsItemElems = 2048; // destination elements per work item
@@ -119,15 +137,14 @@ struct FsTerm {
   int32_t mode;      // 0 slabs contiguous in order, 1 slabs contiguous transposed, 2 gather
 };
 
-// A run of destination elements inside one row of one tile.
+// A run of destination elements inside one tile.
 struct FsItem {
-  int64_t dst;          // destination (and scale) offset of the first element
-  FastDiv fE, fea, feb; // slab size ea * eb and the slab extents
-  uint32_t f0;          // index of the first element within the row
-  uint32_t n;           // elements (<= kFsItemElems)
-  uint32_t o0;          // row
+  int64_t dst;               // destination (and scale) offset of the first element
+  FastDiv fE, fea, feb, fo1; // slab size ea * eb, the slab extents, O1
+  uint32_t f0;               // index of the first element within the tile
+  uint32_t n;                // elements (<= kFsItemElems)
   uint32_t term0, nterm;
-  uint32_t whole;       // whole slabs only (transposed slabs staged in shared memory)
+  uint32_t whole;            // whole slabs only (transposed slabs staged in shared memory)
 };
 
 struct FsSrc {

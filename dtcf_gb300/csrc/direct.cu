@@ -54,19 +54,28 @@ __global__ void __launch_bounds__(kDirThreads, 2)
         ba[k] = (uint32_t)(c0 * pr.sA[0] + c1 * pr.sA[1] + c2 * pr.sA[2] + c3 * pr.sA[3]);
         bb[k] = (uint32_t)(c0 * pr.sB[0] + c1 * pr.sB[1] + c2 * pr.sB[2] + c3 * pr.sB[3]);
       }
-      const bool neg = pr.neg != 0;
-      for (uint32_t k1 = 0; k1 < pr.ek[1]; ++k1) {
-        for (uint32_t k0 = 0; k0 < pr.ek[0]; ++k0) {
-          const double* __restrict__ pa = A + pr.offA + (int64_t)k0 * pr.sAk[0] + (int64_t)k1 * pr.sAk[1];
-          const double* __restrict__ pb = B + pr.offB + (int64_t)k0 * pr.sBk[0] + (int64_t)k1 * pr.sBk[1];
-          double x[kDirPer], y[kDirPer];
+      // the pair's loop fields in registers; its sign flips the sign bit of
+      // the A values on the integer pipe (written as a floating-point
+      // negation it costs a second DFMA per product: both signs computed,
+      // then selected)
+      const uint32_t ek0 = pr.ek[0], ek1 = pr.ek[1];
+      const int64_t sak0 = pr.sAk[0], sak1 = pr.sAk[1], sbk0 = pr.sBk[0], sbk1 = pr.sBk[1];
+      const double* __restrict__ A0 = A + pr.offA;
+      const double* __restrict__ B0 = B + pr.offB;
+      const long long flip = pr.neg != 0 ? (long long)0x8000000000000000ull : 0ll;
+      for (uint32_t k1 = 0; k1 < ek1; ++k1) {
+        for (uint32_t k0 = 0; k0 < ek0; ++k0) {
+          const double* __restrict__ pa = A0 + (int64_t)k0 * sak0 + (int64_t)k1 * sak1;
+          const double* __restrict__ pb = B0 + (int64_t)k0 * sbk0 + (int64_t)k1 * sbk1;
+          long long x[kDirPer];
+          double y[kDirPer];
 #pragma unroll
           for (int k = 0; k < kDirPer; ++k) {
-            x[k] = __ldg(pa + ba[k]);
+            x[k] = __double_as_longlong(__ldg(pa + ba[k]));
             y[k] = __ldg(pb + bb[k]);
           }
 #pragma unroll
-          for (int k = 0; k < kDirPer; ++k) acc[k] = __fma_rn(neg ? -x[k] : x[k], y[k], acc[k]);
+          for (int k = 0; k < kDirPer; ++k) acc[k] = __fma_rn(__longlong_as_double(x[k] ^ flip), y[k], acc[k]);
         }
       }
     }

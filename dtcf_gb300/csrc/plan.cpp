@@ -585,9 +585,7 @@ int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorL
 
 namespace {
 size_t up256(size_t x) { return (x + 255) / 256 * 256; }
-size_t move_bytes(const MoveSet& m) {
-  return m.host.empty() ? 0 : m.host.size() * sizeof(MoveDesc) + (m.host.size() + 1) * sizeof(uint32_t);
-}
+size_t move_bytes(const MoveSet& m) { return m.device_bytes(); }
 }  // namespace
 
 // The split engine's problems over the packed buffers (sizes() only needs
@@ -966,7 +964,8 @@ int plan_fused_sum(const TensorLayout& C, const std::vector<std::string>& lc, co
     const int64_t ea = ext[r - 2], eb = ext[r - 1], E = ea * eb;
     const int64_t O0 = r == 4 ? ext[0] : 1, O1 = r >= 3 ? ext[r - 3] : 1;
     if (E == 0 || O0 == 0 || O1 == 0) continue;
-    if (O1 * E >= ((int64_t)1 << 31)) return fail(GBX_EUNSUPPORTED, "fused sum: tile row too large");
+    if (O0 * O1 * E >= ((int64_t)1 << 31) || O0 >= 65536 || O1 >= 65536)
+      return fail(GBX_EUNSUPPORTED, "fused sum: tile too large");
     const uint32_t term0 = (uint32_t)p->terms.size();
     for (int k = 0; k < nt; ++k) {
       const TensorLayout& A = *specs[k].A;
@@ -992,32 +991,32 @@ int plan_fused_sum(const TensorLayout& C, const std::vector<std::string>& lc, co
       tm.coef = specs[k].coef * f;
       tm.slot = specs[k].slot;
       tm.mode = (tm.sb == 1 && tm.sa == eb) ? 0 : (tm.sa == 1 && tm.sb == ea) ? 1 : 2;
-      const int64_t smax = tm.off + (O0 - 1) * tm.so0 + (O1 - 1) * tm.so1 + (ea - 1) * tm.sa + (eb - 1) * tm.sb;
-      if (tm.off < 0 || smax >= A.nelem) return fail(GBX_EINVAL, "fused sum: term %d reads outside its source", k);
+      const int64_t span = (O0 - 1) * tm.so0 + (O1 - 1) * tm.so1 + (ea - 1) * tm.sa + (eb - 1) * tm.sb;
+      if (tm.off < 0 || tm.off + span >= A.nelem) return fail(GBX_EINVAL, "fused sum: term %d reads outside its source", k);
+      if (span >= ((int64_t)1 << 31)) return fail(GBX_EUNSUPPORTED, "fused sum: source tile too large");
       p->terms.push_back(tm);
     }
     const uint32_t nterm = (uint32_t)p->terms.size() - term0;
-    // items: whole slabs up to kFsItemElems elements, else pieces of a row
-    const int64_t row = O1 * E;
-    for (int64_t o0 = 0; o0 < O0; ++o0) {
-      const int64_t step = E <= kFsItemElems ? (kFsItemElems / E) * E : kFsItemElems;
-      for (int64_t f0 = 0; f0 < row; f0 += step) {
-        FsItem it;
-        std::memset(&it, 0, sizeof(it));
-        const int64_t n = std::min(step, row - f0);
-        it.dst = C.off[t] + o0 * row + f0;
-        it.fE = FastDiv::make((uint32_t)E);
-        it.fea = FastDiv::make((uint32_t)ea);
-        it.feb = FastDiv::make((uint32_t)eb);
-        it.f0 = (uint32_t)f0;
-        it.n = (uint32_t)n;
-        it.o0 = (uint32_t)o0;
-        it.term0 = term0;
-        it.nterm = nterm;
-        it.whole = (f0 % E == 0 && n % E == 0) ? 1u : 0u;
-        if (it.dst < 0 || it.dst + n > C.nelem) return fail(GBX_EINVAL, "fused sum: item outside the destination");
-        p->items.push_back(it);
-      }
+    // items: runs of whole slabs (across rows) up to kFsItemElems
+    // elements, else pieces of one slab
+    const int64_t tile_n = O0 * O1 * E;
+    const int64_t step = E <= kFsItemElems ? (kFsItemElems / E) * E : kFsItemElems;
+    for (int64_t f0 = 0; f0 < tile_n; f0 += step) {
+      FsItem it;
+      std::memset(&it, 0, sizeof(it));
+      const int64_t n = std::min(step, tile_n - f0);
+      it.dst = C.off[t] + f0;
+      it.fE = FastDiv::make((uint32_t)E);
+      it.fea = FastDiv::make((uint32_t)ea);
+      it.feb = FastDiv::make((uint32_t)eb);
+      it.fo1 = FastDiv::make((uint32_t)O1);
+      it.f0 = (uint32_t)f0;
+      it.n = (uint32_t)n;
+      it.term0 = term0;
+      it.nterm = nterm;
+      it.whole = (f0 % E == 0 && n % E == 0) ? 1u : 0u;
+      if (it.dst < 0 || it.dst + n > C.nelem) return fail(GBX_EINVAL, "fused sum: item outside the destination");
+      p->items.push_back(it);
     }
   }
   if (p->items.size() >= ((size_t)1 << 31)) return fail(GBX_EUNSUPPORTED, "fused sum: too many items");
