@@ -138,6 +138,17 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
   return d;
 }
 
+// 64-byte swizzled rows (32 bf16 of K): 8-row groups 512 bytes apart
+__device__ __forceinline__ uint64_t sdesc64(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)1 << 16;              // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(512 >> 4) << 32;     // stride byte offset
+  d |= (uint64_t)1 << 46;              // descriptor version
+  d |= (uint64_t)4 << 61;              // 64-byte swizzle
+  return d;
+}
+
 template <int BN>
 __device__ __forceinline__ constexpr uint32_t idesc_bf16() {
   return (1u << 4)                  // D: f32
@@ -164,6 +175,12 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
         "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t* r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
 }
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
@@ -460,24 +477,86 @@ __global__ void __launch_bounds__(SplitCfg<BN>::kThreads, SplitCfg<BN>::kCtasPer
 // (level l at columns l*32 of a buffer; two buffers alternate between tiles).
 // A level sums at most S products of 64 K-elements, below 2^24, so no drains
 // are needed mid-tile: the drain warps read the levels from S-1 down to 0 and
-// recombine them with FP64 Horner steps directly.
+// recombine them with FP64 Horner steps directly.  The k-block is TBK = 64
+// (128-byte swizzled rows) or, for K <= 32, TBK = 32 (64-byte rows): slices
+// are padded to the k-block, so short K (a virtual block of ~30 orbitals)
+// streams half the bytes with the narrow block.
 constexpr int kThinBN = 32;
-constexpr int kThinSlots = 10;   // ring of (A slice, B slice) pairs, 20 KB each
 constexpr int kThinThreads = 192;
 
+template <int TBK>
 struct ThinSmem {
-  alignas(1024) __nv_bfloat16 a[kThinSlots][BM * BK];
-  alignas(1024) __nv_bfloat16 b[kThinSlots][kThinBN * BK];
-  uint64_t full[kThinSlots], empty[kThinSlots], accfull[2], accempty[2], done;
+  static constexpr int kSlots = 10 * (BK / TBK);  // ring of (A slice, B slice) pairs, 200 KB of them
+  alignas(1024) __nv_bfloat16 a[kSlots][BM * TBK];
+  alignas(1024) __nv_bfloat16 b[kSlots][kThinBN * TBK];
+  uint64_t full[kSlots], empty[kSlots], accfull[2], accempty[2], done;
   uint32_t tmem_base;
 };
 
+// Drain of one thin tile, first NC columns (NC covers ncol): Horner over the
+// levels in exact int64 fixed point, Y = sum_l X_l 2^(8 (L - l)), from level
+// 0 up (|X_l| <= 7 * 64 * 2^14 < 2^23, so |Y| < 2^63 for L <= 5; S = 7 keeps
+// the FP64 recombination); the accumulator buffer is released before the
+// scaled results are stored.
+template <int NC>
+__device__ __forceinline__ void thin_drain(uint32_t tb, int L, int ncol, const DevProblem& pr, int row,
+                                           uint64_t* accempty, int lane) {
+  long long Y[NC];
+  double acc[NC];
+#pragma unroll
+  for (int j = 0; j < NC; ++j) {
+    Y[j] = 0;
+    acc[j] = 0.0;
+  }
+  for (int l = L <= 5 ? 0 : L; L <= 5 ? l <= L : l >= 0; l += L <= 5 ? 1 : -1) {
+    uint32_t r[NC];
+    if (NC == 8) {
+      tmem_ld8(tb + (uint32_t)(l * kThinBN), r);
+    } else {
+#pragma unroll
+      for (int h = 0; h < NC / 16; ++h)
+        tmem_ld16(tb + (uint32_t)(l * kThinBN + 16 * h), *reinterpret_cast<uint32_t(*)[16]>(r + 16 * h));
+    }
+    tmem_wait_ld();
+    if (L <= 5) {
+#pragma unroll
+      for (int j = 0; j < NC; ++j)
+        if (j < ncol) Y[j] = Y[j] * 256 + (long long)__float2int_rn(__uint_as_float(r[j]));
+    } else {
+#pragma unroll
+      for (int j = 0; j < NC; ++j)
+        if (j < ncol) acc[j] = acc[j] * 0x1.0p-8 + (double)__uint_as_float(r[j]);
+    }
+  }
+  tc_fence_before();
+  __syncwarp();
+  if (lane == 0) mbar_arrive(accempty);
+  if (row < pr.M) {
+    const int ea = pr.eA[row];
+    double* crow = pr.C + (int64_t)row * pr.ldc;
+    const int lshift = L <= 5 ? 8 * L : 0;  // the int64 path carries 2^(8L)
+#pragma unroll
+    for (int j = 0; j < NC; ++j) {
+      if (j < ncol) {
+        int ex = ea + pr.eB[j] - 2 * 1022 - 14 - lshift + 1023;
+        ex = ex < 1 ? 1 : (ex > 2046 ? 2046 : ex);
+        const double v = L <= 5 ? (double)Y[j] : acc[j];
+        crow[j] = v * __longlong_as_double((long long)ex << 52);
+      }
+    }
+  }
+}
+
+template <int TBK>
 __global__ void __launch_bounds__(kThinThreads, 1) split_thin_kernel(const GemmParams P) {
+  static_assert(TBK == 32 || TBK == 64, "thin k-block");
+  using Sm = ThinSmem<TBK>;
+  constexpr int kThinSlots = Sm::kSlots;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
-  ThinSmem& sm = *reinterpret_cast<ThinSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  Sm& sm = *reinterpret_cast<Sm*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int S = P.S, L = P.L;
-  constexpr uint32_t kTx = (BM + kThinBN) * BK * 2;
+  constexpr uint32_t kTx = (BM + kThinBN) * TBK * 2;
   constexpr uint32_t kCols = 512;
   if (threadIdx.x == 0) {
     for (int i = 0; i < kThinSlots; ++i) {
@@ -567,10 +646,11 @@ __global__ void __launch_bounds__(kThinThreads, 1) split_thin_kernel(const GemmP
           bool first = true;
           for (int s = max(1, l + 2 - S); s <= min(S, l + 1); ++s) {
             const int t = l + 2 - s;
-            const uint64_t a0 = sdesc(smem_u32(sm.a[sl[s - 1]]));
-            const uint64_t b0 = sdesc(smem_u32(sm.b[sl[t - 1]]));
+            const uint32_t as = smem_u32(sm.a[sl[s - 1]]), bs = smem_u32(sm.b[sl[t - 1]]);
+            const uint64_t a0 = TBK == 64 ? sdesc(as) : sdesc64(as);
+            const uint64_t b0 = TBK == 64 ? sdesc(bs) : sdesc64(bs);
 #pragma unroll
-            for (int k = 0; k < BK / 16; ++k) {
+            for (int k = 0; k < TBK / 16; ++k) {
               umma(d, a0 + (uint64_t)(k * 2), b0 + (uint64_t)(k * 2), idesc, first ? 0u : 1u);
               first = false;
             }
@@ -599,59 +679,18 @@ __global__ void __launch_bounds__(kThinThreads, 1) split_thin_kernel(const GemmP
       if (!w_ok) break;
       __syncwarp();
       tc_fence_after();
-      // Horner over the levels in exact int64 fixed point, Y = sum_l X_l 2^(8 (L - l)),
-      // from level 0 up (|X_l| <= 7 * 64 * 2^14 < 2^23, so |Y| < 2^63 for L <= 5);
-      // S = 7 keeps the FP64 recombination
+      // only the tile's real columns are read and combined: a drain sized
+      // for 8, 16 or 32 columns (the thin problems of a block-sparse
+      // contraction often have an occupied block of ~6 as N)
       const int ncol = min(kThinBN, pr.N - ti.n0);
-      long long Y[kThinBN];
-      double acc[kThinBN];
-#pragma unroll
-      for (int j = 0; j < kThinBN; ++j) {
-        Y[j] = 0;
-        acc[j] = 0.0;
-      }
-      if (L <= 5) {
-        for (int l = 0; l <= L; ++l) {
-          uint32_t r[2][16];
-          tmem_ld16(tmem + lane_addr + (uint32_t)buf * buf_cols + (uint32_t)(l * kThinBN), r[0]);
-          tmem_ld16(tmem + lane_addr + (uint32_t)buf * buf_cols + (uint32_t)(l * kThinBN + 16), r[1]);
-          tmem_wait_ld();
-#pragma unroll
-          for (int j = 0; j < kThinBN; ++j)
-            if (j < ncol) Y[j] = Y[j] * 256 + (long long)__float2int_rn(__uint_as_float(r[j >> 4][j & 15]));
-        }
-      } else {
-        for (int l = L; l >= 0; --l) {
-          uint32_t r[2][16];
-          tmem_ld16(tmem + lane_addr + (uint32_t)buf * buf_cols + (uint32_t)(l * kThinBN), r[0]);
-          tmem_ld16(tmem + lane_addr + (uint32_t)buf * buf_cols + (uint32_t)(l * kThinBN + 16), r[1]);
-          tmem_wait_ld();
-#pragma unroll
-          for (int j = 0; j < kThinBN; ++j)
-            if (j < ncol) acc[j] = acc[j] * 0x1.0p-8 + (double)__uint_as_float(r[j >> 4][j & 15]);
-        }
-      }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&sm.accempty[buf]);
+      const uint32_t tb = tmem + lane_addr + (uint32_t)buf * buf_cols;
+      const int row = ti.m0 + quarter * 32 + lane;
+      if (ncol <= 8) thin_drain<8>(tb, L, ncol, pr, row, &sm.accempty[buf], lane);
+      else if (ncol <= 16) thin_drain<16>(tb, L, ncol, pr, row, &sm.accempty[buf], lane);
+      else thin_drain<32>(tb, L, ncol, pr, row, &sm.accempty[buf], lane);
       if (++buf == 2) {
         buf = 0;
         aphase ^= 1;
-      }
-      const int row = ti.m0 + quarter * 32 + lane;
-      if (row < pr.M) {
-        const int ea = pr.eA[row];
-        double* crow = pr.C + (int64_t)row * pr.ldc;
-        const int lshift = L <= 5 ? 8 * L : 0;  // the int64 path carries 2^(8L)
-#pragma unroll
-        for (int j = 0; j < kThinBN; ++j) {
-          if (j < ncol) {
-            int ex = ea + pr.eB[j] - 2 * 1022 - 14 - lshift + 1023;
-            ex = ex < 1 ? 1 : (ex > 2046 ? 2046 : ex);
-            const double v = L <= 5 ? (double)Y[j] : acc[j];
-            crow[j] = v * __longlong_as_double((long long)ex << 52);
-          }
-        }
       }
     }
   }
@@ -1059,15 +1098,17 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
   return fn;
 }
 
-int encode_slices(CUtensorMap* map, const __nv_bfloat16* base, int64_t S, int64_t rows, int64_t Kp, int box_rows) {
+int encode_slices(CUtensorMap* map, const __nv_bfloat16* base, int64_t S, int64_t rows, int64_t Kp, int box_rows,
+                  int box_k = BK) {
   auto enc = get_encode();
   if (!enc) return fail(GBX_ECUDA, "cuTensorMapEncodeTiled unavailable");
   cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)S};
   cuuint64_t strides[2] = {(cuuint64_t)(Kp * 2), (cuuint64_t)(rows * Kp * 2)};
-  cuuint32_t box[3] = {(cuuint32_t)BK, (cuuint32_t)box_rows, 1};
+  cuuint32_t box[3] = {(cuuint32_t)box_k, (cuuint32_t)box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
   CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, (void*)base, dims, strides, box, estr,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, box_k == BK ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(GBX_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
   return GBX_OK;
@@ -1117,7 +1158,7 @@ struct SplitPlan {
   int S = 0, L = 0;
   std::vector<SplitProblem> host;
   std::vector<int> width;  // per problem
-  std::vector<bool> thin;  // per problem: thin-K kernel
+  std::vector<int> thin;  // per problem: 0, or the thin-K kernel with a 64 (1) or 32 (2) element k-block
   unsigned char* d_persist = nullptr;    // slices and exponents of constant plan operands
   unsigned char* d_own_arena = nullptr;  // the per-run region when no arena was given
   SplitRowSet* d_sets_a = nullptr;  // long rows from the plan's packed A
@@ -1176,6 +1217,7 @@ struct SplitLayout {
   struct Prob {
     int bn = 0;
     bool thin = false;
+    int kb = BK;  // k-block: 64, or 32 for thin problems with K <= 32
     int64_t Mp = 0, Np = 0, Kp = 0;
     int ra = 0, rb = 0;      // region of the GEMM's A and B slices
     int64_t sa = 0, sb = 0;  // slice offsets
@@ -1212,7 +1254,8 @@ int split_layout(const std::vector<SplitProblem>& probs, int S, bool static_a, b
       return fail(GBX_EINVAL, "split tile width %d", o.bn);
     o.Mp = (q.M + BM - 1) / BM * BM;
     o.Np = (q.N + o.bn - 1) / o.bn * o.bn;
-    o.Kp = (q.K + BK - 1) / BK * BK;
+    o.kb = o.thin && q.K <= 32 ? 32 : BK;
+    o.Kp = (q.K + o.kb - 1) / o.kb * o.kb;
     // the GEMM's A rows come from plan operand B when swapped
     const bool a_const = q.a_is_plan_b ? static_b : static_a;
     const bool b_const = q.a_is_plan_b ? static_a : static_b;
@@ -1231,7 +1274,8 @@ int split_layout(const std::vector<SplitProblem>& probs, int S, bool static_a, b
   }
   for (size_t i = 0; i < probs.size(); ++i) {
     SplitLayout::Prob& o = L.p[i];
-    const int nkb = (int)(o.Kp / BK);
+    const int nkb = (int)(o.Kp / o.kb);
+    if (nkb < 1) return fail(GBX_EINVAL, "split problem without a k-block");
     // split K when the output tiles of all problems leave SMs idle; ranges are
     // whole exact-accumulation chunks
     int ks = 1;
@@ -1276,7 +1320,7 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
   GBX_TRY(split_layout(probs, S, static_a, static_b, lay));
   for (auto& o : lay.p) {
     sp->width.push_back(o.bn);
-    sp->thin.push_back(o.thin);
+    sp->thin.push_back(o.thin ? (o.kb == 32 ? 2 : 1) : 0);
   }
   unsigned char* base[2] = {nullptr, nullptr};
   const size_t b0 = lay.bytes(0), b1 = lay.bytes(1);
@@ -1343,7 +1387,7 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
     d.M = (int)p.M;
     d.N = (int)p.N;
     d.K = (int)p.K;
-    d.nkb = (int)(o.Kp / BK);
+    d.nkb = (int)(o.Kp / o.kb);
     d.tiles_m = (int)(o.Mp / BM);
     d.tiles_n = (int)(o.Np / bn);
     d.ksplit = o.ks;
@@ -1363,8 +1407,8 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
     CUtensorMap ma, mb;
     // slices hold only the real rows: a tile's rows past M (or N) lie outside
     // the tensor and TMA fills them with zeros without reading memory
-    GBX_TRY(encode_slices(&ma, slice_ptr(o.ra, o.sa), S, p.M, o.Kp, BM));
-    GBX_TRY(encode_slices(&mb, slice_ptr(o.rb, o.sb), S, p.N, o.Kp, bn));
+    GBX_TRY(encode_slices(&ma, slice_ptr(o.ra, o.sa), S, p.M, o.Kp, BM, o.kb));
+    GBX_TRY(encode_slices(&mb, slice_ptr(o.rb, o.sb), S, p.N, o.Kp, bn, o.kb));
     maps.push_back(ma);
     maps.push_back(mb);
   }
@@ -1396,14 +1440,15 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
   GBX_TRY(up(ssa.data(), sizeof(SplitRowSet) * ssa.size(), (void**)&sp->d_short_a));
   GBX_TRY(up(ssb.data(), sizeof(SplitRowSet) * ssb.size(), (void**)&sp->d_short_b));
   GBX_TRY(up(dp.data(), sizeof(DevProblem) * dp.size(), (void**)&sp->d_all));
-  // one launch per output tile width, plus one for the thin-K problems (bn 0)
-  for (int bn : {0, 32, 64, 128, 256}) {
+  // one launch per output tile width, plus one for the thin-K problems of
+  // each k-block (bn 0: 64, bn 1: 32)
+  for (int bn : {0, 1, 32, 64, 128, 256}) {
     std::vector<DevProblem> lp;
     std::vector<CUtensorMap> lm;
     std::vector<int> first;
     int tiles = 0;
     for (size_t i = 0; i < probs.size(); ++i) {
-      if (bn == 0 ? !sp->thin[i] : (sp->thin[i] || sp->width[i] != bn)) continue;
+      if (bn <= 1 ? sp->thin[i] != bn + 1 : (sp->thin[i] || sp->width[i] != bn)) continue;
       lp.push_back(dp[i]);
       lm.push_back(maps[2 * i]);
       lm.push_back(maps[2 * i + 1]);
@@ -1432,8 +1477,10 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
                                 (int)(sizeof(KsSmem) + 1024)));
   GBX_CUDA(cudaFuncSetAttribute(split_ks_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)(sizeof(KsSmem) + 1024)));
-  GBX_CUDA(cudaFuncSetAttribute(split_thin_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)(sizeof(ThinSmem) + 1024)));
+  GBX_CUDA(cudaFuncSetAttribute(split_thin_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(sizeof(ThinSmem<64>) + 1024)));
+  GBX_CUDA(cudaFuncSetAttribute(split_thin_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(sizeof(ThinSmem<32>) + 1024)));
   *out = sp.release();
   return GBX_OK;
 }
@@ -1490,7 +1537,8 @@ int run_split_plan(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   for (const SplitLaunch& L : sp->launches) {
-    if (L.bn == 0) {
+    if (L.total_tiles <= 0) continue;
+    if (L.bn <= 1) {
       GemmParams P;
       P.probs = L.d_probs;
       P.tile_first = L.d_tile_first;
@@ -1500,8 +1548,19 @@ int run_split_plan(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st) {
       P.S = sp->S;
       P.L = sp->L;
       P.err = sp->d_err;
-      split_thin_kernel<<<std::min(L.total_tiles, nsm), kThinThreads, sizeof(ThinSmem) + 1024, st>>>(P);
-      GBX_CUDA(cudaGetLastError());
+      if (L.bn == 0)
+        split_thin_kernel<64><<<std::min(L.total_tiles, nsm), kThinThreads, sizeof(ThinSmem<64>) + 1024, st>>>(P);
+      else
+        split_thin_kernel<32><<<std::min(L.total_tiles, nsm), kThinThreads, sizeof(ThinSmem<32>) + 1024, st>>>(P);
+      const cudaError_t le = cudaGetLastError();
+      if (le != cudaSuccess) {
+        cudaFuncAttributes fa;
+        std::memset(&fa, 0, sizeof(fa));
+        cudaFuncGetAttributes(&fa, L.bn == 0 ? (const void*)split_thin_kernel<64> : (const void*)split_thin_kernel<32>);
+        return fail(GBX_ECUDA, "thin-K launch (k-block %d): %s; dynamic smem %zu (max %d), static %zu, regs %d, max threads %d",
+                    L.bn == 0 ? 64 : 32, cudaGetErrorString(le), (L.bn == 0 ? sizeof(ThinSmem<64>) : sizeof(ThinSmem<32>)) + 1024,
+                    fa.maxDynamicSharedSizeBytes, fa.sharedSizeBytes, fa.numRegs, fa.maxThreadsPerBlock);
+      }
       continue;
     }
     switch (L.bn) {
@@ -1554,7 +1613,8 @@ double split_plan_tensor_flops(const SplitPlan* sp) {
     const SplitProblem& p = sp->host[i];
     const int bn = sp->width[i];  // thin-K problems: 32
     double Mp = (double)((p.M + BM - 1) / BM * BM), Np = (double)((p.N + bn - 1) / bn * bn);
-    double Kp = (double)((p.K + BK - 1) / BK * BK);
+    const int kb = sp->thin[i] == 2 ? 32 : BK;
+    double Kp = (double)((p.K + kb - 1) / kb * kb);
     f += 2.0 * pairs * Mp * Np * Kp;
   }
   return f;

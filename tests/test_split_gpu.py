@@ -62,10 +62,13 @@ def test_split_gemm_exact_every_tile_width(width, M, N, K):
     assert np.array_equal(C.cpu().numpy(), want)
 
 
-@pytest.mark.parametrize("M,N,K", [(5000, 8, 38), (300, 1, 1), (1000, 32, 64), (129, 17, 5)])
+@pytest.mark.parametrize("M,N,K", [(5000, 8, 38), (300, 1, 1), (1000, 32, 64), (129, 17, 5), (7000, 30, 30),
+                                   (513, 32, 32), (200, 5, 16), (300, 20, 33)])
 def test_split_gemm_thin_k_exact(M, N, K):
     """K <= 64 and N <= 32: the thin-K kernel (all slice products of a tile
-    in per-level TMEM accumulators) is exact on integer data."""
+    in per-level TMEM accumulators) is exact on integer data, with the
+    64-element k-block (K > 32) and the 32-element one (K <= 32, 64-byte
+    swizzled slices)."""
     import dtcf_gb300
     rng = np.random.default_rng(M + N + K)
     A = rng.integers(-(1 << 20), 1 << 20, size=(M, K)).astype(np.float64)
@@ -97,6 +100,21 @@ def test_split_gemm_k_stationary_exact(slices, M, N, K):
     want = (A.astype(np.int64) @ B.astype(np.int64).T).astype(np.float64)
     C = torch.zeros((M, N), dtype=torch.float64, device="cuda")
     dtcf_gb300.split_gemm(dev(A), dev(B), C, slices=slices)
+    assert np.array_equal(C.cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("K", [7, 30, 32, 33, 60])
+def test_split_gemm_thin_k_four_slices_exact(K):
+    """The thin-K kernel at 4 slices (the coupled-cluster setting) on both
+    k-blocks: exact on integers whose digits fall in the kept products."""
+    import dtcf_gb300
+    rng = np.random.default_rng(K)
+    M, N = 3000, 24
+    A = rng.integers(-(1 << 14), 1 << 14, size=(M, K)).astype(np.float64)
+    B = rng.integers(-(1 << 14), 1 << 14, size=(N, K)).astype(np.float64)
+    want = (A.astype(np.int64) @ B.astype(np.int64).T).astype(np.float64)
+    C = torch.zeros((M, N), dtype=torch.float64, device="cuda")
+    dtcf_gb300.split_gemm(dev(A), dev(B), C, slices=4)
     assert np.array_equal(C.cpu().numpy(), want)
 
 
