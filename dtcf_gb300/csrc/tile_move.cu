@@ -205,10 +205,17 @@ __global__ void __launch_bounds__(kMoveThreads) tile_move_kernel(const MoveDesc*
     double x[kPer];
 #pragma unroll
     for (int k = 0; k < kPer; ++k) x[k] = in[k] ? __ldg(s + so[k]) : 0.0;
-    if (op == 0) {
+    const unsigned long long sb = (unsigned long long)__double_as_longlong(scale);
+    if (op == 0 && (sb & 0x7FFFFFFFFFFFFFFFull) == 0x3FF0000000000000ull) {
+      // +-x: a bit copy with the sign bit set on the integer pipe
+      const long long flip = (long long)(sb & 0x8000000000000000ull);
 #pragma unroll
       for (int k = 0; k < kPer; ++k)
-        if (in[k]) t[to[k]] = (scale == 1.0) ? x[k] : __dmul_rn(scale, x[k]);
+        if (in[k]) t[to[k]] = __longlong_as_double(__double_as_longlong(x[k]) ^ flip);
+    } else if (op == 0) {
+#pragma unroll
+      for (int k = 0; k < kPer; ++k)
+        if (in[k]) t[to[k]] = __dmul_rn(scale, x[k]);
     } else {
       double y[kPer];
 #pragma unroll
@@ -243,7 +250,12 @@ __global__ void __launch_bounds__(kMoveThreads) tile_move4_kernel(const MoveDesc
     const int64_t t0 = md->dstr[0], t1 = md->dstr[1], t2 = md->dstr[2], t3 = md->dstr[3];
     const double* __restrict__ s = src + md->src;
     double* __restrict__ t = dst + md->dst;
-    const bool plain = op == 0 && scale == 1.0;
+    // stores of +-x are bit copies with the sign bit set on the integer pipe
+    // (a select between x and scale * x would issue the multiply anyway, and
+    // FP64 instructions are scarce on this part)
+    const unsigned long long sb = (unsigned long long)__double_as_longlong(scale);
+    const bool unit = op == 0 && (sb & 0x7FFFFFFFFFFFFFFFull) == 0x3FF0000000000000ull;
+    const long long flip = (long long)(sb & 0x8000000000000000ull);
 #pragma unroll 1
     for (int bt = 0; bt < kBatches; ++bt) {
       int64_t so[kPer], to[kPer];
@@ -262,10 +274,14 @@ __global__ void __launch_bounds__(kMoveThreads) tile_move4_kernel(const MoveDesc
       double x[kPer];
 #pragma unroll
       for (int k = 0; k < kPer; ++k) x[k] = in[k] ? __ldg(s + so[k]) : 0.0;
-      if (op == 0) {
+      if (unit) {
 #pragma unroll
         for (int k = 0; k < kPer; ++k)
-          if (in[k]) t[to[k]] = plain ? x[k] : __dmul_rn(scale, x[k]);
+          if (in[k]) t[to[k]] = __longlong_as_double(__double_as_longlong(x[k]) ^ flip);
+      } else if (op == 0) {
+#pragma unroll
+        for (int k = 0; k < kPer; ++k)
+          if (in[k]) t[to[k]] = __dmul_rn(scale, x[k]);
       } else {
         double y[kPer];
 #pragma unroll
