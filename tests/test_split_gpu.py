@@ -85,13 +85,15 @@ def test_split_gemm_thin_k_exact(M, N, K):
 
 
 @pytest.mark.parametrize("slices", [2, 3, 4])
-@pytest.mark.parametrize("M,N,K", [(128, 64, 64), (300, 270, 2100), (129, 33, 70), (100, 40, 40000), (257, 190, 4100)])
+@pytest.mark.parametrize("M,N,K", [(128, 64, 64), (300, 270, 2100), (129, 33, 70), (100, 40, 40000), (257, 190, 4100),
+                                   (128, 200, 40000), (70, 130, 300)])
 def test_split_gemm_k_stationary_exact(slices, M, N, K):
     """Up to 4 slices the 64-column k-stationary kernel runs (all slice
     products of a k-block from one load of each slice, exact int64 sums):
     exact on integers whose digits all fall in the kept slice products
     (|x| < 2^(8 h - 2) with h = (slices + 1) // 2 leading digits), including
-    several accumulation groups, ragged edges and a split K."""
+    several accumulation groups, ragged edges and a split K ((128, 200,
+    40000) splits K over several column tiles)."""
     import dtcf_gb300
     rng = np.random.default_rng(M + N + K + slices)
     lim = 1 << (8 * ((slices + 1) // 2) - 2)
