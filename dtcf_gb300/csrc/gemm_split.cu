@@ -977,6 +977,43 @@ __device__ __forceinline__ void locate_chunk(const SplitRowSet* __restrict__ set
   k0 = (local - row * per_row) * kSplitChunk;
 }
 
+// One element's S slices: X = the element scaled by 2^-(emax - 1022 - F +
+// 53) and rounded half up to an integer of F = 7 + 8 (S - 1) bits, cut into
+// balanced base-256 digits (the digits of |X|, with X's sign), least
+// significant in slice S - 1.  For S <= 4 (F <= 31) |X| <= 2^31 and the
+// digits come from 32-bit arithmetic: d = ((U + 128) & 255) - 128 and
+// U <- (U + 128) >> 8, since U - d = (U + 128) rounded down to a multiple of
+// 256.  Larger S keeps 64-bit arithmetic.
+__device__ __forceinline__ void write_digits(long long bits, uint32_t emax, int F, int S, __nv_bfloat16* out,
+                                             int64_t stride) {
+  const uint32_t e = (uint32_t)((bits >> 52) & 0x7FF);
+  const bool neg = bits < 0;
+  unsigned long long U = 0;
+  if (e != 0 && emax != 0) {
+    const unsigned long long mant = ((unsigned long long)bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = 53 + (int)(emax - e) - F;  // U = mant * 2^-sh, rounded half up
+    if (sh <= 0) U = mant << (-sh);
+    else if (sh < 64) U = (mant + (1ull << (sh - 1))) >> sh;
+  }
+  if (F <= 31) {
+    uint32_t u = (uint32_t)U;  // <= 2^31
+    for (int s = S - 1; s >= 1; --s) {
+      const int d = (int)((u + 128u) & 255u) - 128;
+      u = (u + 128u) >> 8;
+      out[s * stride] = __int2bfloat16_rn(neg ? -d : d);
+    }
+    out[0] = __int2bfloat16_rn(neg ? -(int)u : (int)u);
+  } else {
+    unsigned long long u = U;
+    for (int s = S - 1; s >= 1; --s) {
+      const int d = (int)((u + 128ull) & 255ull) - 128;
+      u = (u + 128ull) >> 8;
+      out[s * stride] = __int2bfloat16_rn(neg ? -d : d);
+    }
+    out[0] = __int2bfloat16_rn(neg ? -(int)u : (int)u);
+  }
+}
+
 __global__ void __launch_bounds__(256) row_exponent_kernel(const SplitRowSet* __restrict__ sets, int nsets,
                                                            int64_t total_chunks) {
   __shared__ uint32_t red[8];
@@ -1015,25 +1052,8 @@ __global__ void __launch_bounds__(256) digits_kernel(const SplitRowSet* __restri
     __nv_bfloat16* dst = rs.dst + row * rs.Kp;
     const uint32_t emax = (uint32_t)rs.exps[row];
     const int64_t k1 = min(rs.K, k0 + kSplitChunk);
-    for (int64_t k = k0 + threadIdx.x; k < k1; k += 256) {
-      const long long bits = __double_as_longlong(__ldg(src + k));
-      const uint32_t e = (uint32_t)((bits >> 52) & 0x7FF);
-      long long X = 0;
-      if (e != 0 && emax != 0) {
-        const long long mant = (bits & 0xFFFFFFFFFFFFFll) | (1ll << 52);
-        const int sh = 53 + (int)(emax - e) - F;  // X = mant * 2^-sh, rounded half up
-        if (sh <= 0) X = mant << (-sh);
-        else if (sh < 63) X = (mant + (1ll << (sh - 1))) >> sh;
-        if (bits < 0) X = -X;
-      }
-      // balanced base-256 digits, least significant first
-      for (int s = S - 1; s >= 1; --s) {
-        const long long d = ((X + 128) & 255) - 128;
-        X = (X - d) >> 8;
-        dst[s * rs.slice_stride + k] = __int2bfloat16_rn((int)d);
-      }
-      dst[k] = __int2bfloat16_rn((int)X);
-    }
+    for (int64_t k = k0 + threadIdx.x; k < k1; k += 256)
+      write_digits(__double_as_longlong(__ldg(src + k)), emax, F, S, dst + k, rs.slice_stride);
     // the row's last chunk also clears its K padding (the slice buffers may be
     // an arena shared with other plans, so nothing else keeps it zero)
     if (k1 == rs.K)
@@ -1063,24 +1083,8 @@ __global__ void __launch_bounds__(256) split_short_rows_kernel(const SplitRowSet
     for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
     if (lane == 0) rs.exps[row] = (int)emax;
     __nv_bfloat16* dst = rs.dst + row * rs.Kp;
-    for (int64_t k = lane; k < rs.K; k += 32) {
-      const long long bits = __double_as_longlong(__ldg(src + k));
-      const uint32_t e = (uint32_t)((bits >> 52) & 0x7FF);
-      long long X = 0;
-      if (e != 0 && emax != 0) {
-        const long long mant = (bits & 0xFFFFFFFFFFFFFll) | (1ll << 52);
-        const int sh = 53 + (int)(emax - e) - F;
-        if (sh <= 0) X = mant << (-sh);
-        else if (sh < 63) X = (mant + (1ll << (sh - 1))) >> sh;
-        if (bits < 0) X = -X;
-      }
-      for (int s = S - 1; s >= 1; --s) {
-        const long long d = ((X + 128) & 255) - 128;
-        X = (X - d) >> 8;
-        dst[s * rs.slice_stride + k] = __int2bfloat16_rn((int)d);
-      }
-      dst[k] = __int2bfloat16_rn((int)X);
-    }
+    for (int64_t k = lane; k < rs.K; k += 32)
+      write_digits(__double_as_longlong(__ldg(src + k)), emax, F, S, dst + k, rs.slice_stride);
     for (int64_t k = rs.K + lane; k < rs.Kp; k += 32)
       for (int s = 0; s < S; ++s) dst[s * rs.slice_stride + k] = __int2bfloat16_rn(0);
   }
