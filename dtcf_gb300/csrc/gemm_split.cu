@@ -1281,14 +1281,18 @@ int split_layout(const std::vector<SplitProblem>& probs, int S, bool static_a, b
     const int nkb = (int)(o.Kp / o.kb);
     if (nkb < 1) return fail(GBX_EINVAL, "split problem without a k-block");
     // split K when the output tiles of all problems leave SMs idle; ranges are
-    // whole exact-accumulation chunks
+    // whole exact-accumulation chunks: 16 k-blocks for the pair-by-pair
+    // kernel, 16 / S for the k-stationary one (whose exact groups are that
+    // short, so few-tile problems -- matrix-vector shapes, small outputs with
+    // long K -- spread over many more CTAs instead of walking K serially)
+    const int chunk = (!o.thin && S <= kKsMaxS && o.bn == kKsBN) ? 16 / S : kChunkKb;
     int ks = 1;
-    if (!o.thin && out_tiles < kSplitFill && nkb > 2 * kChunkKb) {
+    if (!o.thin && out_tiles < kSplitFill && nkb > 2 * chunk) {
       int want = (int)((kSplitFill + out_tiles - 1) / out_tiles);
-      ks = std::max(1, std::min(want, nkb / kChunkKb));
+      ks = std::max(1, std::min(want, nkb / chunk));
     }
     int per = (nkb + ks - 1) / ks;
-    per = (per + kChunkKb - 1) / kChunkKb * kChunkKb;
+    per = (per + chunk - 1) / chunk * chunk;
     ks = (nkb + per - 1) / per;
     o.ks = ks;
     o.per = per;
