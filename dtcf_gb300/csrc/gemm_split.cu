@@ -738,9 +738,12 @@ __global__ void __launch_bounds__(kKsThreads, 1) split_ks_kernel(const GemmParam
   constexpr int L = S - 1;
   constexpr int D = 16 / S;  // k-blocks per exact accumulation group
   constexpr uint32_t kTx = (BM + kKsBN) * BK * 2;
+  // a stage is one k-block's S slot pairs behind one full and one empty
+  // barrier: one wait and one commit per k-block for the MMA-issuing thread
+  constexpr int kStages = kKsSlots / S;
   constexpr uint32_t kCols = 512;
   if (threadIdx.x == 0) {
-    for (int i = 0; i < kKsSlots; ++i) {
+    for (int i = 0; i < kStages; ++i) {
       mbar_init(&sm.full[i], 1);
       mbar_init(&sm.empty[i], 1);
     }
@@ -765,35 +768,37 @@ __global__ void __launch_bounds__(kKsThreads, 1) split_ks_kernel(const GemmParam
   if (warp == 0) {
     // ---------------- TMA producer: a k-block's S slice pairs ----------------
     if (lane == 0) {
-      int slot = 0;
+      int st = 0;
       uint32_t phase = 0;
       bool ok = true;
       for (int tile = blockIdx.x; tile < P.total_tiles && ok; tile += gridDim.x) {
         const TileInfo ti = decode_tile<kKsBN>(P, tile);
         const CUtensorMap* ma = P.maps + 2 * ti.p;
         const CUtensorMap* mb = P.maps + 2 * ti.p + 1;
-        for (int kb = ti.kb0; kb < ti.kb0 + ti.nkb && ok; ++kb)
-          for (int s = 0; s < S; ++s) {
-            if (!mbar_wait(&sm.empty[slot], phase ^ 1, P.err, 21)) {
-              ok = false;
-              break;
-            }
-            mbar_expect_tx(&sm.full[slot], kTx);
-            tma_load_3d(sm.a[slot], ma, &sm.full[slot], kb * BK, ti.m0, s);
-            tma_load_3d(sm.b[slot], mb, &sm.full[slot], kb * BK, ti.n0, s);
-            if (++slot == kKsSlots) {
-              slot = 0;
-              phase ^= 1;
-            }
+        for (int kb = ti.kb0; kb < ti.kb0 + ti.nkb && ok; ++kb) {
+          if (!mbar_wait(&sm.empty[st], phase ^ 1, P.err, 21)) {
+            ok = false;
+            break;
           }
+          mbar_expect_tx(&sm.full[st], (uint32_t)S * kTx);
+#pragma unroll
+          for (int s = 0; s < S; ++s) {
+            tma_load_3d(sm.a[st * S + s], ma, &sm.full[st], kb * BK, ti.m0, s);
+            tma_load_3d(sm.b[st * S + s], mb, &sm.full[st], kb * BK, ti.n0, s);
+          }
+          if (++st == kStages) {
+            st = 0;
+            phase ^= 1;
+          }
+        }
       }
-      for (int i = 0; i < kKsSlots; ++i) {
-        if (--slot < 0) {
-          slot = kKsSlots - 1;
+      for (int i = 0; i < kStages; ++i) {
+        if (--st < 0) {
+          st = kStages - 1;
           phase ^= 1;
         }
         long long t0 = clock64();
-        while (!mbar_try_wait(&sm.full[slot], phase) && !mbar_try_wait(&sm.empty[slot], phase)) {
+        while (!mbar_try_wait(&sm.full[st], phase) && !mbar_try_wait(&sm.empty[st], phase)) {
           if (clock64() - t0 > kWaitCycles) {
             atomicCAS(P.err, 0, 25);
             break;
@@ -804,7 +809,7 @@ __global__ void __launch_bounds__(kKsThreads, 1) split_ks_kernel(const GemmParam
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
-      int slot = 0, buf = 0;
+      int st = 0, buf = 0;
       uint32_t phase = 0, aphase = 0;
       bool ok = true;
       constexpr uint32_t idesc = idesc_bf16<kKsBN>();
@@ -822,21 +827,12 @@ __global__ void __launch_bounds__(kKsThreads, 1) split_ks_kernel(const GemmParam
           tc_fence_after();
           const int g1 = min(nkb, g0 + D);
           for (int kb = g0; kb < g1 && ok; ++kb) {
-            int sl[S];
-#pragma unroll
-            for (int s = 0; s < S; ++s) {
-              sl[s] = slot;
-              if (!mbar_wait(&sm.full[slot], phase, P.err, 23)) {
-                ok = false;
-                break;
-              }
-              if (++slot == kKsSlots) {
-                slot = 0;
-                phase ^= 1;
-              }
+            if (!mbar_wait(&sm.full[st], phase, P.err, 23)) {
+              ok = false;
+              break;
             }
-            if (!ok) break;
             tc_fence_after();
+            const int base = st * S;
             const uint32_t fresh = kb == g0 ? 0u : 1u;
 #pragma unroll
             for (int l = 0; l <= L; ++l) {
@@ -844,16 +840,19 @@ __global__ void __launch_bounds__(kKsThreads, 1) split_ks_kernel(const GemmParam
 #pragma unroll
               for (int s = (l + 2 - S > 1 ? l + 2 - S : 1); s <= (S < l + 1 ? S : l + 1); ++s) {
                 const int t = l + 2 - s;
-                const uint64_t a0 = ad0 + (uint64_t)sl[s - 1] * kAStep;
-                const uint64_t b0 = bd0 + (uint64_t)sl[t - 1] * kBStep;
+                const uint64_t a0 = ad0 + (uint64_t)(base + s - 1) * kAStep;
+                const uint64_t b0 = bd0 + (uint64_t)(base + t - 1) * kBStep;
                 const bool lead = s == (l + 2 - S > 1 ? l + 2 - S : 1);  // first product of the level
 #pragma unroll
                 for (int k = 0; k < BK / 16; ++k)
                   umma(d, a0 + (uint64_t)(k * 2), b0 + (uint64_t)(k * 2), idesc, (lead && k == 0) ? fresh : 1u);
               }
             }
-#pragma unroll
-            for (int s = 0; s < S; ++s) umma_commit(&sm.empty[sl[s]]);
+            umma_commit(&sm.empty[st]);
+            if (++st == kStages) {
+              st = 0;
+              phase ^= 1;
+            }
           }
           if (!ok) break;
           umma_commit(&sm.accfull[buf]);
