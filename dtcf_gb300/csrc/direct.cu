@@ -12,7 +12,7 @@
 namespace gbx {
 
 namespace {
-constexpr int kDirThreads = 256;
+constexpr int kDirThreads = 512;
 constexpr int kDirPer = kDirItemElems / kDirThreads;
 static_assert(kDirPer * kDirThreads == kDirItemElems, "item size");
 }  // namespace
