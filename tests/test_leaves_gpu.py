@@ -181,6 +181,24 @@ def test_rrr_plan_cntr4a_shape(gbx):
     assert ctr.plan("a,b,k,l", "m,n,k,l", "a,b,m,n").flops == 2.0 * n ** 6
 
 
+@pytest.mark.parametrize("mode", ["fp64", "split"])
+@pytest.mark.parametrize("sign", [1, -1])
+def test_rrr_plan_direct_engine(gbx, mode, sign):
+    """C[a,b,i,j] += 0.5 sum_m A[a,b,i,m] B[m,j] with a contracted extent of 4
+    per output element: the planner runs it on the direct FP64 kernel (no
+    packing) in either mode; A and C keep unique (a, b) blocks, so reads go
+    through the symmetric / antisymmetric un-flip with its sign."""
+    from dtcf_gb300.rrr import Contraction
+    o, v, m, blk = 8, 12, 4, 4
+    A, B, C = _rrr_case("aabc", "ab", "aabc", [(v, v, o, m), (m, o), (v, v, o, o)],
+                        [(v // blk, v // blk, o // blk, m // blk), (m // blk, o // blk),
+                         (v // blk, v // blk, o // blk, o // blk)], 31)
+    want = oracle.rrr.contract(_as_oracle(A), _as_oracle(B), _as_oracle(C), "a,b,i,m", "m,j", "a,b,i,j", 0.5, sign)
+    Contraction(A, B, C, mode=mode, sign=sign).contract("a,b,i,m", "m,j", "a,b,i,j", 0.5)
+    got = host(C.tiles).reshape(want.shape)
+    assert np.max(np.abs(got - want)) <= 1e-13 * max(1.0, np.abs(want).max())
+
+
 @pytest.mark.parametrize("sign", [1, -1])
 def test_rrr_plan_split_engine(gbx, sign):
     """The same unique-block ladder on the split-precision engine (6 slices):
