@@ -77,16 +77,68 @@ def workload(a):
 
 
 class Clocks:
-    """nvidia-smi sampler started before and stopped after the timed region."""
+    """SM clock and clock-event reasons sampled during the timed region.
+
+    Read-only NVML queries through ctypes (libnvidia-ml ships with the
+    driver), polled every 5 ms by a thread, on the GPU this process runs on
+    (matched by PCI bus id, since NVML numbers every GPU of the machine);
+    nvidia-smi every 200 ms when NVML cannot be loaded."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
+    REASONS = [(0x4, "sw_power_cap"), (0x8, "hw_slowdown"), (0x20, "sw_thermal_slowdown"),
+               (0x40, "hw_thermal_slowdown"), (0x80, "hw_power_brake_slowdown")]
 
     def __init__(self, index):
         self.index = index
         self.proc = None
+        self.thread = None
+        self.samples = []
+        self.reasons = set()
+        self.smax = None
+
+    def _nvml(self):
+        import ctypes
+        import threading
+        import torch
+        nv = ctypes.CDLL("libnvidia-ml.so.1")
+        if nv.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        bus = ctypes.create_string_buffer(64)
+        cudart_bus = torch.cuda.get_device_properties(torch.cuda.current_device())
+        pci = "%08X:%02X:%02X.0" % (getattr(cudart_bus, "pci_domain_id", 0), cudart_bus.pci_bus_id,
+                                    cudart_bus.pci_device_id)
+        bus.value = pci.encode()
+        dev = ctypes.c_void_p()
+        if nv.nvmlDeviceGetHandleByPciBusId_v2(bus, ctypes.byref(dev)) != 0:
+            raise OSError("no NVML device for " + pci)
+        mx = ctypes.c_uint()
+        if nv.nvmlDeviceGetMaxClockInfo(dev, 1, ctypes.byref(mx)) == 0:  # NVML_CLOCK_SM
+            self.smax = float(mx.value)
+        get_reasons = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        self.stop_flag = threading.Event()
+
+        def poll():
+            clk, rs = ctypes.c_uint(), ctypes.c_ulonglong()
+            while not self.stop_flag.is_set():
+                if nv.nvmlDeviceGetClockInfo(dev, 1, ctypes.byref(clk)) == 0:
+                    self.samples.append(float(clk.value))
+                if get_reasons(dev, ctypes.byref(rs)) == 0:
+                    for bit, name in self.REASONS:
+                        if rs.value & bit:
+                            self.reasons.add(name)
+                time.sleep(0.005)
+        self.thread = threading.Thread(target=poll, daemon=True)
+        self.thread.start()
+        time.sleep(0.02)  # the first samples precede the timed region by a few ms
 
     def start(self):
+        try:
+            self._nvml()
+            return
+        except (OSError, AttributeError, ValueError):
+            self.thread = None
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -95,6 +147,12 @@ class Clocks:
             self.proc = None
 
     def stop(self):
+        if self.thread is not None:
+            self.stop_flag.set()
+            self.thread.join(timeout=5)
+            sm = sorted(self.samples)
+            return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": self.smax,
+                    "reasons": sorted(self.reasons), "samples": len(sm), "source": "nvml"}
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -114,7 +172,7 @@ class Clocks:
                     reasons.add(name)
         sm.sort()
         return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvidia-smi"}
 
 
 def dist_setup():
