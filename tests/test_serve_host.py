@@ -29,6 +29,25 @@ def test_footprint_is_host_only_and_monotone():
     assert sym[0] < big[0] and sym[2] < big[2]
 
 
+@pytest.mark.parametrize("method", ["ccd", "ccsd"])
+@pytest.mark.parametrize("engine", ["fp64", "split"])
+@pytest.mark.parametrize("nocc,nvir,nirrep,max_block,min_block", [
+    (4, 64, 1, 64, 1),     # 64 x 64 (a, b) slabs: fused-sum items cover half slabs
+    (6, 14, 2, 5, 1),      # ragged blocks, two irreps
+    (8, 24, 4, 4, 1),      # blocks of 1..4 orbitals
+    (16, 48, 8, 6, 1),     # eight irreps, uneven occupations
+    (24, 120, 8, 40, 4),   # the bench system's blocking at a smaller size
+])
+def test_host_planning_of_every_step(method, engine, nocc, nvir, nirrep, max_block, min_block):
+    """Every step of an iteration -- contraction plans on the packed or the
+    direct engine, the fused permuted sums, the tau-family tile table -- is
+    planned on the host (no device) for a range of blockings, and the peak
+    covers the resident bytes."""
+    r, p, f = footprint(nocc=nocc, nvir=nvir, nirrep=nirrep, max_block=max_block, min_block=min_block,
+                        method=method, engine=engine, slices=4)
+    assert 0 < r <= p and f > 0
+
+
 def test_server_records_footprints_and_validates_requests():
     s = Server(budget_bytes=1e9, slots=2)
     j = s.add_job(config(nocc=8, nvir=32, nirrep=1, max_block=8, method="ccd", engine="fp64"))
