@@ -85,7 +85,6 @@ struct gbx_cc_job {
   CCDeviceTables tab;
   std::map<std::string, std::unique_ptr<CCTensor>> T;
   std::vector<std::unique_ptr<ContractionPlan>> cplans;
-  std::vector<std::unique_ptr<SumPlan>> splans;
   std::vector<std::unique_ptr<FusedSumPlan>> fplans;
   // tau / taut / Q from t2 and t1 (CCSD): per-tile t1 offsets and work items
   std::vector<CCAmpTile> amp_tiles;
@@ -124,7 +123,6 @@ struct gbx_cc_job {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     cplans.clear();
-    splans.clear();
     fplans.clear();
     amp.release();
     T.clear();
@@ -208,24 +206,6 @@ struct gbx_cc_job {
     cplans.push_back(std::move(p));
     plan_operands.push_back({A, B});
     plan_outputs.push_back(C);
-    return GBX_OK;
-  }
-
-  // C[lc] += coef * A[la]
-  int sum(const char* c, const char* lc, const char* a, const char* la, double coef) {
-    CCTensor *C = get(c), *A = get(a);
-    GBX_TRY(check_labels(C, lc, c));
-    GBX_TRY(check_labels(A, la, a));
-    std::unique_ptr<SumPlan> p;
-    GBX_TRY(plan_sum(A->L, C->L, labels(la), labels(lc), coef, p, /*defer=*/true));
-    SumPlan* pp = p.get();
-    dynamic_use.insert(a);
-    dynamic_use.insert(c);
-    steps.push_back([=](cudaStream_t st) { return pp->execute(A->d, C->d, 1.0, st); });
-    info.push_back({std::string(c) + "[" + lc + "]+=" + a + "[" + la + "]", 1, 0.0,
-                    8.0 * (double)(A->L.nelem + 2 * C->L.nelem)});
-    launches += 1;
-    splans.push_back(std::move(p));
     return GBX_OK;
   }
 
@@ -574,7 +554,6 @@ int gbx_cc_job::footprint(double* resident, double* peak) const {
     ws = std::max(ws, (double)w);
     scratch = std::max(scratch, (double)sc);
   }
-  for (auto& p : splans) keep += (double)p->moves.device_bytes();
   for (auto& p : fplans) keep += up256d((double)(p->items.size() * sizeof(FsItem))) + up256d((double)(p->terms.size() * sizeof(FsTerm)));
   keep += up256d((double)(amp_tiles.size() * sizeof(CCAmpTile))) + up256d((double)(amp_items.size() * sizeof(CCAmpItem)));
   auto tiles_bytes = [](const TensorLayout& L) {
@@ -650,7 +629,6 @@ int gbx_cc_job::materialize(cudaStream_t st) {
   }
   unsigned char* d_scratch = nullptr;
   if (scratch_bytes) GBX_TRY(dev_alloc((void**)&d_scratch, scratch_bytes));
-  for (auto& p : splans) GBX_TRY(p->moves.upload());
   for (auto& p : fplans) GBX_TRY(p->upload());
   if (!amp_items.empty()) GBX_TRY(amp.upload(amp_tiles, amp_items));
   for (size_t i = 0; i < cplans.size(); ++i) {
@@ -836,7 +814,7 @@ int gbx_cc_stats_get(const gbx_cc_job* job, gbx_cc_stats* s) {
   s->gemm_flops_per_iter = job->gemm_flops;
   s->resident_bytes = (double)job->account.load();
   s->ncontractions = (int)job->cplans.size() - job->iter_plan_begin;
-  s->nsums = (int)job->splans.size();
+  s->nsums = (int)job->fplans.size();
   s->nblocks_occ = (int)job->occ->ext.size();
   s->nblocks_vir = (int)job->vir->ext.size();
   s->launches_per_iter = job->launches;

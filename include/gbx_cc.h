@@ -42,7 +42,9 @@ typedef struct {
     double flops_per_iter;       /* algorithmic FP64 flops of one iteration (nonzero block triples) */
     double gemm_flops_per_iter;  /* flops the packed GEMMs execute */
     double resident_bytes;       /* device bytes held by the job (tensors + plans) */
-    int ncontractions, nsums, nblocks_occ, nblocks_vir;
+    int ncontractions;           /* contraction plans of one iteration */
+    int nsums;                   /* fused summation steps of one iteration */
+    int nblocks_occ, nblocks_vir;
     int launches_per_iter;       /* kernels launched by one iteration */
 } gbx_cc_stats;
 
