@@ -817,7 +817,22 @@ int gbx_cc_stats_get(const gbx_cc_job* job, gbx_cc_stats* s) {
   s->nsums = (int)job->fplans.size();
   s->nblocks_occ = (int)job->occ->ext.size();
   s->nblocks_vir = (int)job->vir->ext.size();
+  // once the iteration is captured, its kernel nodes; before, the planned count
   s->launches_per_iter = job->launches;
+  if (job->graph) {
+    size_t n = 0;
+    if (cudaGraphGetNodes(job->graph, nullptr, &n) == cudaSuccess && n > 0) {
+      std::vector<cudaGraphNode_t> nodes(n);
+      if (cudaGraphGetNodes(job->graph, nodes.data(), &n) == cudaSuccess) {
+        int kernels = 0;
+        for (size_t i = 0; i < n; ++i) {
+          cudaGraphNodeType t;
+          if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++kernels;
+        }
+        s->launches_per_iter = kernels;
+      }
+    }
+  }
   return GBX_OK;
 }
 

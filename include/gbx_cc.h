@@ -45,7 +45,8 @@ typedef struct {
     int ncontractions;           /* contraction plans of one iteration */
     int nsums;                   /* fused summation steps of one iteration */
     int nblocks_occ, nblocks_vir;
-    int launches_per_iter;       /* kernels launched by one iteration */
+    int launches_per_iter;       /* kernels of one iteration: the captured graph's kernel nodes once it
+                                    exists, the planned count before */
 } gbx_cc_stats;
 
 typedef struct gbx_cc_job gbx_cc_job;
