@@ -51,7 +51,6 @@ def parse():
                    help="time one split GEMM alone: 'ladder' = one irrep block of the canonical-tile "
                         "<ab||ef> ladder of this workload (3600 x 144 x 7200); 'thin' = one irrep block of t_i^e <ab||ej> "
                         "(346174 x 8 x 38, the thin-K kernel)")
-    p.add_argument("--rates", action="store_true", help="build and run the arithmetic-rate probe")
     p.add_argument("--grouped", type=int, default=0, metavar="T",
                    help="grouped block-triple sweep instead of CCSD: T triples, m, n, k log-uniform in [8, 256], "
                         "entries sign * 10^u, u uniform in [-6, 6]; FP64 per-triple launches vs one persistent "
@@ -387,19 +386,9 @@ def serve_arm(a):
     return 0
 
 
-def rates_arm():
-    import tempfile
-    src = os.path.join(ROOT, "dtcf_gb300", "measure", "rates_probe.cu")
-    exe = os.path.join(tempfile.mkdtemp(), "rates_probe")
-    subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-o", exe, src], check=True)
-    return subprocess.run([exe]).returncode
-
-
 def main():
     a = parse()
     world, rank, local = dist_setup()
-    if a.rates:
-        return rates_arm()
     if a.kernel:
         return kernel_arm(a)
     if a.grouped:
@@ -497,33 +486,30 @@ def main():
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except (OSError, ValueError):
         pass
+    extra = {}
     if kt["engine"] == 1:
-        # tensor-pipe work of the slice products against the measured bf16 peak
-        peak, src = peaks.get("bf16_tflops", 1900.0), "of measured (MEASURED_PEAKS.json bf16_tflops, burst)"
-        achieved = kt["tensor_flops"] / (kt["ms"] * 1e-3) / 1e12
+        # tensor-pipe work of the slice products against the measured bf16 peak,
+        # credited with the real (unpadded) slice products: S(S+1)/2 bf16
+        # GEMMs of the packed shapes; the padded work the kernel issues is
+        # reported beside it
         pi = P["job"].plan_info(top["plan"])
-        w = pi["split_width"] or (64 if pi["slices"] <= 4 else 0)
-        kname = ("split_ks_kernel (tcgen05 bf16 slices, k-stationary, 64 columns)" if w == 64 and pi["slices"] <= 4
+        S = pi["slices"]
+        real = S * (S + 1) / 2 * kt["fp64_flops"]
+        peak, src = peaks.get("bf16_tflops", 1900.0), "of measured (MEASURED_PEAKS.json bf16_tflops, burst)"
+        achieved = real / (kt["ms"] * 1e-3) / 1e12
+        extra = {"slice_products": S * (S + 1) // 2, "padding_ratio": kt["tensor_flops"] / real,
+                 "issued_tflops_padded": kt["tensor_flops"] / (kt["ms"] * 1e-3) / 1e12}
+        w = pi["split_width"] or (64 if S <= 4 else 0)
+        kname = ("split_ks_kernel (tcgen05 bf16 slices, k-stationary, 64 columns)" if w == 64 and S <= 4
                  else "split_gemm_kernel<%s> (tcgen05 bf16 slices)" % (w or "model width"))
     else:
-        # FP64 tensor-pipe ceiling measured on this GPU (DMMA m8n8k4 throughput probe)
-        peak, src = 1.05, "of measured DMMA probe (profiles/)"
+        # FP64 pipe: nominal dense FP64 rate of the part (DMMA runs no faster than FP64 FMA on it)
+        peak, src = 1.25, "of nominal FP64 (1.25 TFLOP/s)"
         achieved = kt["fp64_flops"] / (kt["ms"] * 1e-3) / 1e12
         kname = "grouped_gemm_f64_kernel (DMMA)"
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                 "traffic": None, "kernel": kname, "contraction": top["name"], "kernel_ms": kt["ms"],
-                "fp64_equiv_tflops": kt["fp64_flops"] / (kt["ms"] * 1e-3) / 1e12, "peak_source": src}
-    # DRAM traffic of the ladder launch from the committed ncu summary of one of
-    # its irrep blocks (scaled by the 8 blocks), when this is that workload
-    prof_md = os.path.join(ROOT, "profiles", "split_ks_kernel_ladder_3600x144x7200.md")
-    if (top["name"].startswith("Lad[ijab]+=VVVV") and "split_ks_kernel" in kname and os.path.exists(prof_md)
-            and (a.nocc, a.nvir, a.nirrep, a.max_block, a.min_block, a.seed, a.slices) == (48, 240, 8, 40, 4, 1, 4)):
-        for ln in open(prof_md):
-            if ln.startswith("traffic_bytes_per_ladder_launch:"):
-                roofline["traffic"] = float(ln.split(":")[1].split()[0])
-                roofline["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one irrep block x 8 "
-                                              "(profiles/split_ks_kernel_ladder_3600x144x7200.md)")
-
+                "fp64_equiv_tflops": kt["fp64_flops"] / (kt["ms"] * 1e-3) / 1e12, "peak_source": src, **extra}
     # end to end through the public API with host buffers: every step copies the
     # amplitudes in from pinned host memory and reads the energy back
     job = P["job"]

@@ -42,6 +42,7 @@ SIGNATURES = {
     "gbx_server_destroy": (_i, [_p]),
     "gbx_split_gemm": (_i, [_p, _p, _p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, _i, _p]),
     "gbx_split_set_width": (_i, [_i]),
+    "gbx_wait_selftest": (_i, [ctypes.c_longlong, _p]),
     "gbx_cc_default_config": (None, [_p]),
     "gbx_cc_footprint": (_i, [_p, ctypes.POINTER(_d), ctypes.POINTER(_d), ctypes.POINTER(_d)]),
     "gbx_cc_capture": (_i, [_p]),

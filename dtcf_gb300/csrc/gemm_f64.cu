@@ -647,9 +647,10 @@ int F64Gemm::run_each(cudaStream_t st) const {
 // same FP64 GEMM with its descriptor and split-K partial sums in one
 // file-scope device array of kNoAllocBytes, which every GPU that loads the
 // library holds until the process exits.  What must start at zero: the
-// work-queue ticket, written (with the whole descriptor) by every call before
-// its kernels run.  The partial-sum slabs need no clearing: every split-K
-// range overwrites its slab in full before the reduction reads it.
+// work-queue ticket, written (with the whole descriptor, by a one-thread
+// kernel on the caller's stream) by every call before its GEMM runs.  The
+// partial-sum slabs need no clearing: every split-K range overwrites its slab
+// in full before the reduction reads it.
 namespace gbx {
 namespace {
 constexpr size_t kNoAllocHeader = 4096;                   // descriptor, schedule words
@@ -668,6 +669,12 @@ static_assert(sizeof(NoAllocHeader) <= kNoAllocHeader, "header does not fit");
 }  // namespace
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+// Writes the call's descriptor (ticket 0 included) into the scratch array
+// ahead of the GEMM on the same stream: the descriptor travels as a kernel
+// argument, so the call needs no host staging buffer and never waits for the
+// stream.
+__global__ void noalloc_header_kernel(NoAllocHeader h, NoAllocHeader* dst) { *dst = h; }
 
 // Device address of the scratch array, looked up once per device (the host
 // symbol is only a stand-in for it).
@@ -738,8 +745,9 @@ extern "C" int gbx_local_contraction_noalloc(int n_a, int n_b, int n_k, const do
   h.red_prob = 0;
   h.red_first = 0;
   NoAllocHeader* dh = (NoAllocHeader*)scratch;
-  // the header is staged from host memory on the stream; the ticket starts at 0
-  GBX_CUDA(cudaMemcpyAsync(dh, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+  // the descriptor is written on the stream by a one-thread kernel; the ticket starts at 0
+  noalloc_header_kernel<<<1, 1, 0, st>>>(h, dh);
+  GBX_CUDA(cudaGetLastError());
   int tiles;
   if (variant == 4) tiles = (n_a + 255) / 256;
   else if (variant == 5) tiles = (n_b + 255) / 256;

@@ -106,11 +106,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // Bounded wait; false (and the error word set) when it ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code,
+                                          long long limit = kWaitCycles) {
   if (mbar_try_wait(bar, parity)) return true;
   long long t0 = clock64();
   while (!mbar_try_wait(bar, parity)) {
-    if (clock64() - t0 > kWaitCycles) {
+    if (clock64() - t0 > limit) {
       atomicCAS(err, 0, code);
       return false;
     }
@@ -1637,4 +1638,42 @@ int split_set_width(int bn) {
 
 double split_plan_bytes(const SplitPlan* sp) { return sp ? sp->bytes : 0.0; }
 
+// ---- self-test of the bounded waits ---------------------------------------
+// One CTA waits on an mbarrier that nothing arrives on, through the same
+// bounded wait as the split kernels' pipeline waits; it gives up after the
+// limit, records its stage in the error word and returns.
+namespace {
+constexpr int kSelftestStage = 31;
+__device__ int g_wait_selftest_err;
+
+__global__ void wait_selftest_reset_kernel() { g_wait_selftest_err = 0; }
+
+__global__ void wait_selftest_kernel(long long limit) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) mbar_wait(&bar, 0, &g_wait_selftest_err, kSelftestStage, limit);
+  __syncthreads();
+}
+}  // namespace
+
 }  // namespace gbx
+
+extern "C" int gbx_wait_selftest(long long limit_cycles, void* stream) {
+  using namespace gbx;
+  if (limit_cycles < 0 || limit_cycles > kWaitCycles)
+    return fail(GBX_EINVAL, "limit_cycles %lld outside [0, %lld]", limit_cycles, (long long)kWaitCycles);
+  cudaStream_t st = (cudaStream_t)stream;
+  wait_selftest_reset_kernel<<<1, 1, 0, st>>>();
+  GBX_CUDA(cudaGetLastError());
+  wait_selftest_kernel<<<1, 32, 0, st>>>(limit_cycles);
+  GBX_CUDA(cudaGetLastError());
+  GBX_CUDA(cudaStreamSynchronize(st));
+  int e = 0;
+  GBX_CUDA(cudaMemcpyFromSymbol(&e, g_wait_selftest_err, sizeof(int)));
+  if (e != 0) return fail(GBX_ETIMEOUT, "a bounded device wait ran out (stage %d)", e);
+  return GBX_OK;
+}

@@ -169,6 +169,16 @@ GBX_API int gbx_plan_destroy(gbx_plan* plan);
 GBX_API int gbx_split_gemm(const double* d_A, const double* d_B, double* d_C, int64_t M, int64_t N, int64_t K,
                            int slices, void* stream);
 
+/* Self-test of the bounded device waits of the split engine's kernels: one
+ * CTA waits, through the same bounded mbarrier wait as the split GEMM
+ * pipelines, on a barrier that nothing arrives on, gives up after
+ * limit_cycles SM clocks (0 .. about one second's worth), records the wait's
+ * stage (31) in its error word and returns.  The call waits for the stream and
+ * returns GBX_ETIMEOUT with the same message as a split GEMM whose wait ran
+ * out; the CUDA context stays usable.  No counterpart in the reference (its
+ * waits are blocking MPI calls). */
+GBX_API int gbx_wait_selftest(long long limit_cycles, void* stream);
+
 /* Tuning knob of the split engine: output tile width (32, 64, 128 or 256
  * columns) for plans created after the call; 0 restores the built-in
  * throughput model.  Process-wide; used by the autotuner. */

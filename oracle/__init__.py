@@ -27,12 +27,17 @@ _p = ctypes.c_void_p
 
 
 def build(ref=True):
-    """Compile liboracle.so, and oracle/_ref/libref.so when the reference tree exists."""
+    """Compile liboracle.so, and oracle/_ref/libref.so when the reference tree
+    exists.  The tree's location is the Makefile's REF (DTCF_REFERENCE, when
+    set, overrides it); `make ref` reports a missing tree and builds nothing."""
     subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
-    if ref and os.path.isdir(os.environ.get("DTCF_REFERENCE", "/root/reference")):
+    if ref:
         env = dict(os.environ)
-        env.setdefault("REF", os.environ.get("DTCF_REFERENCE", "/root/reference"))
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True, env=env)
+        if "DTCF_REFERENCE" in env:
+            env["REF"] = env["DTCF_REFERENCE"]
+        probe = subprocess.run(["make", "-s", "-C", HERE, "ref-present"], env=env, capture_output=True, text=True)
+        if probe.returncode == 0:
+            subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True, env=env)
 
 
 def lib():

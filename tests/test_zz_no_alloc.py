@@ -1,5 +1,6 @@
 """The allocation-free entry point gbx_local_contraction_noalloc, called
-through the C ABI, against gbx_local_contraction on the same inputs.
+through the C ABI, against gbx_local_contraction on the same inputs and
+against the oracle's corrected local_contraction.
 
 It serves callers that cannot let a library allocate device memory (a
 framework that handed the GPU's memory to its own pool, or a latency-bound
@@ -14,14 +15,19 @@ import numpy as np
 import pytest
 import torch
 
+import oracle
+
 pytestmark = pytest.mark.gpu
 
 SHAPES = [
     (40, 30, 20000, 0, 1),   # small output, long K: split-K partials in the workspace
     (200, 150, 700, 0, 1),
-    (5000, 6, 30, 0, 0),     # thin output
+    (5000, 6, 30, 0, 0),     # thin output, one thread per row
     (130, 70, 64, 1, 1),
     (64, 64, 4096, 1, 0),
+    (6, 5000, 30, 0, 1),     # thin output, one thread per column
+    (300, 200, 4, 1, 0),     # K <= 8: one thread per output element
+    (50, 40, 0, 0, 0),       # K = 0: C unchanged
 ]
 
 
@@ -40,14 +46,20 @@ def test_noalloc_matches_allocating_entry_point_twice(na, nb, nk, at, bt):
     C_ref, C_new = C0.clone(), C0.clone()
     s = torch.cuda.current_stream()
     sp = ctypes.c_void_p(s.cuda_stream)
+    want = C0.cpu().numpy().copy()
+    a_h, b_h = A.cpu().numpy(), B.cpu().numpy()
     for call in range(2):
         assert L.gbx_local_contraction(na, nb, nk, _ptr(A), _ptr(B), _ptr(C_ref), at, bt, 0.75, sp) == 0
         rc = L.gbx_local_contraction_noalloc(na, nb, nk, _ptr(A), _ptr(B), _ptr(C_new), at, bt, 0.75, sp)
         assert rc == 0, L.gbx_last_error()
+        oracle.local_contraction(na, nb, nk, a_h, b_h, want, at, bt, 0.75)
         torch.cuda.synchronize()
         ref, got = C_ref.cpu().numpy(), C_new.cpu().numpy()
         scale = max(1.0, float(np.abs(ref).max()))
         assert np.max(np.abs(got - ref)) <= 1e-12 * scale, (call, np.max(np.abs(got - ref)))
+        # the oracle's loop sums in another order: 1e-13 of |A| |B| K
+        tol = 1e-13 * float(np.abs(a_h).max(initial=1)) * float(np.abs(b_h).max(initial=1)) * max(nk, 1)
+        assert np.max(np.abs(got - want)) <= tol, (call, np.max(np.abs(got - want)))
 
 
 def test_noalloc_rejects_outputs_beyond_the_workspace():
