@@ -10,9 +10,9 @@ denominator update and the correlation energy), job state resident in HBM.
 
 N > 1 runs N independent replicas (one job per GPU, no collective on the data
 path) under torchrun; value = iterations/s summed over ranks.  Rank 0 prints
-one JSON line.  --impl reference times the reference's CPU path (the oracle
-port of its permute + big-matrix + dgemm leaf algorithm, GEMM part) on the
-host cores.
+one JSON line.  --impl reference times the reference's CPU path (the port of
+its permute + big-matrix + dgemm + unpack leaf algorithm over every packed
+GEMM of the iteration) on the host cores.
 """
 import argparse
 import json
@@ -179,26 +179,65 @@ def dist_setup():
     return world()
 
 
-def cpu_arm(a, steps, warmup, label_impl):
-    """The reference's CPU path on this host: per contraction and irrep one
-    dgemm with the packed shapes, all host threads."""
-    import numpy as np  # noqa: F401
+def cpu_arm(a, steps, warmup, one_core=False):
+    """The reference's node-local algorithm on this host's cores for every
+    packed GEMM of one CCSD iteration of the workload: both operands permuted
+    from tile storage into the packed layout, one dgemm, the product permuted
+    back and accumulated (transpose_and_dgemm + kevin_dgemm + the C permutes,
+    contraction.cc:1779-2002, 2693-2830), numpy/OpenBLAS FP64 on all host
+    threads; the median over `steps` iterations after `warmup`.  one_core:
+    also one iteration with one thread for copies and BLAS."""
+    import numpy as np
     from oracle import cc as occ, cc_cpu
     sysm = occ.System(a.nocc, a.nvir, nirrep=a.nirrep, max_block=a.max_block, min_block=a.min_block, seed=a.seed)
     shapes = cc_cpu.gemm_shapes(sysm, "ccsd")
-    g = cc_cpu.IterationGemms(shapes)
     fl = cc_cpu.flops(shapes)
-    for _ in range(warmup):
-        g.run()
-    t = time.perf_counter()
-    for _ in range(steps):
-        g.run()
-    dt = (time.perf_counter() - t) / max(steps, 1)
     cores = os.cpu_count()
-    return dict(value=1.0 / dt, unit="iter/s", cores=cores, kind="port", ms_per_step=dt * 1e3,
-                sample="all %d per-irrep dgemms of one CCSD iteration (%.3g flops, packed shapes of the reference's "
-                       "transpose_and_dgemm), numpy/OpenBLAS FP64 on %d threads; permutes and packs not timed"
-                       % (len(shapes), fl, cores), gemm_tflops=fl / dt / 1e12)
+    L = cc_cpu.IterationLeaves(shapes, threads=cores)
+    for _ in range(warmup):
+        L.run()
+    runs = []
+    for _ in range(max(steps, 1)):
+        t = time.perf_counter()
+        L.run()
+        runs.append(time.perf_counter() - t)
+    L.close()
+    dt = float(np.median(runs))
+    out = dict(value=1.0 / dt, unit="iter/s", cores=cores, kind="port", ms_per_step=dt * 1e3,
+               runs_s=runs, gemm_tflops=fl / dt / 1e12,
+               sample="one CCSD iteration of the reference's leaf algorithm over all %d per-irrep packed GEMMs "
+                      "(%.3g flops): permute + pack both operands, dgemm, unpack + accumulate C; numpy/OpenBLAS FP64 "
+                      "on %d host threads; median of %d iterations after %d warm-up" % (len(shapes), fl, cores,
+                                                                                         len(runs), warmup))
+    if one_core:
+        prev = cc_cpu.blas_threads(1)
+        if prev is not None:
+            L1 = cc_cpu.IterationLeaves(shapes, threads=1)
+            t = time.perf_counter()
+            L1.run()
+            out["one_core_iter_s"] = 1.0 / (time.perf_counter() - t)
+            L1.close()
+            cc_cpu.blas_threads(prev)
+        else:
+            out["one_core_iter_s"] = None
+    return out
+
+
+def oracle_arm(a, niter):
+    """The irrep-blocked FP64 restatement of the CCSD iteration (the oracle):
+    the MP2 guess and niter iterations of the workload; energies and the time
+    of one iteration on the host cores."""
+    from oracle import cc as occ, cc_blocks
+    sysm = occ.System(a.nocc, a.nvir, nirrep=a.nirrep, max_block=a.max_block, min_block=a.min_block, seed=a.seed)
+    t0 = time.perf_counter()
+    ref = cc_blocks.CC(sysm, "ccsd")
+    setup = time.perf_counter() - t0
+    per = []
+    for _ in range(niter):
+        t = time.perf_counter()
+        ref.iterate(1)
+        per.append(time.perf_counter() - t)
+    return dict(energies=list(ref.energies), s_per_iter=per, setup_s=setup)
 
 
 def kernel_arm(a):
@@ -398,7 +437,7 @@ def main():
     if a.impl == "reference":
         if rank != 0:
             return 0
-        r = cpu_arm(a, max(a.steps, 1), max(min(a.warmup, 1), 0), "reference")
+        r = cpu_arm(a, max(a.steps, 1), max(min(a.warmup, 1), 0))
         line = {"metric": METRIC, "impl": "reference", "value": r["value"], "unit": "iter/s", "n_gpus": a.gpus,
                 "steps": a.steps, "warmup": a.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
@@ -456,7 +495,7 @@ def main():
         have = len(job.energies()) - 1
         if have < 12:
             job.iterate(12 - have)
-        energies = job.energies()[1:13]
+        energies = job.energies()[:13]  # the MP2 guess and 12 iterations
         results[eng] = dict(ms=ms / steps, steps=steps, stats=st, energies=energies, job=job)
         if primary is None:
             primary = eng
@@ -510,6 +549,19 @@ def main():
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                 "traffic": None, "kernel": kname, "contraction": top["name"], "kernel_ms": kt["ms"],
                 "fp64_equiv_tflops": kt["fp64_flops"] / (kt["ms"] * 1e-3) / 1e12, "peak_source": src, **extra}
+    # error of every contraction of the split path against the plain FP64
+    # path on the same operands (the state after the timed iterations)
+    if primary == "split":
+        errs = []
+        for c in range(st.ncontractions):
+            rel, mx = P["job"].contraction_error(c, stream)
+            errs.append({"contraction": c, "rel_frob_err": rel, "max_abs_err": mx})
+        names = {s["plan"]: s["name"] for s in prof if s["kind"] == 0}
+        for e in errs:
+            e["name"] = names.get(e["contraction"], "")
+        split_err = {"max_rel_frob_err": max(e["rel_frob_err"] for e in errs), "per_contraction": errs}
+    else:
+        split_err = None
     # end to end through the public API with host buffers: every step copies the
     # amplitudes in from pinned host memory and reads the energy back
     job = P["job"]
@@ -536,23 +588,40 @@ def main():
             "dtype": "f64" if primary == "fp64" else "bf16-slices/f64", "data": "synthetic (seeded)",
             "config": dict(workload(a), engine=primary), "engine": primary,
             "eff_tflops": st.flops_per_iter * iters / 1e12, "flops_per_iter": st.flops_per_iter,
-            "gpu_launches": int(st.launches_per_iter * a.steps), "clocks": clocks, "roofline": roofline, "e2e": e2e}
+            "gpu_launches": int(st.launches_per_iter * a.steps), "clocks": clocks, "roofline": roofline, "e2e": e2e,
+            "split_contraction_err": split_err}
     if "fp64" in results and primary != "fp64":
         F = results["fp64"]
         line["fp64_iter_s"] = sum_over_ranks(1000.0 / F["ms"])
         line["split_speedup_vs_fp64"] = F["ms"] / P["ms"]
-        err = np.abs(np.array(F["energies"]) - np.array(P["energies"]))
+        err = np.abs(np.array(F["energies"][1:]) - np.array(P["energies"][1:]))
         line["energy_err_vs_fp64_eh"] = float(np.max(err))
         line["energy_err_per_iter_eh"] = [float(x) for x in err]
         line["energy_iterations_compared"] = int(len(err))
     if rank == 0:
         try:
-            cb = cpu_arm(a, 1, 1, "port")
+            cb = cpu_arm(a, 5, 1, one_core=True)
             line["cpu_baseline"] = {"value": cb["value"], "unit": "iter/s", "cores": cb["cores"], "kind": cb["kind"],
-                                    "sample": cb["sample"]}
+                                    "sample": cb["sample"], "runs_s": cb["runs_s"],
+                                    "one_core_iter_s": cb.get("one_core_iter_s"),
+                                    "gemm_tflops": cb["gemm_tflops"]}
         except Exception as ex:  # the CPU sample must not hide the GPU number
             line["cpu_baseline"] = {"value": None, "unit": "iter/s", "cores": os.cpu_count(), "kind": "port",
                                     "sample": "failed: %s" % ex}
+        try:
+            # the FP64 oracle (irrep-blocked restatement on the host) for the
+            # first iterations: the energy error of every engine against it
+            n_or = 2
+            orc = oracle_arm(a, n_or)
+            line["energy_err_vs_oracle_eh"] = {
+                eng: [abs(R["energies"][i] - orc["energies"][i]) for i in range(n_or + 1)]
+                for eng, R in results.items()}
+            line["oracle"] = {"kind": "irrep-blocked FP64 CCSD restatement, numpy/OpenBLAS on %d host threads"
+                              % os.cpu_count(), "iterations": n_or, "s_per_iter": orc["s_per_iter"],
+                              "energies_eh": orc["energies"], "compared": "MP2 guess and iterations 1..%d" % n_or}
+        except Exception as ex:
+            line["energy_err_vs_oracle_eh"] = None
+            line["oracle"] = {"failed": str(ex)}
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()

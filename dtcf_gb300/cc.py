@@ -143,6 +143,14 @@ class Job:
                                      ctypes.byref(ten), ctypes.byref(eng), _stream(stream)))
         return dict(ms=ms.value, fp64_flops=f64.value, tensor_flops=ten.value, engine=eng.value)
 
+    def contraction_error(self, contraction, stream=None):
+        """(relative Frobenius error, max abs error) of one contraction of
+        this job against a plain FP64 plan of it, on the current operands."""
+        rel, mx = ctypes.c_double(), ctypes.c_double()
+        check(lib().gbx_cc_contraction_error(self.handle, contraction, ctypes.byref(rel), ctypes.byref(mx),
+                                             _stream(stream)))
+        return rel.value, mx.value
+
     def close(self):
         if getattr(self, "handle", None) and self.handle.value:
             lib().gbx_cc_destroy(self.handle)

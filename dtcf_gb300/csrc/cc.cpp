@@ -5,6 +5,7 @@
 #include "split.h"
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -95,6 +96,7 @@ struct gbx_cc_job {
   std::set<std::string> dynamic_use;  // tensors read or written outside constant plan operands
   std::vector<std::pair<CCTensor*, CCTensor*>> plan_operands;  // A, B of each contraction plan
   std::vector<CCTensor*> plan_outputs;                         // C of each contraction plan
+  std::vector<std::array<std::string, 3>> plan_labels;          // la, lb, lc of each contraction plan
   unsigned char* d_arena = nullptr;  // packed operands and split slices, shared by every plan
   size_t arena_bytes = 0;
   std::atomic<int64_t> account{0};  // device bytes the job's allocations hold
@@ -206,6 +208,7 @@ struct gbx_cc_job {
     cplans.push_back(std::move(p));
     plan_operands.push_back({A, B});
     plan_outputs.push_back(C);
+    plan_labels.push_back({la, lb, lc});
     return GBX_OK;
   }
 
@@ -1017,6 +1020,57 @@ int gbx_cc_time_gemm(gbx_cc_job* job, int contraction, int reps, float* ms, doub
   if (fp64_flops) *fp64_flops = p->direct ? p->flops : p->gemm_flops;
   if (tensor_flops) *tensor_flops = split_plan_tensor_flops(p->split);
   if (engine) *engine = p->direct ? 3 : p->split ? (p->f64.nprob ? 2 : 1) : 0;
+  return GBX_OK;
+}
+
+int gbx_cc_contraction_error(gbx_cc_job* job, int contraction, double* rel_frob_err, double* max_abs_err,
+                             void* stream) {
+  if (!job || contraction < 0 || contraction >= (int)job->cplans.size()) return fail(GBX_EINVAL, "bad arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  ContractionPlan* p = job->cplans[contraction].get();
+  const CCTensor* A = job->plan_operands[contraction].first;
+  const CCTensor* B = job->plan_operands[contraction].second;
+  const CCTensor* C = job->plan_outputs[contraction];
+  const auto& lab = job->plan_labels[contraction];
+  // a plain FP64 plan of the same contraction (its own workspace; constant
+  // operands packed like the changing ones)
+  std::unique_ptr<ContractionPlan> ref;
+  GBX_TRY(plan_contraction(A->L, B->L, C->L, gbx_cc_job::labels(lab[0].c_str()), gbx_cc_job::labels(lab[1].c_str()),
+                           gbx_cc_job::labels(lab[2].c_str()), Engine::F64, 0, ref, false, false));
+  const int64_t n = C->L.nelem;
+  double *c_job = nullptr, *c_ref = nullptr;
+  GBX_TRY(dev_alloc((void**)&c_job, sizeof(double) * std::max<int64_t>(n, 1)));
+  int rc = dev_alloc((void**)&c_ref, sizeof(double) * std::max<int64_t>(n, 1));
+  std::vector<double> h_job(n), h_ref(n);
+  if (rc == GBX_OK) {
+    cudaMemsetAsync(c_job, 0, sizeof(double) * n, st);
+    cudaMemsetAsync(c_ref, 0, sizeof(double) * n, st);
+    // the job's plan on the current operands (static ones are already split)
+    rc = p->execute(A->d, B->d, c_job, 1.0, st);
+    if (rc == GBX_OK) rc = ref->execute(A->d, B->d, c_ref, 1.0, st);
+    if (rc == GBX_OK) {
+      cudaError_t e = cudaMemcpyAsync(h_job.data(), c_job, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(h_ref.data(), c_ref, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) rc = cuda_fail(e, "contraction error readback", __FILE__, __LINE__);
+    }
+    if (rc == GBX_OK && p->split) {
+      const int err = split_plan_error(p->split);
+      if (err != 0) rc = fail(GBX_ETIMEOUT, "split GEMM: a bounded device wait ran out (stage %d)", err);
+    }
+  }
+  dev_free(c_job);
+  dev_free(c_ref);
+  GBX_TRY(rc);
+  double num = 0.0, den = 0.0, mx = 0.0;
+  for (int64_t i = 0; i < n; ++i) {
+    const double d = h_job[i] - h_ref[i];
+    num += d * d;
+    den += h_ref[i] * h_ref[i];
+    mx = std::max(mx, std::fabs(d));
+  }
+  if (rel_frob_err) *rel_frob_err = den > 0.0 ? std::sqrt(num / den) : std::sqrt(num);
+  if (max_abs_err) *max_abs_err = mx;
   return GBX_OK;
 }
 

@@ -114,6 +114,16 @@ GBX_API int gbx_cc_plan_info(const gbx_cc_job* job, int contraction, int* split_
  * element, timed with alpha = 0 so that C keeps its values). */
 GBX_API int gbx_cc_time_gemm(gbx_cc_job* job, int contraction, int reps, float* ms, double* fp64_flops,
                              double* tensor_flops, int* engine, void* stream);
+/* Error of one contraction of the job's iteration against the plain FP64
+ * path: the contraction runs on its current operands (call after at least
+ * one iteration, so that the intermediates exist) twice into scratch
+ * outputs -- with the job's own plan (e.g. the split engine) and with a
+ * plain FP64 plan of the same contraction built for the call -- and
+ * rel_frob_err = ||C_job - C_fp64||_F / ||C_fp64||_F, max_abs_err = the
+ * largest element difference.  The job's tensors are not changed; the call
+ * allocates its scratch and waits for the stream. */
+GBX_API int gbx_cc_contraction_error(gbx_cc_job* job, int contraction, double* rel_frob_err, double* max_abs_err,
+                                     void* stream);
 GBX_API int gbx_cc_destroy(gbx_cc_job* job);
 
 #ifdef __cplusplus

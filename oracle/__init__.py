@@ -55,6 +55,7 @@ def lib():
         _lib.orc_dltc_compute.argtypes = [_l, _l, _l, _p, _p, _p]
         _lib.orc_task_mul.argtypes = [_d, _i, _p, _p, _i, _p, _p, _i, _p, _p] + [_i] * 6
         _lib.orc_task_sum.argtypes = [_d, _i, _p, _p, _i, _p, _p] + [_i] * 5
+        _lib.orc_cc_integrals.argtypes = [ctypes.c_uint64, _l, _p, _p] + [_l, _p] * 4 + [_p]
     return _lib
 
 
@@ -254,3 +255,17 @@ class Drand48:
             out[i] = x / float(1 << 48)
         self.x = x
         return out
+
+
+def cc_integrals(system, P, Q, R, S):
+    """<pq||rs> of an oracle.cc.System over the outer product of four orbital
+    index lists (oracle/cc_ints.c; the same values as System.integral_values)."""
+    idx = [np.ascontiguousarray(x, dtype=np.int64).reshape(-1) for x in (P, Q, R, S)]
+    mag = np.ascontiguousarray(system.mag, dtype=np.float64)
+    irr = np.ascontiguousarray(system.irrep, dtype=np.int64)
+    out = np.empty([len(x) for x in idx])
+    args = []
+    for x in idx:
+        args += [len(x), _ptr(x)]
+    lib().orc_cc_integrals(system.seed_int, system.n, _ptr(mag), _ptr(irr), *args, _ptr(out))
+    return out

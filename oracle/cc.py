@@ -86,8 +86,14 @@ class System:
 
     def integrals(self):
         """Dense antisymmetrised <pq||rs>, shape (n, n, n, n)."""
+        ar = np.arange(self.n, dtype=np.uint64)
+        return self.integral_values(ar[:, None, None, None], ar[None, :, None, None], ar[None, None, :, None],
+                                    ar[None, None, None, :])
+
+    def integral_values(self, p, q, r, s):
+        """<pq||rs> at broadcastable arrays of orbital indices (uint64)."""
+        p, q, r, s = np.broadcast_arrays(*[np.asarray(x, dtype=np.uint64) for x in (p, q, r, s)])
         n = self.n
-        p, q, r, s = np.meshgrid(*([np.arange(n, dtype=np.uint64)] * 4), indexing="ij")
         sg = np.ones(p.shape)
         swap = p > q
         sg[swap] *= -1

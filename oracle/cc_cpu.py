@@ -11,6 +11,10 @@ module derives those shapes from the synthetic system's irrep occupations
 (independently of the product's planner) for the contraction list of one
 CCSD / CCD iteration, and times the dgemms with numpy's multithreaded BLAS.
 """
+import concurrent.futures
+import ctypes
+import glob
+import os
 import time
 
 import numpy as np
@@ -168,3 +172,85 @@ class IterationGemms:
         for _ in range(reps):
             self.run()
         return (time.perf_counter() - t) / reps
+
+
+def _factor(x, cap=64):
+    """x = a * b with b the largest divisor of x not above cap."""
+    for b in range(min(cap, x), 0, -1):
+        if x % b == 0:
+            return x // b, b
+    return x, 1
+
+
+class IterationLeaves:
+    """The reference's node-local leaf algorithm for every packed GEMM of one
+    iteration (Contraction::transpose_and_dgemm, contraction.cc:1779-2002;
+    DLTC task_mul, DLTC/task.cc:83-137): both operands permuted from tile
+    storage into the packed externals-by-contracted layout (the per-block
+    transpose + create_big_matrix copy, done here as one strided copy per
+    operand), one dgemm, and the product permuted back and accumulated into
+    C's tile storage (revert_big_matrix + inverse transpose + accumulate, one
+    strided pass).  Copies run on `threads` host threads (row slabs), the
+    dgemm on BLAS's threads."""
+
+    def __init__(self, shapes, seed=0, threads=None):
+        rng = np.random.default_rng(seed)
+        self.threads = threads or os.cpu_count() or 1
+        self.pool = concurrent.futures.ThreadPoolExecutor(self.threads) if self.threads > 1 else None
+        self.ops = []
+        for m, n, k in shapes:
+            ma, mb = _factor(m)
+            ka, kb = _factor(k)
+            na, nb = _factor(n)
+            a_src = rng.uniform(-1, 1, (ma, ka, mb, kb))
+            b_src = rng.uniform(-1, 1, (na, ka, nb, kb))
+            c_dst = np.zeros((ma, na, mb, nb))
+            self.ops.append((a_src, b_src, c_dst, np.empty((ma, mb, ka, kb)), np.empty((na, nb, ka, kb)),
+                             np.empty((m, n)), (m, n, k)))
+
+    def _par(self, fn, rows):
+        if self.pool is None or rows < 2:
+            fn(0, rows)
+            return
+        step = -(-rows // self.threads)
+        list(self.pool.map(lambda lo: fn(lo, min(rows, lo + step)), range(0, rows, step)))
+
+    def run(self):
+        for a_src, b_src, c_dst, a_pk, b_pk, c, (m, n, k) in self.ops:
+            def pack(lo, hi, src=a_src, dst=a_pk):
+                dst[lo:hi] = src[lo:hi].transpose(0, 2, 1, 3)
+            self._par(pack, a_src.shape[0])
+            self._par(lambda lo, hi: pack(lo, hi, b_src, b_pk), b_src.shape[0])
+            np.matmul(a_pk.reshape(m, k), b_pk.reshape(n, k).T, out=c)
+            c4 = c.reshape(c_dst.shape[0], c_dst.shape[2], c_dst.shape[1], c_dst.shape[3])
+
+            def unpack(lo, hi, c4=c4, dst=c_dst):
+                dst[lo:hi] += c4[lo:hi].transpose(0, 2, 1, 3)
+            self._par(unpack, c_dst.shape[0])
+
+    def close(self):
+        if self.pool is not None:
+            self.pool.shutdown()
+
+
+def blas_threads(n):
+    """Set the thread count of numpy's bundled OpenBLAS (returns the previous
+    count, or None when the library or its symbols are not found)."""
+    import numpy
+    libs = glob.glob(os.path.join(os.path.dirname(numpy.__file__), "..", "numpy.libs", "*openblas*"))
+    for path in libs:
+        try:
+            lib = ctypes.CDLL(path)
+        except OSError:
+            continue
+        for get_name, set_name in (("scipy_openblas_get_num_threads64_", "scipy_openblas_set_num_threads64_"),
+                                   ("openblas_get_num_threads64_", "openblas_set_num_threads64_"),
+                                   ("openblas_get_num_threads", "openblas_set_num_threads")):
+            g, s = getattr(lib, get_name, None), getattr(lib, set_name, None)
+            if g is not None and s is not None:
+                g.restype = ctypes.c_int
+                prev = g()
+                s.argtypes = [ctypes.c_int]
+                s(int(n))
+                return prev
+    return None
