@@ -63,6 +63,16 @@ SIGNATURES = {
     "gbx_cc_profile": (_i, [_p, _i, _p, _p, _p, _p, _p, _p, _i, _ip, _p]),
     "gbx_cc_time_gemm": (_i, [_p, _i, _i, _p, _p, _p, _p, _p]),
     "gbx_cc_contraction_error": (_i, [_p, _i, _p, _p, _p]),
+    "gbx_dltc_mul_orders": (_i, [_i, _p, _i, _p, _p, _p, _p, _p, _p, _p]),
+    "gbx_dltc_task_mul": (_i, [_d, _i, _p, _p, _i, _p, _p, _i, _p, _p, _p, _p, _p, _i, _p]),
+    "gbx_dltc_task_sum": (_i, [_d, _i, _p, _p, _i, _p, _p, _p, _p, _p, _p]),
+    "gbx_dltc_table": (_i, [_i, _p, _p, _p, _p, _p, _i]),
+    "gbx_dltc_program_create": (_i, [_i, _p, _i, ctypes.POINTER(_p)]),
+    "gbx_dltc_program_tensor": (_i, [_p, _i, _p, _p]),
+    "gbx_dltc_program_run": (_i, [_p, _i, _i, _p]),
+    "gbx_dltc_program_check": (_i, [_p]),
+    "gbx_dltc_program_flops": (_d, [_p]),
+    "gbx_dltc_program_destroy": (_i, [_p]),
 }
 
 _lib = None

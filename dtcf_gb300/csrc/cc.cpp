@@ -1039,15 +1039,47 @@ int gbx_cc_contraction_error(gbx_cc_job* job, int contraction, double* rel_frob_
                            gbx_cc_job::labels(lab[2].c_str()), Engine::F64, 0, ref, false, false));
   const int64_t n = C->L.nelem;
   double *c_job = nullptr, *c_ref = nullptr;
-  GBX_TRY(dev_alloc((void**)&c_job, sizeof(double) * std::max<int64_t>(n, 1)));
-  int rc = dev_alloc((void**)&c_ref, sizeof(double) * std::max<int64_t>(n, 1));
+  // Integral operands that only served as constant plan operands were
+  // released when the job was built (the job's plan keeps them packed and
+  // split); the FP64 plan packs them, so they are generated again into
+  // scratch from the same device tables.
+  std::vector<double*> regen;
+  const size_t ntiles0 = job->tilesets.size();
+  auto release = [&]() {
+    cudaStreamSynchronize(st);
+    for (double* d : regen) dev_free(d);
+    job->tilesets.resize(ntiles0);
+  };
+  auto operand = [&](const CCTensor* t, const double** out) -> int {
+    *out = t->d;
+    if (t->d) return GBX_OK;
+    std::string name;
+    for (auto& kv : job->T)
+      if (kv.second.get() == t) name = kv.first;
+    if (!gbx_cc_job::is_integral(name.c_str()))
+      return fail(GBX_EINVAL, "operand %s of contraction %d has no device memory", name.c_str(), contraction);
+    double* d = nullptr;
+    GBX_TRY(dev_alloc((void**)&d, sizeof(double) * std::max<int64_t>(1, t->L.nelem)));
+    regen.push_back(d);
+    CCTileSet* ts = job->tileset(t);
+    if (!ts) return fail(GBX_ENOMEM, "tile set upload failed");
+    GBX_TRY(run_cc_tiles(*ts, CC_OP_INTEGRAL, job->tab, nullptr, d, st));
+    *out = d;
+    return GBX_OK;
+  };
+  const double *rA = nullptr, *rB = nullptr;
+  int rc = operand(A, &rA);
+  if (rc == GBX_OK) rc = operand(B, &rB);
+  if (rc == GBX_OK) rc = dev_alloc((void**)&c_job, sizeof(double) * std::max<int64_t>(n, 1));
+  if (rc == GBX_OK) rc = dev_alloc((void**)&c_ref, sizeof(double) * std::max<int64_t>(n, 1));
   std::vector<double> h_job(n), h_ref(n);
   if (rc == GBX_OK) {
     cudaMemsetAsync(c_job, 0, sizeof(double) * n, st);
     cudaMemsetAsync(c_ref, 0, sizeof(double) * n, st);
-    // the job's plan on the current operands (static ones are already split)
+    // the job's plan on the current operands (constant ones are already
+    // packed and split and are not read again)
     rc = p->execute(A->d, B->d, c_job, 1.0, st);
-    if (rc == GBX_OK) rc = ref->execute(A->d, B->d, c_ref, 1.0, st);
+    if (rc == GBX_OK) rc = ref->execute(rA, rB, c_ref, 1.0, st);
     if (rc == GBX_OK) {
       cudaError_t e = cudaMemcpyAsync(h_job.data(), c_job, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
       if (e == cudaSuccess) e = cudaMemcpyAsync(h_ref.data(), c_ref, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
@@ -1059,6 +1091,7 @@ int gbx_cc_contraction_error(gbx_cc_job* job, int contraction, double* rel_frob_
       if (err != 0) rc = fail(GBX_ETIMEOUT, "split GEMM: a bounded device wait ran out (stage %d)", err);
     }
   }
+  release();
   dev_free(c_job);
   dev_free(c_ref);
   GBX_TRY(rc);

@@ -817,6 +817,7 @@ int ContractionPlan::prepare_static(const double* dA, const double* dB, cudaStre
 int ContractionPlan::stage(const double* dA, const double* dB, cudaStream_t st) {
   if (direct) return GBX_OK;
   const bool skipA = a_static && static_ready, skipB = b_static && static_ready;
+  if ((!skipA && !dA) || (!skipB && !dB)) return fail(GBX_EINVAL, "contraction operand without device memory");
   if (!skipA) {
     if (a_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Abig, 0, sizeof(double) * a_elems, st));
     GBX_TRY(run_moves(packA, dA, d_Abig, st));
@@ -830,9 +831,13 @@ int ContractionPlan::stage(const double* dA, const double* dB, cudaStream_t st) 
 }
 
 int ContractionPlan::execute(const double* dA, const double* dB, double* dC, double alpha, cudaStream_t st) {
-  if (direct) return run_direct(d_dir_items, (int)dir_items.size(), d_dir_pairs, dA, dB, dC, alpha, st);
+  if (direct) {
+    if (!dA || !dB || !dC) return fail(GBX_EINVAL, "contraction operand without device memory");
+    return run_direct(d_dir_items, (int)dir_items.size(), d_dir_pairs, dA, dB, dC, alpha, st);
+  }
   if (f64.nprob == 0 && !split) return GBX_OK;
   const bool skipA = a_static && static_ready, skipB = b_static && static_ready;
+  if ((!skipA && !dA) || (!skipB && !dB)) return fail(GBX_EINVAL, "contraction operand without device memory");
   if (!skipA) {
     if (a_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Abig, 0, sizeof(double) * a_elems, st));
     GBX_TRY(run_moves(packA, dA, d_Abig, st));
