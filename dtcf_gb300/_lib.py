@@ -60,6 +60,7 @@ SIGNATURES = {
     "gbx_cc_amplitude_elems": (_i, [_p, _p, _p]),
     "gbx_cc_set_amplitudes": (_i, [_p, _p, _p, _p]),
     "gbx_cc_read_energy": (_i, [_p, _p, _p]),
+    "gbx_cc_save_amplitudes": (_i, [_p, _p, _p, _p]),
     "gbx_cc_profile": (_i, [_p, _i, _p, _p, _p, _p, _p, _p, _i, _ip, _p]),
     "gbx_cc_time_gemm": (_i, [_p, _i, _i, _p, _p, _p, _p, _p]),
     "gbx_cc_contraction_error": (_i, [_p, _i, _p, _p, _p]),

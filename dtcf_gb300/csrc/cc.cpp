@@ -934,6 +934,17 @@ int gbx_cc_set_amplitudes(gbx_cc_job* job, const double* t1, const double* t2, v
   return GBX_OK;
 }
 
+int gbx_cc_save_amplitudes(gbx_cc_job* job, double* t1, double* t2, void* stream) {
+  if (!job) return fail(GBX_EINVAL, "null job");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (t2) GBX_CUDA(cudaMemcpyAsync(t2, job->get("t2")->d, sizeof(double) * job->get("t2")->L.nelem,
+                                   cudaMemcpyDeviceToHost, st));
+  if (t1 && job->T.count("t1"))
+    GBX_CUDA(cudaMemcpyAsync(t1, job->get("t1")->d, sizeof(double) * job->get("t1")->L.nelem, cudaMemcpyDeviceToHost,
+                             st));
+  return GBX_OK;
+}
+
 int gbx_cc_read_energy(gbx_cc_job* job, double* energy, void* stream) {
   if (!job || !energy) return fail(GBX_EINVAL, "bad arguments");
   int k = job->nenergies - 1;

@@ -8,6 +8,13 @@
 // admitted jobs (host planning, integrals, constant operands, graph capture)
 // and checks and destroys finished ones, so that neither stalls dispatch.
 //
+// Idle jobs do not hold the budget: when a job waiting for admission does
+// not fit, resident jobs with no request waiting (least recently used first)
+// are evicted -- their amplitudes saved to pinned host memory, their device
+// state released -- and an evicted job is admitted again, rebuilt and given
+// its saved amplitudes back, when its next request arrives.  The iterations
+// after a restore repeat those of a job that never left the device.
+//
 // Job state comes from the stream-ordered allocator on a stream of the
 // server's own, so releasing a finished job does not wait for the whole
 // device (cudaFree would, and with other jobs' iterations always in flight
@@ -38,7 +45,7 @@ struct Req {
   int status = kPending, slot = -1;
 };
 
-enum class JobState { Waiting, Building, Ready, Busy, Finished, Rejected };
+enum class JobState { Waiting, Building, Ready, Busy, Finished, Rejected, Evicting, Evicted };
 
 struct Job {
   gbx_cc_config cfg;
@@ -49,6 +56,20 @@ struct Job {
   gbx_cc_job* h = nullptr;
   int build_status = GBX_OK, check_status = GBX_OK;
   double build_s = 0.0;
+  double last_done = 0.0;  // when its last request finished (eviction order)
+  // amplitudes saved in pinned host memory while the job is evicted
+  double* h_t1 = nullptr;
+  double* h_t2 = nullptr;
+  int64_t n1 = 0, n2 = 0;
+  bool saved = false;
+  double evict_s = 0.0;
+  int evict_status = GBX_OK;
+  void free_saved() {
+    if (h_t1) cudaFreeHost(h_t1);
+    if (h_t2) cudaFreeHost(h_t2);
+    h_t1 = h_t2 = nullptr;
+    saved = false;
+  }
 };
 
 double pct(std::vector<double> v, double q) {
@@ -73,9 +94,28 @@ struct gbx_server {
   // builder thread queues (guarded by mu)
   std::mutex mu;
   std::condition_variable cv;
-  std::deque<int> to_build, to_destroy;
-  std::vector<int> built, destroyed;
+  std::deque<int> to_build, to_destroy, to_evict;
+  std::vector<int> built, destroyed, evicted;
   bool stop = false;
+
+  // Saves an idle job's amplitudes to pinned host memory and releases its
+  // device state (builder thread).
+  int evict(Job& j) {
+    int rc = gbx_cc_amplitude_elems(j.h, &j.n1, &j.n2);
+    if (rc == GBX_OK && !j.h_t2) {
+      if (cudaMallocHost((void**)&j.h_t2, sizeof(double) * std::max<int64_t>(j.n2, 1)) != cudaSuccess ||
+          cudaMallocHost((void**)&j.h_t1, sizeof(double) * std::max<int64_t>(j.n1, 1)) != cudaSuccess)
+        rc = gbx::fail(GBX_ENOMEM, "pinned host memory for evicted amplitudes");
+    }
+    if (rc == GBX_OK) rc = gbx_cc_save_amplitudes(j.h, j.n1 ? j.h_t1 : nullptr, j.h_t2, nullptr);
+    if (rc == GBX_OK && cudaStreamSynchronize(nullptr) != cudaSuccess)
+      rc = gbx::fail(GBX_ECUDA, "saving amplitudes failed");
+    const int chk = gbx_cc_check(j.h);
+    if (rc == GBX_OK) rc = chk;
+    gbx_cc_destroy(j.h);
+    j.saved = rc == GBX_OK;
+    return rc;
+  }
 
   void builder() {
     cudaSetDevice(device);
@@ -84,10 +124,23 @@ struct gbx_server {
       int b = -1, d = -1;
       {
         std::unique_lock<std::mutex> lk(mu);
-        cv.wait(lk, [&] { return stop || !to_build.empty() || !to_destroy.empty(); });
+        cv.wait(lk, [&] { return stop || !to_build.empty() || !to_destroy.empty() || !to_evict.empty(); });
         if (!to_destroy.empty()) {
           d = to_destroy.front();
           to_destroy.pop_front();
+        } else if (!to_evict.empty()) {
+          const int e = to_evict.front();
+          to_evict.pop_front();
+          lk.unlock();
+          Job& j = jobs[e];
+          const auto t0 = Clock::now();
+          const int rc = evict(j);
+          lk.lock();
+          j.h = nullptr;
+          j.evict_status = rc;
+          j.evict_s = std::chrono::duration<double>(Clock::now() - t0).count();
+          evicted.push_back(e);
+          continue;
         } else if (!to_build.empty()) {
           b = to_build.front();
           to_build.pop_front();
@@ -101,6 +154,7 @@ struct gbx_server {
         // its bounded device waits, then release the state
         const int st = gbx_cc_check(j.h);
         gbx_cc_destroy(j.h);
+        j.free_saved();
         std::lock_guard<std::mutex> lk(mu);
         j.h = nullptr;
         j.check_status = st;
@@ -112,6 +166,12 @@ struct gbx_server {
         gbx_cc_job* h = nullptr;
         int rc = gbx_cc_create(&j.cfg, nullptr, &h);
         if (rc == GBX_OK) rc = gbx_cc_capture(h);
+        if (rc == GBX_OK && j.saved) {
+          // an evicted job comes back with the amplitudes it left with
+          rc = gbx_cc_set_amplitudes(h, j.n1 ? j.h_t1 : nullptr, j.h_t2, nullptr);
+          if (rc == GBX_OK && cudaStreamSynchronize(nullptr) != cudaSuccess)
+            rc = gbx::fail(GBX_ECUDA, "restoring amplitudes failed");
+        }
         double meas = 0.0;
         if (rc == GBX_OK) {
           gbx_cc_stats st;
@@ -213,7 +273,7 @@ int gbx_server_run(gbx_server* s, double time_limit_s) {
   if (rc == GBX_OK) worker = std::thread([s] { s->builder(); });
 
   double planned = 0.0, measured = 0.0;
-  int building = 0, finished_reqs = 0;
+  int building = 0, evicting = 0, finished_reqs = 0;
   const int total = (int)s->reqs.size();
   const auto t0 = Clock::now();
   auto now = [&] { return std::chrono::duration<double>(Clock::now() - t0).count(); };
@@ -249,6 +309,22 @@ int gbx_server_run(gbx_server* s, double time_limit_s) {
       any = true;
     }
     s->built.clear();
+    for (int e : s->evicted) {
+      Job& j = s->jobs[e];
+      --evicting;
+      planned -= j.footprint;
+      measured -= j.measured;
+      s->stats.evict_s_total += j.evict_s;
+      if (j.evict_status == GBX_OK) {
+        j.state = JobState::Evicted;
+        ++s->stats.evictions;
+      } else {
+        j.state = JobState::Rejected;
+        finish_job_requests(j, j.evict_status);
+      }
+      any = true;
+    }
+    s->evicted.clear();
     for (int d : s->destroyed) {
       Job& j = s->jobs[d];
       planned -= j.footprint;
@@ -282,6 +358,7 @@ int gbx_server_run(gbx_server* s, double time_limit_s) {
         rc = cuda_fail(q, "iteration request", __FILE__, __LINE__);
         break;
       }
+      j.last_done = t;
       if (j.done == (int)j.reqs.size()) {
         j.state = JobState::Finished;
         std::lock_guard<std::mutex> lk(s->mu);
@@ -292,11 +369,16 @@ int gbx_server_run(gbx_server* s, double time_limit_s) {
       }
     }
     if (collect()) progress = true;
-    // admission: first fit in order of first arrival, one build at a time
-    if (building == 0) {
+    // admission: first fit in order of first arrival, one build at a time;
+    // the first job that does not fit may evict idle jobs to make room
+    if (building == 0 && evicting == 0) {
+      bool tried_evict = false;
       for (int jb : job_order) {
         Job& j = s->jobs[jb];
-        if (j.state != JobState::Waiting || j.reqs.empty() || s->reqs[j.reqs[0]].arrival > t) continue;
+        const bool fresh = j.state == JobState::Waiting && !j.reqs.empty() && s->reqs[j.reqs[0]].arrival <= t;
+        const bool back = j.state == JobState::Evicted && j.next < (int)j.reqs.size() &&
+                          s->reqs[j.reqs[j.next]].arrival <= t;
+        if (!fresh && !back) continue;
         if (j.footprint > s->cfg.budget_bytes) {
           j.state = JobState::Rejected;
           finish_job_requests(j, GBX_ENOMEM);
@@ -304,7 +386,39 @@ int gbx_server_run(gbx_server* s, double time_limit_s) {
           progress = true;
           continue;
         }
-        if (planned + j.footprint > s->cfg.budget_bytes) continue;
+        if (planned + j.footprint > s->cfg.budget_bytes) {
+          if (tried_evict) continue;
+          tried_evict = true;
+          // idle resident jobs: no request of theirs waiting; least recently used first
+          std::vector<int> idle;
+          for (size_t k = 0; k < s->jobs.size(); ++k) {
+            const Job& q = s->jobs[k];
+            if (q.state == JobState::Ready && q.next < (int)q.reqs.size() && s->reqs[q.reqs[q.next]].arrival > t)
+              idle.push_back((int)k);
+          }
+          std::sort(idle.begin(), idle.end(),
+                    [&](int a, int b) { return s->jobs[a].last_done < s->jobs[b].last_done; });
+          double room = s->cfg.budget_bytes - planned;
+          std::vector<int> victims;
+          for (int k : idle) {
+            if (room >= j.footprint) break;
+            victims.push_back(k);
+            room += s->jobs[k].footprint;
+          }
+          if (room >= j.footprint && !victims.empty()) {
+            std::lock_guard<std::mutex> lk(s->mu);
+            for (int k : victims) {
+              s->jobs[k].state = JobState::Evicting;
+              ++evicting;
+              s->to_evict.push_back(k);
+            }
+            s->cv.notify_one();
+            progress = true;
+            break;
+          }
+          continue;
+        }
+        if (back) ++s->stats.restores;
         planned += j.footprint;
         s->stats.peak_planned_bytes = std::max(s->stats.peak_planned_bytes, planned);
         j.state = JobState::Building;
@@ -369,7 +483,7 @@ int gbx_server_run(gbx_server* s, double time_limit_s) {
     // signal this thread), then every job still resident is released
     for (;;) {
       collect();
-      if (building <= 0) break;
+      if (building <= 0 && evicting <= 0) break;
       std::this_thread::sleep_for(std::chrono::milliseconds(1));
     }
     {
@@ -446,8 +560,10 @@ int gbx_server_stats(const gbx_server* s, gbx_serve_stats* out) {
 
 int gbx_server_destroy(gbx_server* s) {
   if (s) {
-    for (auto& j : s->jobs)
+    for (auto& j : s->jobs) {
       if (j.h) gbx_cc_destroy(j.h);
+      j.free_saved();
+    }
     if (s->mem_stream) {
       cudaStreamSynchronize(s->mem_stream);
       cudaStreamDestroy(s->mem_stream);

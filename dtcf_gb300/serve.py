@@ -25,7 +25,8 @@ class ServeStats(ctypes.Structure):
                 ("latency_p50_s", ctypes.c_double), ("latency_p99_s", ctypes.c_double),
                 ("latency_max_s", ctypes.c_double), ("service_p50_s", ctypes.c_double),
                 ("peak_planned_bytes", ctypes.c_double), ("peak_measured_bytes", ctypes.c_double),
-                ("build_s_total", ctypes.c_double)]
+                ("build_s_total", ctypes.c_double), ("evictions", ctypes.c_int), ("restores", ctypes.c_int),
+                ("evict_s_total", ctypes.c_double)]
 
 
 class Server:

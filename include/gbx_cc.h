@@ -92,6 +92,11 @@ GBX_API int gbx_cc_amplitude_elems(const gbx_cc_job* job, int64_t* n1, int64_t* 
  * stream, and the tau / taut / Q combinations of them; the next iteration
  * starts from them.  Pinned host memory keeps the copies asynchronous. */
 GBX_API int gbx_cc_set_amplitudes(gbx_cc_job* job, const double* t1, const double* t2, void* stream);
+/* Enqueue device -> host copies of the amplitudes in tile storage order (the
+ * layout gbx_cc_set_amplitudes takes back) on stream; either pointer may be
+ * NULL.  With set_amplitudes, a job's state can leave the device and come
+ * back: the iterations after a restore repeat those of the job that saved. */
+GBX_API int gbx_cc_save_amplitudes(gbx_cc_job* job, double* t1, double* t2, void* stream);
 /* Enqueue a device -> host copy of the latest energy on stream. */
 GBX_API int gbx_cc_read_energy(gbx_cc_job* job, double* energy, void* stream);
 /* Run one iteration step by step with CUDA events between the steps and

@@ -11,7 +11,10 @@
  * last request.  Every request's latency is recorded.
  *
  * The reference has no serving layer (its jobs are single MPI runs); this is
- * the request loop around the node-local contraction path.
+ * the request loop around the node-local contraction path.  A resident job
+ * with no request waiting may be evicted to admit another: its amplitudes
+ * move to pinned host memory and come back, with the job rebuilt, when its
+ * next request arrives; its results do not change.
  */
 #ifndef GBX_SERVE_H
 #define GBX_SERVE_H
@@ -48,6 +51,9 @@ typedef struct {
     double peak_planned_bytes;  /* largest sum of admitted footprints */
     double peak_measured_bytes; /* largest sum of the resident jobs' measured device bytes */
     double build_s_total;       /* time spent building job states */
+    int evictions;              /* idle jobs moved to host memory to admit others */
+    int restores;               /* evicted jobs admitted again */
+    double evict_s_total;       /* time spent saving evicted job states */
 } gbx_serve_stats;
 
 typedef struct gbx_server gbx_server;

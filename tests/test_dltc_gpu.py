@@ -163,7 +163,7 @@ def test_task_ranges_match_the_tile_loop_definition():
     sl = {x: slice(lo[x] * wb[x], hi[x] * wb[x]) for x in range(24)}
     want = C.copy()
     want[sl[p3], sl[p4], sl[h1], sl[h2]] += 0.5 * np.einsum(
-        "acie,edjb->abij", A[sl[p3], sl[p6], sl[h1], sl[h5]], B[sl[h5], sl[p6], sl[h2], sl[p4]])
+        "acie,ecjb->abij", A[sl[p3], sl[p6], sl[h1], sl[h5]], B[sl[h5], sl[p6], sl[h2], sl[p4]])
     np.testing.assert_allclose(host(dC).reshape(C.shape), want, rtol=0, atol=1e-13)
     # task_sum over a range: C[p3,h1] += -1 * A[h1,p3] on the range's tiles only
     X = rng.uniform(-1, 1, (O, V))

@@ -97,3 +97,34 @@ def test_planned_footprint_matches_measured_bytes(c):
     job.close()
     assert abs(got - res.value) <= 0.02 * res.value + (4 << 20), (got, res.value)
     assert peak.value >= res.value
+
+
+def test_idle_jobs_are_evicted_and_restored_with_the_same_results():
+    """A budget that holds about two of the jobs, requests of each job spread
+    over time: jobs idle between their requests are evicted (amplitudes to
+    pinned host memory) to admit the others and rebuilt when their next
+    request arrives.  Every request completes, and every job's energies equal
+    those of the job served alone."""
+    cfgs = OTHERS[:4] + [X]
+    probe = Server(budget_bytes=1e12, slots=2)
+    for c in cfgs:
+        probe.add_job(config(**c))
+    fps = sorted(probe.footprints)
+    probe.close()
+    budget = fps[-1] + fps[-2]
+    s = Server(budget_bytes=budget, slots=2)
+    ids = [s.add_job(config(**c)) for c in cfgs]
+    for n, j in enumerate(ids):
+        for k in range(NIT):
+            s.submit(j, 0.01 * n + 0.25 * k)
+    s.run(LIMIT)
+    res = s.results()
+    st = s.stats()
+    s.close()
+    assert st["completed"] == st["requests"] == NIT * len(cfgs)
+    assert st["peak_planned_bytes"] <= budget
+    assert st["evictions"] >= 1 and st["restores"] >= 1, st
+    for c, j in zip(cfgs, ids):
+        direct = Job(**c)
+        assert np.array_equal(_energies(res, j), direct.iterate(NIT)), c
+        direct.close()
