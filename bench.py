@@ -65,6 +65,9 @@ def parse():
     p.add_argument("--serve-limit", type=float, default=300.0, help="time limit of each serving run (s)")
     p.add_argument("--serve-engines", default="split,fp64", help="engines to serve with, in order")
     p.add_argument("--serve-o-max", type=int, default=64, help="largest occupied count of a job")
+    p.add_argument("--serve-slices", type=int, default=5,
+                   help="bf16 slices of the split engine when serving (5: energies within 1e-10 Eh of the FP64 path "
+                        "on the largest jobs of the mix, o=64, v=384; 4 slices drift to ~2e-10 there)")
     return p.parse_args()
 
 
@@ -391,7 +394,7 @@ def serve_arm(a):
     out, energies = {}, {}
     for eng in a.serve_engines.split(","):
         s = Server(budget_bytes=a.serve_budget_gb * 1e9, slots=a.serve_slots)
-        ids = [s.add_job(config(engine=eng, slices=a.slices if eng == "split" else 0, **j)) for j in jobs]
+        ids = [s.add_job(config(engine=eng, slices=a.serve_slices if eng == "split" else 0, **j)) for j in jobs]
         for job, t in stream:
             s.submit(ids[job], t)
         clocks = Clocks(0)
@@ -419,7 +422,7 @@ def serve_arm(a):
                       "workload": "cc_serving_%djobs_o16-%d_v4-6o_halfsym" % (a.serve, a.serve_o_max),
                       "jobs": a.serve, "requests_per_job": a.serve_requests, "arrival_rate_per_s": a.serve_rate,
                       "budget_gb": a.serve_budget_gb, "slots": a.serve_slots, "time_limit_s": a.serve_limit,
-                      "split_slices": a.slices,
+                      "split_slices": a.serve_slices,
                       "seed": a.seed, "engines": out, "energy_max_diff_split_vs_fp64_eh": diff,
                       "data": "synthetic (seeded)"}))
     return 0

@@ -158,6 +158,11 @@ __device__ __forceinline__ constexpr uint32_t idesc_bf16() {
          | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
 }
 
+// The same with the output width N (a multiple of 16, at most 256) as a value.
+__device__ __forceinline__ constexpr uint32_t idesc_bf16_n(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
+
 __device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
@@ -813,7 +818,6 @@ __global__ void __launch_bounds__(kKsThreads, 1) split_ks_kernel(const GemmParam
       int st = 0, buf = 0;
       uint32_t phase = 0, aphase = 0;
       bool ok = true;
-      constexpr uint32_t idesc = idesc_bf16<kKsBN>();
       // slot descriptors: slot 0's plus the slot offset in 16-byte units
       // (the address field holds shared-memory address / 16, below 2^14)
       const uint64_t ad0 = sdesc(smem_u32(sm.a[0])), bd0 = sdesc(smem_u32(sm.b[0]));
@@ -835,19 +839,22 @@ __global__ void __launch_bounds__(kKsThreads, 1) split_ks_kernel(const GemmParam
             tc_fence_after();
             const int base = st * S;
             const uint32_t fresh = kb == g0 ? 0u : 1u;
+            // One UMMA per A slice s and K step: B slices 1 .. S + 1 - s sit
+            // back to back in the stage (64 rows each), so one instruction of
+            // N = 64 (S + 1 - s) forms every product (s, t) with t <= S + 1 - s
+            // at once; with D at column 64 (s - 1) of the buffer, product
+            // (s, t) lands in columns 64 (s + t - 2), its level's accumulator.
+            // The first instruction of a group (s = 1, N = 64 S) spans every
+            // level and starts them all from zero.
+            const uint64_t b0 = bd0 + (uint64_t)base * kBStep;
 #pragma unroll
-            for (int l = 0; l <= L; ++l) {
-              const uint32_t d = tmem + (uint32_t)buf * buf_cols + (uint32_t)(l * kKsBN);
+            for (int s = 1; s <= S; ++s) {
+              const uint32_t d = tmem + (uint32_t)buf * buf_cols + (uint32_t)((s - 1) * kKsBN);
+              const uint64_t a0 = ad0 + (uint64_t)(base + s - 1) * kAStep;
 #pragma unroll
-              for (int s = (l + 2 - S > 1 ? l + 2 - S : 1); s <= (S < l + 1 ? S : l + 1); ++s) {
-                const int t = l + 2 - s;
-                const uint64_t a0 = ad0 + (uint64_t)(base + s - 1) * kAStep;
-                const uint64_t b0 = bd0 + (uint64_t)(base + t - 1) * kBStep;
-                const bool lead = s == (l + 2 - S > 1 ? l + 2 - S : 1);  // first product of the level
-#pragma unroll
-                for (int k = 0; k < BK / 16; ++k)
-                  umma(d, a0 + (uint64_t)(k * 2), b0 + (uint64_t)(k * 2), idesc, (lead && k == 0) ? fresh : 1u);
-              }
+              for (int k = 0; k < BK / 16; ++k)
+                umma(d, a0 + (uint64_t)(k * 2), b0 + (uint64_t)(k * 2), idesc_bf16_n(kKsBN * (S + 1 - s)),
+                     (s == 1 && k == 0) ? fresh : 1u);
             }
             umma_commit(&sm.empty[st]);
             if (++st == kStages) {
