@@ -35,6 +35,8 @@ constexpr int kSmallKElems = 2048;  // output elements per CTA
 constexpr int kSmallOutDim = 16;    // small outputs: at most 16 x 16 ...
 constexpr int kSmallOutMinK = 4096;  // ... with at least this K
 constexpr int kSmallOutChunk = 4096;  // K per work item
+constexpr int kGemvDim = 8;           // matrix-vector problems: one side at most this ...
+constexpr int kGemvMinK = 64;         // ... with K above this
 }  // namespace
 
 // Tile shapes: 64x64 for large problems, 64x16 / 16x64 / 16x16 for skinny ones
@@ -56,6 +58,9 @@ int f64_variant(int m, int n) { return (m < 48 ? 2 : 0) + (n < 48 ? 1 : 0); }
 // K, one CTA per K chunk holding the whole output (reduced in a fixed order).
 int f64_variant_planned(int m, int n, int k) {
   if (m <= kSmallOutDim && n <= kSmallOutDim && k >= kSmallOutMinK) return 7;
+  // matrix-vector shapes (one side <= 8, K > 64): one warp per output of the
+  // wide side, the wide operand's rows read once and coalesced
+  if (k > kGemvMinK && ((m <= kGemvDim && n > kSmallOutDim) || (n <= kGemvDim && m > kSmallOutDim))) return 8;
   return f64_variant(m, n, k);
 }
 int f64_tile_m(int variant) { return (variant & 2) ? 16 : 64; }
@@ -112,6 +117,58 @@ __global__ void __launch_bounds__(256) thin_gemm_f64_kernel(const GemmProblem* _
       for (int j = 0; j < kThinN; ++j) {
         if (j >= tn) break;
         double* c = kRows ? p.C + i * p.c_rs + j : p.C + (int64_t)j * p.c_rs + i;
+        const double v = __dmul_rn(p.alpha, acc[j]);
+        *c = p.accumulate ? __dadd_rn(*c, v) : v;
+      }
+    }
+  }
+}
+
+// Matrix-vector shapes (variant 8): one warp per output of the wide side --
+// column j of C when A is the thin operand (m <= 8), row i when B is (n <=
+// 8).  The lanes stride K, so the wide operand's row is read once and
+// coalesced when its K stride is 1; each lane keeps one partial sum per thin
+// row, and the warp adds them in a fixed butterfly order (deterministic).
+// Eight warps per CTA: a work item is eight consecutive wide-side outputs.
+__global__ void __launch_bounds__(256) gemv_f64_kernel(const GemmProblem* __restrict__ probs, int nprob,
+                                                       const int* __restrict__ block_first, int total_blocks) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int blk = blockIdx.x; blk < total_blocks; blk += gridDim.x) {
+    int lo = 0, hi = nprob - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (block_first[mid] <= blk) lo = mid; else hi = mid - 1;
+    }
+    const GemmProblem& p = probs[lo];
+    const bool a_thin = p.m <= kGemvDim && p.m <= p.n;
+    const int tn = a_thin ? p.m : p.n;
+    const int64_t wide = a_thin ? p.n : p.m;
+    const int64_t w = (int64_t)(blk - block_first[lo]) * 8 + warp;
+    if (w >= wide) continue;
+    const double* W = a_thin ? p.B + w * p.b_rs : p.A + w * p.a_rs;
+    const int64_t wcs = a_thin ? p.b_cs : p.a_cs;
+    const double* T = a_thin ? p.A : p.B;
+    const int64_t trs = a_thin ? p.a_rs : p.b_rs, tcs = a_thin ? p.a_cs : p.b_cs;
+    double acc[kGemvDim];
+#pragma unroll
+    for (int j = 0; j < kGemvDim; ++j) acc[j] = 0.0;
+    for (int64_t k = lane; k < p.k; k += 32) {
+      const double x = __ldg(W + k * wcs);
+#pragma unroll
+      for (int j = 0; j < kGemvDim; ++j)
+        if (j < tn) acc[j] = fma(x, __ldg(T + j * trs + k * tcs), acc[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < kGemvDim; ++j) {
+      if (j >= tn) break;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], o);
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int j = 0; j < kGemvDim; ++j) {
+        if (j >= tn) break;
+        double* c = a_thin ? p.C + (int64_t)j * p.c_rs + w : p.C + w * p.c_rs + j;
         const double v = __dmul_rn(p.alpha, acc[j]);
         *c = p.accumulate ? __dadd_rn(*c, v) : v;
       }
@@ -431,10 +488,10 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
     if (q.m <= 0 || q.n <= 0) continue;
     probs.push_back(q);
     int v = variants && i < variants->size() ? (*variants)[i] : -1;
-    if (v < -1 || v > 7) return fail(GBX_EINVAL, "FP64 tile variant %d", v);
+    if (v < -1 || v > 8) return fail(GBX_EINVAL, "FP64 tile variant %d", v);
     // the thin kernels need their shape limits
     if ((v == 4 && q.n > kThinN) || (v == 5 && q.m > kThinN) || (v == 6 && q.k > kSmallK) ||
-        (v == 7 && (q.m > kSmallOutDim || q.n > kSmallOutDim)))
+        (v == 7 && (q.m > kSmallOutDim || q.n > kSmallOutDim)) || (v == 8 && q.m > kGemvDim && q.n > kGemvDim))
       return fail(GBX_EINVAL, "FP64 tile variant %d does not fit %d x %d x %d", v, q.m, q.n, q.k);
     want.push_back(v);
   }
@@ -510,7 +567,7 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
   for (auto& q : probs)
     if (q.partial) q.partial = d_partial + ((intptr_t)q.partial - 1);
   // one launch per tile shape
-  for (int v = 0; v < 8; ++v) {
+  for (int v = 0; v < 9; ++v) {
     std::vector<GemmProblem> vp;
     std::vector<int> first;
     int64_t tiles = 0;
@@ -522,6 +579,7 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
       else if (v == 5) tiles += (q.n + 255) / 256;
       else if (v == 6) tiles += ((int64_t)q.m * q.n + kSmallKElems - 1) / kSmallKElems;
       else if (v == 7) tiles += q.ksplit;
+      else if (v == 8) tiles += ((q.m <= kGemvDim && q.m <= q.n ? (int64_t)q.n : (int64_t)q.m) + 7) / 8;
       else tiles += (int64_t)((q.m + f64_tile_m(v) - 1) / f64_tile_m(v)) * ((q.n + f64_tile_n(v) - 1) / f64_tile_n(v)) * q.ksplit;
     }
     if (vp.empty()) continue;
@@ -585,6 +643,10 @@ int F64Gemm::run(cudaStream_t st) const {
         small_out_gemm_f64_kernel<<<std::min(sb.total_tiles, 152 * 8), 256, 0, st>>>(sb.d_probs, sb.nprob,
                                                                                      sb.d_first, sb.total_tiles);
         break;
+      case 8:
+        gemv_f64_kernel<<<std::min(sb.total_tiles, 152 * 8), 256, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first,
+                                                                           sb.total_tiles);
+        break;
       default:
         thin_gemm_f64_kernel<false><<<std::min(sb.total_tiles, 152 * 8), 256, 0, st>>>(sb.d_probs, sb.nprob,
                                                                                        sb.d_first, sb.total_tiles);
@@ -613,6 +675,7 @@ int launch_one(int v, const GemmProblem* prob, const int* zero, int tiles, cudaS
     case 4: thin_gemm_f64_kernel<true><<<tgrid, 256, 0, st>>>(prob, 1, zero, tiles); break;
     case 6: small_k_gemm_f64_kernel<<<tgrid, 256, 0, st>>>(prob, 1, zero, tiles); break;
     case 7: small_out_gemm_f64_kernel<<<tgrid, 256, 0, st>>>(prob, 1, zero, tiles); break;
+    case 8: gemv_f64_kernel<<<tgrid, 256, 0, st>>>(prob, 1, zero, tiles); break;
     default: thin_gemm_f64_kernel<false><<<tgrid, 256, 0, st>>>(prob, 1, zero, tiles); break;
   }
   GBX_CUDA(cudaGetLastError());

@@ -633,6 +633,14 @@ int ContractionPlan::sizes(size_t* persist, size_t* arena, size_t* static_scratc
     split_problems(sp);
     size_t sp_keep = 0, sp_ws = 0;
     GBX_TRY(split_plan_sizes(sp, slices, a_static, b_static, &sp_keep, &sp_ws));
+    // the width autotuner tries every output width in the plan's region:
+    // room for the largest of them (split-K partial sums differ by width)
+    if (split_width == 0)
+      for (int w : {64, 128, 256}) {
+        for (auto& q : sp) q.width = w;
+        size_t k2 = 0, w2 = 0;
+        if (split_plan_sizes(sp, slices, a_static, b_static, &k2, &w2) == GBX_OK) sp_ws = std::max(sp_ws, w2);
+      }
     keep += sp_keep;
     ws += sp_ws;
   }

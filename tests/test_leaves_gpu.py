@@ -314,3 +314,26 @@ def test_config1_ladder_exact_spec(gbx, mode):
     else:
         assert err <= 1e-13 * np.abs(want).max(), err
     assert ctr.plan("a,b,e,f", "e,f,i,j", "a,b,i,j").flops == 1.189085184e9
+
+
+@pytest.mark.parametrize("m,n,k,acc", [(1, 7200, 1440, 1), (3, 500, 100, 0), (8, 1000, 4097, 1), (2000, 1, 300, 1),
+                                       (700, 5, 65, 0), (17, 8, 2000, 1)])
+def test_grouped_gemm_matrix_vector_shapes(gbx, m, n, k, acc):
+    """One side at most 8 with K above 64: one warp per output of the wide
+    side, lanes striding K, fixed-order reduction."""
+    from dtcf_gb300.leaves import Triple
+    rng = np.random.default_rng(m * 3 + n + k)
+    A, B, C = rng.standard_normal((m, k)), rng.standard_normal((n, k)), rng.standard_normal((m, n))
+    dA, dB, dC = dev(A), dev(B), dev(C)
+    gbx.grouped_gemm_f64([Triple(dA.data_ptr(), dB.data_ptr(), dC.data_ptr(), k, 1, k, 1, n, m, n, k, 0.25, acc)])
+    want = (C if acc else 0.0) + 0.25 * A @ B.T
+    got = host(dC).reshape(m, n)
+    np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-13 * np.sqrt(k))
+    # twice in a row: the same bits (deterministic reduction order)
+    dC2 = dev(C)
+    gbx.grouped_gemm_f64([Triple(dA.data_ptr(), dB.data_ptr(), dC2.data_ptr(), k, 1, k, 1, n, m, n, k, 0.25, acc)])
+    assert np.array_equal(host(dC2).reshape(m, n), got)
+    # strided operands through the leaf entry point (A transposed)
+    dC3 = dev(C)
+    gbx.local_contraction(m, n, k, dev(np.ascontiguousarray(A.T)), dB, dC3, 1, 1, 0.25)
+    np.testing.assert_allclose(host(dC3).reshape(m, n), C + 0.25 * A @ B.T, rtol=1e-12, atol=1e-13 * np.sqrt(k))
