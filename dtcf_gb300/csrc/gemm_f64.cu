@@ -35,8 +35,10 @@ constexpr int kSmallKElems = 2048;  // output elements per CTA
 constexpr int kSmallOutDim = 16;    // small outputs: at most 16 x 16 ...
 constexpr int kSmallOutMinK = 4096;  // ... with at least this K
 constexpr int kSmallOutChunk = 4096;  // K per work item
-constexpr int kGemvDim = 8;           // matrix-vector problems: one side at most this ...
+constexpr int kGemvDim = 2;           // matrix-vector problems: one side at most this ...
 constexpr int kGemvMinK = 64;         // ... with K above this
+constexpr int kGemvItems = 152 * 4;   // work items that keep every SM busy
+constexpr int kGemvMinChunk = 1024;   // smallest K range of a split
 }  // namespace
 
 // Tile shapes: 64x64 for large problems, 64x16 / 16x64 / 16x16 for skinny ones
@@ -58,7 +60,7 @@ int f64_variant(int m, int n) { return (m < 48 ? 2 : 0) + (n < 48 ? 1 : 0); }
 // K, one CTA per K chunk holding the whole output (reduced in a fixed order).
 int f64_variant_planned(int m, int n, int k) {
   if (m <= kSmallOutDim && n <= kSmallOutDim && k >= kSmallOutMinK) return 7;
-  // matrix-vector shapes (one side <= 8, K > 64): one warp per output of the
+  // matrix-vector shapes (one side <= 2, K > 64): one warp per output of the
   // wide side, the wide operand's rows read once and coalesced
   if (k > kGemvMinK && ((m <= kGemvDim && n > kSmallOutDim) || (n <= kGemvDim && m > kSmallOutDim))) return 8;
   return f64_variant(m, n, k);
@@ -125,11 +127,13 @@ __global__ void __launch_bounds__(256) thin_gemm_f64_kernel(const GemmProblem* _
 }
 
 // Matrix-vector shapes (variant 8): one warp per output of the wide side --
-// column j of C when A is the thin operand (m <= 8), row i when B is (n <=
-// 8).  The lanes stride K, so the wide operand's row is read once and
+// column j of C when A is the thin operand (m <= 2), row i when B is (n <=
+// 2).  The lanes stride K, so the wide operand's row is read once and
 // coalesced when its K stride is 1; each lane keeps one partial sum per thin
 // row, and the warp adds them in a fixed butterfly order (deterministic).
-// Eight warps per CTA: a work item is eight consecutive wide-side outputs.
+// Eight warps per CTA: a work item is eight consecutive wide-side outputs
+// over one K range; with several ranges (few outputs, long K) each writes
+// its raw sums to a partial slab that the split-K reduction adds in order.
 __global__ void __launch_bounds__(256) gemv_f64_kernel(const GemmProblem* __restrict__ probs, int nprob,
                                                        const int* __restrict__ block_first, int total_blocks) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -143,8 +147,12 @@ __global__ void __launch_bounds__(256) gemv_f64_kernel(const GemmProblem* __rest
     const bool a_thin = p.m <= kGemvDim && p.m <= p.n;
     const int tn = a_thin ? p.m : p.n;
     const int64_t wide = a_thin ? p.n : p.m;
-    const int64_t w = (int64_t)(blk - block_first[lo]) * 8 + warp;
+    const int64_t groups = (wide + 7) / 8;
+    const int64_t local = blk - block_first[lo];
+    const int kc = (int)(local / groups);
+    const int64_t w = (local - kc * groups) * 8 + warp;
     if (w >= wide) continue;
+    const int64_t k0 = (int64_t)kc * p.kchunk, k1 = min((int64_t)p.k, k0 + p.kchunk);
     const double* W = a_thin ? p.B + w * p.b_rs : p.A + w * p.a_rs;
     const int64_t wcs = a_thin ? p.b_cs : p.a_cs;
     const double* T = a_thin ? p.A : p.B;
@@ -152,7 +160,7 @@ __global__ void __launch_bounds__(256) gemv_f64_kernel(const GemmProblem* __rest
     double acc[kGemvDim];
 #pragma unroll
     for (int j = 0; j < kGemvDim; ++j) acc[j] = 0.0;
-    for (int64_t k = lane; k < p.k; k += 32) {
+    for (int64_t k = k0 + lane; k < k1; k += 32) {
       const double x = __ldg(W + k * wcs);
 #pragma unroll
       for (int j = 0; j < kGemvDim; ++j)
@@ -168,9 +176,14 @@ __global__ void __launch_bounds__(256) gemv_f64_kernel(const GemmProblem* __rest
 #pragma unroll
       for (int j = 0; j < kGemvDim; ++j) {
         if (j >= tn) break;
-        double* c = a_thin ? p.C + (int64_t)j * p.c_rs + w : p.C + w * p.c_rs + j;
-        const double v = __dmul_rn(p.alpha, acc[j]);
-        *c = p.accumulate ? __dadd_rn(*c, v) : v;
+        const int64_t row = a_thin ? j : w, col = a_thin ? w : j;
+        if (p.ksplit > 1) {
+          p.partial[(int64_t)kc * p.m * p.n + row * p.n + col] = acc[j];
+        } else {
+          double* c = p.C + row * p.c_rs + col;
+          const double v = __dmul_rn(p.alpha, acc[j]);
+          *c = p.accumulate ? __dadd_rn(*c, v) : v;
+        }
       }
     }
   }
@@ -469,6 +482,18 @@ int64_t f64_partial_elems(const std::vector<GemmProblem>& probs) {
       if (ks7 > 1) part += ks7 * q.m * q.n;
       continue;
     }
+    if (v == 8) {
+      const int64_t wide = q.m <= kGemvDim && q.m <= q.n ? q.n : q.m;
+      const int64_t groups = (wide + 7) / 8;
+      int64_t ks8 = 1;
+      if (groups < kGemvItems && q.k > 2 * kGemvMinChunk)
+        ks8 = std::min<int64_t>((kGemvItems + groups - 1) / groups, (q.k + kGemvMinChunk - 1) / kGemvMinChunk);
+      int64_t chunk = (q.k + ks8 - 1) / ks8;
+      chunk = (chunk + 31) / 32 * 32;
+      ks8 = std::max<int64_t>(1, (q.k + chunk - 1) / chunk);
+      if (ks8 > 1) part += ks8 * q.m * q.n;
+      continue;
+    }
     if (v >= 4) continue;
     int ks = 1, chunk = 0;
     f64_ksplit(q.k, out_tiles, &ks, &chunk);
@@ -514,6 +539,28 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
       q.kchunk = kSmallOutChunk;
       q.partial = nullptr;
       q.pad_ = 7;
+      if (ks > 1) {
+        q.partial = (double*)(intptr_t)(part_elems + 1);  // offset + 1, patched below
+        part_elems += (int64_t)ks * q.m * q.n;
+        red.push_back(i);
+        red_first.push_back((uint32_t)rc);
+        rc += ((uint64_t)q.m * q.n + kRedChunk - 1) / kRedChunk;
+      }
+      continue;
+    }
+    if (thin == 8) {  // matrix-vector: K ranges when the outputs are few
+      const int64_t wide = q.m <= kGemvDim && q.m <= q.n ? q.n : q.m;
+      const int64_t groups = (wide + 7) / 8;
+      ks = 1;
+      if (groups < kGemvItems && q.k > 2 * kGemvMinChunk)
+        ks = (int)std::min<int64_t>((kGemvItems + groups - 1) / groups, (q.k + kGemvMinChunk - 1) / kGemvMinChunk);
+      int chunk = (q.k + ks - 1) / ks;
+      chunk = (chunk + 31) / 32 * 32;
+      ks = std::max(1, (q.k + chunk - 1) / chunk);
+      q.ksplit = ks;
+      q.kchunk = chunk;
+      q.partial = nullptr;
+      q.pad_ = 8;
       if (ks > 1) {
         q.partial = (double*)(intptr_t)(part_elems + 1);  // offset + 1, patched below
         part_elems += (int64_t)ks * q.m * q.n;
@@ -579,7 +626,7 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
       else if (v == 5) tiles += (q.n + 255) / 256;
       else if (v == 6) tiles += ((int64_t)q.m * q.n + kSmallKElems - 1) / kSmallKElems;
       else if (v == 7) tiles += q.ksplit;
-      else if (v == 8) tiles += ((q.m <= kGemvDim && q.m <= q.n ? (int64_t)q.n : (int64_t)q.m) + 7) / 8;
+      else if (v == 8) tiles += ((q.m <= kGemvDim && q.m <= q.n ? (int64_t)q.n : (int64_t)q.m) + 7) / 8 * q.ksplit;
       else tiles += (int64_t)((q.m + f64_tile_m(v) - 1) / f64_tile_m(v)) * ((q.n + f64_tile_n(v) - 1) / f64_tile_n(v)) * q.ksplit;
     }
     if (vp.empty()) continue;

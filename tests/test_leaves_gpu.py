@@ -316,11 +316,12 @@ def test_config1_ladder_exact_spec(gbx, mode):
     assert ctr.plan("a,b,e,f", "e,f,i,j", "a,b,i,j").flops == 1.189085184e9
 
 
-@pytest.mark.parametrize("m,n,k,acc", [(1, 7200, 1440, 1), (3, 500, 100, 0), (8, 1000, 4097, 1), (2000, 1, 300, 1),
-                                       (700, 5, 65, 0), (17, 8, 2000, 1)])
+@pytest.mark.parametrize("m,n,k,acc", [(1, 7200, 1440, 1), (2, 30, 345000, 0), (1, 40, 100000, 1), (2000, 1, 300, 1),
+                                       (700, 2, 65, 0), (17, 1, 2000, 1), (3, 500, 100, 0)])
 def test_grouped_gemm_matrix_vector_shapes(gbx, m, n, k, acc):
-    """One side at most 8 with K above 64: one warp per output of the wide
-    side, lanes striding K, fixed-order reduction."""
+    """One side at most 2 with K above 64: one warp per output of the wide
+    side, lanes striding K, fixed-order reduction; few outputs with long K
+    split K into ranges reduced in a fixed order."""
     from dtcf_gb300.leaves import Triple
     rng = np.random.default_rng(m * 3 + n + k)
     A, B, C = rng.standard_normal((m, k)), rng.standard_normal((n, k)), rng.standard_normal((m, n))
