@@ -4,6 +4,8 @@
 #include "cc.h"
 #include "split.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <algorithm>
 #include <array>
 #include <atomic>
@@ -962,7 +964,12 @@ int gbx_cc_profile(gbx_cc_job* job, int cap, float* ms, double* flops, double* b
   for (auto& e : ev) GBX_CUDA(cudaEventCreate(&e));
   GBX_CUDA(cudaEventRecord(ev[0], st));
   for (int i = 0; i < n; ++i) {
-    GBX_TRY(job->steps[i](st));
+    // each step inside an NVTX range of its name, so that a profiler's
+    // launch list maps every kernel to its step
+    nvtxRangePushA(job->info[i].name.c_str());
+    const int rc = job->steps[i](st);
+    nvtxRangePop();
+    GBX_TRY(rc);
     GBX_CUDA(cudaEventRecord(ev[i + 1], st));
   }
   GBX_CUDA(cudaEventSynchronize(ev[n]));
