@@ -384,34 +384,39 @@ def serve_jobs(a):
     return jobs, list(zip(who.tolist(), arrivals.tolist()))
 
 
+def serve_once(a, eng, device=0):
+    """One serving run of the job mix on one engine: statistics and the
+    energy of every completed request."""
+    from dtcf_gb300.cc import config
+    from dtcf_gb300.serve import Server
+    jobs, stream = serve_jobs(a)
+    s = Server(budget_bytes=a.serve_budget_gb * 1e9, slots=a.serve_slots)
+    ids = [s.add_job(config(engine=eng, slices=a.serve_slices if eng == "split" else 0, **j)) for j in jobs]
+    for job, t in stream:
+        s.submit(ids[job], t)
+    clocks = Clocks(device)
+    clocks.start()
+    t0 = time.perf_counter()
+    s.run(time_limit_s=a.serve_limit)
+    wall = time.perf_counter() - t0
+    st = s.stats()
+    res = s.results()
+    fps = list(s.footprints)
+    s.close()
+    st["wall_s"] = wall
+    st["clocks"] = clocks.stop()
+    st["jobs_over_budget"] = sum(1 for f in fps if f > a.serve_budget_gb * 1e9)
+    return st, {(r["job"], r["iteration"]): r["energy"] for r in res if r["status"] == 0}
+
+
 def serve_arm(a):
     """The serving loop over the job mix, once per engine; one JSON line."""
     import torch
-    from dtcf_gb300.cc import config
-    from dtcf_gb300.serve import Server
     torch.cuda.set_device(0)
-    jobs, stream = serve_jobs(a)
     out, energies = {}, {}
     for eng in a.serve_engines.split(","):
-        s = Server(budget_bytes=a.serve_budget_gb * 1e9, slots=a.serve_slots)
-        ids = [s.add_job(config(engine=eng, slices=a.serve_slices if eng == "split" else 0, **j)) for j in jobs]
-        for job, t in stream:
-            s.submit(ids[job], t)
-        clocks = Clocks(0)
-        clocks.start()
-        t0 = time.perf_counter()
-        s.run(time_limit_s=a.serve_limit)
-        wall = time.perf_counter() - t0
-        st = s.stats()
-        res = s.results()
-        fps = list(s.footprints)
-        s.close()
-        st["wall_s"] = wall
-        st["clocks"] = clocks.stop()
-        st["jobs_over_budget"] = sum(1 for f in fps if f > a.serve_budget_gb * 1e9)
-        out[eng] = st
-        energies[eng] = {(r["job"], r["iteration"]): r["energy"] for r in res if r["status"] == 0}
-        print(json.dumps({"engine": eng, **st}), file=sys.stderr, flush=True)
+        out[eng], energies[eng] = serve_once(a, eng)
+        print(json.dumps({"engine": eng, **out[eng]}), file=sys.stderr, flush=True)
     diff = None
     if len(energies) == 2:
         e1, e2 = energies.values()
@@ -593,6 +598,30 @@ def main():
             "eff_tflops": st.flops_per_iter * iters / 1e12, "flops_per_iter": st.flops_per_iter,
             "gpu_launches": int(st.launches_per_iter * a.steps), "clocks": clocks, "roofline": roofline, "e2e": e2e,
             "split_contraction_err": split_err}
+    # serving under load (the metric's p99 request latency): the config-5 job
+    # mix -- 64 jobs, o uniform in [16, 64], v = o * U[4, 6], 8-irrep symmetry
+    # on every other job, CCD or CCSD -- two iteration requests each in a
+    # Poisson stream at 20 requests/s (above what the server completes, so
+    # the GPU stays saturated), 160 GB admission budget, 4 stream slots, the
+    # split engine (5 slices); one process on one GPU
+    if world == 1 and primary == "split":
+        for R in results.values():
+            R["job"].close()
+        sa = argparse.Namespace(**vars(a))
+        sa.serve, sa.serve_requests, sa.serve_rate, sa.serve_limit = 64, 2, 20.0, 180.0
+        try:
+            sst, _ = serve_once(sa, "split", local)
+            line["serving"] = {"workload": "cc_serving_64jobs_o16-64_v4-6o_halfsym", "engine": "split",
+                               "slices": sa.serve_slices, "requests": sst["requests"],
+                               "completed": sst["completed"], "rejected_over_budget": sst["rejected"],
+                               "arrival_rate_per_s": sa.serve_rate, "iter_per_s": sst["iter_per_s"],
+                               "latency_p50_s": sst["latency_p50_s"], "latency_p99_s": sst["latency_p99_s"],
+                               "service_p50_s": sst["service_p50_s"], "makespan_s": sst["makespan_s"],
+                               "evictions": sst["evictions"], "build_s_total": sst["build_s_total"],
+                               "peak_planned_gb": sst["peak_planned_bytes"] / 1e9, "budget_gb": sa.serve_budget_gb,
+                               "clocks": sst["clocks"]}
+        except Exception as ex:  # the serving run must not hide the CCSD number
+            line["serving"] = {"failed": str(ex)}
     if "fp64" in results and primary != "fp64":
         F = results["fp64"]
         line["fp64_iter_s"] = sum_over_ranks(1000.0 / F["ms"])

@@ -1,12 +1,14 @@
 // Serving loop for CC iteration requests (include/gbx_serve.h).
 //
-// Two host threads.  The dispatcher (the caller of gbx_server_run) polls
+// Host threads: the dispatcher (the caller of gbx_server_run) polls
 // completion events, admits waiting jobs by planned footprint against the
 // byte budget, and puts the earliest runnable request on every free stream
 // slot: one graph launch of the job's iteration, an asynchronous read of its
-// energy into pinned memory, then an event.  The builder thread creates
-// admitted jobs (host planning, integrals, constant operands, graph capture)
-// and checks and destroys finished ones, so that neither stalls dispatch.
+// energy into pinned memory, then an event.  Three builder threads create
+// admitted jobs (host planning, integrals, constant operands, graph capture;
+// up to three at once, so one large job does not hold up the others), evict
+// idle jobs and check and destroy finished ones, so that none of this stalls
+// dispatch.
 //
 // Idle jobs do not hold the budget: when a job waiting for admission does
 // not fit, resident jobs with no request waiting (least recently used first)
@@ -38,6 +40,7 @@ namespace {
 using Clock = std::chrono::steady_clock;
 
 constexpr int kPending = 1;  // request status while it has not finished
+constexpr int kBuilders = 3;  // builder threads: job builds in flight at once
 
 struct Req {
   int job = 0, iter = 0;
@@ -91,7 +94,7 @@ struct gbx_server {
   bool ran = false;
   int device = 0;
   cudaStream_t mem_stream = nullptr;  // stream-ordered allocations of job state
-  // builder thread queues (guarded by mu)
+  // builder threads' queues (guarded by mu)
   std::mutex mu;
   std::condition_variable cv;
   std::deque<int> to_build, to_destroy, to_evict;
@@ -99,7 +102,7 @@ struct gbx_server {
   bool stop = false;
 
   // Saves an idle job's amplitudes to pinned host memory and releases its
-  // device state (builder thread).
+  // device state (a builder thread).
   int evict(Job& j) {
     int rc = gbx_cc_amplitude_elems(j.h, &j.n1, &j.n2);
     if (rc == GBX_OK && !j.h_t2) {
@@ -269,8 +272,9 @@ int gbx_server_run(gbx_server* s, double time_limit_s) {
   }
   if (rc == GBX_OK && cudaMallocHost((void**)&pinned, sizeof(double) * nslot) != cudaSuccess)
     rc = fail(GBX_ECUDA, "pinned buffer allocation failed");
-  std::thread worker;
-  if (rc == GBX_OK) worker = std::thread([s] { s->builder(); });
+  std::vector<std::thread> workers;
+  if (rc == GBX_OK)
+    for (int b = 0; b < kBuilders; ++b) workers.emplace_back([s] { s->builder(); });
 
   double planned = 0.0, measured = 0.0;
   int building = 0, evicting = 0, finished_reqs = 0;
@@ -287,7 +291,7 @@ int gbx_server_run(gbx_server* s, double time_limit_s) {
     }
     j.next = (int)j.reqs.size();
   };
-  // results of the builder thread: builds done, jobs destroyed
+  // results of the builder threads: builds done, jobs evicted or destroyed
   auto collect = [&]() -> bool {
     bool any = false;
     std::lock_guard<std::mutex> lk(s->mu);
@@ -369,9 +373,9 @@ int gbx_server_run(gbx_server* s, double time_limit_s) {
       }
     }
     if (collect()) progress = true;
-    // admission: first fit in order of first arrival, one build at a time;
+    // admission: first fit in order of first arrival, up to kBuilders builds at a time;
     // the first job that does not fit may evict idle jobs to make room
-    if (building == 0 && evicting == 0) {
+    if (building < kBuilders && evicting == 0) {
       bool tried_evict = false;
       for (int jb : job_order) {
         Job& j = s->jobs[jb];
@@ -478,8 +482,8 @@ int gbx_server_run(gbx_server* s, double time_limit_s) {
   }
   for (auto& r : s->reqs)
     if (r.status == kPending) r.status = timed_out ? GBX_ETIMEOUT : GBX_EINVAL;
-  if (worker.joinable()) {
-    // builds still queued or running end first (polled: the builder does not
+  if (!workers.empty()) {
+    // builds still queued or running end first (polled: the builders do not
     // signal this thread), then every job still resident is released
     for (;;) {
       collect();
@@ -491,9 +495,9 @@ int gbx_server_run(gbx_server* s, double time_limit_s) {
       for (size_t jb = 0; jb < s->jobs.size(); ++jb)
         if (s->jobs[jb].h && s->jobs[jb].state != JobState::Finished) s->to_destroy.push_back((int)jb);
       s->stop = true;
-      s->cv.notify_one();
+      s->cv.notify_all();
     }
-    worker.join();
+    for (auto& w : workers) w.join();
     collect();
   }
   for (int i = 0; i < nslot; ++i) {
