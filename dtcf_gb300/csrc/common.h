@@ -92,11 +92,6 @@ struct MoveDesc4 {
   double scale;
 };
 
-// Launch geometry of moves of at most four dimensions: one CTA of
-// kMoveThreads threads per chunk of kMove4Chunk elements of one move.
-constexpr int kMoveThreads = 256;
-constexpr int kMove4Chunk = 4096;
-
 // A set of moves uploaded to the device with its launch schedule.  When every
 // move has at most four dimensions the compact descriptors and a chunk ->
 // descriptor table are uploaded instead of the general ones.

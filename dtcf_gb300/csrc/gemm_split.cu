@@ -62,16 +62,6 @@ struct SplitRowSet {   // one operand of one problem for the split kernel
   int64_t ld;          // source row stride (elements)
 };
 
-// One row set of a gathered split: the packed rows [a_off, a_off + rows * K)
-// of a plan operand and where their slices and exponents go.
-struct GatherSet {
-  int64_t a_off;
-  int64_t rows, K, Kp, slice_stride;
-  FastDiv fK;
-  __nv_bfloat16* dst;
-  int* exps;
-};
-
 struct DevProblem {
   int M, N, K, nkb;
   int tiles_m, tiles_n;
@@ -1146,113 +1136,6 @@ __global__ void __launch_bounds__(256) split_short_rows_kernel(const SplitRowSet
   }
 }
 
-// ---- gathered operand split --------------------------------------------
-//
-// A changing plan operand is normally packed (a tile move into a row-major
-// FP64 matrix), then split from the packed matrix: one pass for the row
-// exponents, one for the digits.  The gathered split walks the pack's own
-// move descriptors instead and reads every element straight from the stored
-// tiles: the exponent pass reduces each packed row's largest exponent, the
-// digit pass writes the slices at the element's packed position; the packed
-// FP64 matrix is never written.  A move copies +-x, so the sign bit is
-// flipped on the integer pipe before the split.  Elements of one k-slot of a
-// warp are consecutive in the move's order, in which packed rows never
-// decrease (row dimensions have the larger packed strides), so equal rows
-// form runs: a segmented warp maximum leaves one atomicMax per run.
-
-// Zeroes the exponents of every row of the sets and the slices' K padding
-// (full: whole rows, when the pack leaves elements unwritten).  One warp per
-// row.
-__global__ void __launch_bounds__(256) gather_zero_kernel(const GatherSet* __restrict__ sets, int nsets,
-                                                          const int64_t* __restrict__ row_first, int64_t total_rows,
-                                                          int S, int full) {
-  const int lane = threadIdx.x & 31;
-  const int64_t nwarps = (int64_t)gridDim.x * 8;
-  for (int64_t rg = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5); rg < total_rows; rg += nwarps) {
-    int lo = 0, hi = nsets - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (row_first[mid] <= rg) lo = mid; else hi = mid - 1;
-    }
-    const GatherSet& gs = sets[lo];
-    const int64_t row = rg - row_first[lo];
-    if (lane == 0) gs.exps[row] = 0;
-    const int64_t c0 = full ? 0 : gs.K;
-    for (int sl = 0; sl < S; ++sl) {
-      __nv_bfloat16* d = gs.dst + sl * gs.slice_stride + row * gs.Kp;
-      for (int64_t c = c0 + lane; c < gs.Kp; c += 32) d[c] = __int2bfloat16_rn(0);
-    }
-  }
-}
-
-template <bool kDigits>
-__global__ void __launch_bounds__(kMoveThreads) gather_split_kernel(const MoveDesc4* __restrict__ descs,
-                                                                    const uint32_t* __restrict__ chunk_desc,
-                                                                    uint32_t nchunks, const int* __restrict__ desc_set,
-                                                                    const GatherSet* __restrict__ sets,
-                                                                    const double* __restrict__ src, int S) {
-  constexpr int kPer = 8;
-  constexpr int kBatches = kMove4Chunk / (kMoveThreads * kPer);
-  const int lane = threadIdx.x & 31;
-  const int F = 7 + 8 * (S - 1);
-  for (uint32_t chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
-    const uint32_t di = __ldg(chunk_desc + chunk);
-    const MoveDesc4* __restrict__ md = descs + di;
-    const GatherSet& gs = sets[__ldg(desc_set + di)];
-    const uint32_t n = md->n;
-    const uint32_t base = (chunk - md->first) * kMove4Chunk;
-    const FastDiv d1 = md->div[1], d2 = md->div[2], d3 = md->div[3];
-    const int64_t s0 = md->sstr[0], s1 = md->sstr[1], s2 = md->sstr[2], s3 = md->sstr[3];
-    const int64_t t0 = md->dstr[0], t1 = md->dstr[1], t2 = md->dstr[2], t3 = md->dstr[3];
-    const double* __restrict__ sp = src + md->src;
-    const int64_t rel0 = md->dst - gs.a_off;  // packed position of the move's first element in its set
-    const long long flip = (long long)((unsigned long long)__double_as_longlong(md->scale) & 0x8000000000000000ull);
-    const FastDiv fK = gs.fK;
-#pragma unroll 1
-    for (int bt = 0; bt < kBatches; ++bt) {
-      int64_t so[kPer];
-      uint32_t rel[kPer];
-      bool in[kPer];
-#pragma unroll
-      for (int k = 0; k < kPer; ++k) {
-        const uint32_t e = base + (uint32_t)((bt * kPer + k) * kMoveThreads) + threadIdx.x;
-        in[k] = e < n;
-        const uint32_t r = in[k] ? e : 0;
-        const uint32_t q3 = d3.div(r), c3 = r - q3 * d3.d;
-        const uint32_t q2 = d2.div(q3), c2 = q3 - q2 * d2.d;
-        const uint32_t c0 = d1.div(q2), c1 = q2 - c0 * d1.d;
-        so[k] = (int64_t)c0 * s0 + (int64_t)c1 * s1 + (int64_t)c2 * s2 + (int64_t)c3 * s3;
-        rel[k] = (uint32_t)(rel0 + (int64_t)c0 * t0 + (int64_t)c1 * t1 + (int64_t)c2 * t2 + (int64_t)c3 * t3);
-      }
-      long long x[kPer];
-#pragma unroll
-      for (int k = 0; k < kPer; ++k) x[k] = in[k] ? (__double_as_longlong(__ldg(sp + so[k])) ^ flip) : 0;
-#pragma unroll
-      for (int k = 0; k < kPer; ++k) {
-        const int row = in[k] ? (int)fK.div(rel[k]) : -1;
-        if (kDigits) {
-          if (in[k]) {
-            const int64_t col = (int64_t)rel[k] - (int64_t)row * gs.K;
-            write_digits(x[k], (uint32_t)__ldg(gs.exps + row), F, S, gs.dst + (int64_t)row * gs.Kp + col,
-                         gs.slice_stride);
-          }
-        } else {
-          uint32_t v = (uint32_t)((x[k] >> 52) & 0x7FF);
-          // segmented maximum over runs of equal rows, then one atomic per run
-#pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t ov = __shfl_up_sync(0xffffffffu, v, o);
-            const int orow = __shfl_up_sync(0xffffffffu, row, o);
-            if (lane >= o && orow == row) v = max(v, ov);
-          }
-          const int nrow = __shfl_down_sync(0xffffffffu, row, 1);
-          if ((lane == 31 || nrow != row) && row >= 0 && v != 0) atomicMax(gs.exps + row, (int)v);
-        }
-      }
-    }
-  }
-}
-
 PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   if (!fn) {
@@ -1337,15 +1220,6 @@ struct SplitPlan {
   int nsets = 0;
   int64_t rows_a = 0, rows_b = 0;  // (row, K chunk) work items per side
   std::vector<std::pair<void*, size_t>> exp_ranges_a, exp_ranges_b;  // exponent words reset before a split
-  std::vector<SplitRowSet> host_sets[2];  // every row set (long and short) from plan A / plan B
-  struct Gather {                         // gathered split of one side (split_gather_prepare)
-    GatherSet* d_sets = nullptr;
-    int* d_desc_set = nullptr;
-    int64_t* d_row_first = nullptr;
-    int nsets = 0;
-    int64_t rows = 0;
-    bool full_zero = false;
-  } gather[2];
   std::vector<SplitLaunch> launches;
   DevProblem* d_all = nullptr;  // every problem, for the split-K reduction
   int* d_err = nullptr;
@@ -1355,11 +1229,6 @@ struct SplitPlan {
   int64_t red_total = 0;
   double bytes = 0.0;
   ~SplitPlan() {
-    for (auto& g : gather) {
-      dev_free(g.d_sets);
-      dev_free(g.d_desc_set);
-      dev_free(g.d_row_first);
-    }
     dev_free(d_red_prob);
     dev_free(d_red_first);
     dev_free(d_persist);
@@ -1605,10 +1474,6 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
     sp->nred = (int)red.size();
     sp->red_total = red_total;
   }
-  sp->host_sets[0] = sa;
-  sp->host_sets[0].insert(sp->host_sets[0].end(), ssa.begin(), ssa.end());
-  sp->host_sets[1] = sb;
-  sp->host_sets[1].insert(sp->host_sets[1].end(), ssb.begin(), ssb.end());
   sp->nsets = (int)probs.size();
   sp->rows_a = ra;
   sp->rows_b = rb;
@@ -1699,81 +1564,6 @@ int split_operands(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st) {
       GBX_CUDA(cudaGetLastError());
     }
   }
-  return GBX_OK;
-}
-
-int split_gather_prepare(SplitPlan* sp, int side, const MoveSet& pack, const double* packed_base, bool full_zero,
-                         bool* ok) {
-  *ok = false;
-  if (!sp || side < 0 || side > 1 || !pack.d_desc4 || !pack.d_chunk_desc || pack.ndesc == 0 || !packed_base)
-    return GBX_OK;
-  const std::vector<SplitRowSet>& hs = sp->host_sets[side];
-  if (hs.empty()) return GBX_OK;
-  std::vector<GatherSet> gs;
-  std::vector<int64_t> row_first;
-  int64_t rows = 0;
-  for (const SplitRowSet& r : hs) {
-    const int64_t a_off = r.src - packed_base;
-    if (a_off < 0 || r.ld != r.K || r.K < 1 || r.rows * r.K >= ((int64_t)1 << 31) || r.K >= ((int64_t)1 << 31))
-      return GBX_OK;
-    GatherSet g;
-    g.a_off = a_off;
-    g.rows = r.rows;
-    g.K = r.K;
-    g.Kp = r.Kp;
-    g.slice_stride = r.slice_stride;
-    g.fK = FastDiv::make((uint32_t)r.K);
-    g.dst = r.dst;
-    g.exps = r.exps;
-    gs.push_back(g);
-    row_first.push_back(rows);
-    rows += r.rows;
-  }
-  // every move copies +-x into exactly one row set
-  std::vector<int> desc_set(pack.host.size(), -1);
-  for (size_t i = 0; i < pack.host.size(); ++i) {
-    const MoveDesc& m = pack.host[i];
-    if (m.op != 0 || (m.scale != 1.0 && m.scale != -1.0) || m.rank > 4) return GBX_OK;
-    if (m.n == 0) {
-      desc_set[i] = 0;
-      continue;
-    }
-    int64_t hi = m.dst;
-    for (int d = 0; d < m.rank; ++d) hi += (int64_t)(m.ext[d] - 1) * m.dstr[d];
-    for (size_t k = 0; k < gs.size(); ++k)
-      if (m.dst >= gs[k].a_off && hi < gs[k].a_off + gs[k].rows * gs[k].K) desc_set[i] = (int)k;
-    if (desc_set[i] < 0) return GBX_OK;
-  }
-  SplitPlan::Gather& g = sp->gather[side];
-  GBX_TRY(dev_alloc((void**)&g.d_sets, sizeof(GatherSet) * gs.size()));
-  GBX_TRY(dev_alloc((void**)&g.d_desc_set, sizeof(int) * desc_set.size()));
-  GBX_TRY(dev_alloc((void**)&g.d_row_first, sizeof(int64_t) * row_first.size()));
-  GBX_CUDA(cudaMemcpy(g.d_sets, gs.data(), sizeof(GatherSet) * gs.size(), cudaMemcpyHostToDevice));
-  GBX_CUDA(cudaMemcpy(g.d_desc_set, desc_set.data(), sizeof(int) * desc_set.size(), cudaMemcpyHostToDevice));
-  GBX_CUDA(cudaMemcpy(g.d_row_first, row_first.data(), sizeof(int64_t) * row_first.size(), cudaMemcpyHostToDevice));
-  g.nsets = (int)gs.size();
-  g.rows = rows;
-  g.full_zero = full_zero;
-  *ok = true;
-  return GBX_OK;
-}
-
-int split_gather(SplitPlan* sp, int side, const MoveSet& pack, const double* src, cudaStream_t st) {
-  const SplitPlan::Gather& g = sp->gather[side];
-  if (!g.d_sets) return fail(GBX_EINVAL, "gathered split not prepared");
-  if (g.rows > 0) {
-    const int grid = (int)std::min<int64_t>((g.rows + 7) / 8, 152 * 16);
-    gather_zero_kernel<<<grid, 256, 0, st>>>(g.d_sets, g.nsets, g.d_row_first, g.rows, sp->S, g.full_zero ? 1 : 0);
-    GBX_CUDA(cudaGetLastError());
-  }
-  if (pack.nchunks == 0) return GBX_OK;
-  const int grid = (int)std::min<uint32_t>(pack.nchunks, 152u * 8u);
-  gather_split_kernel<false><<<grid, kMoveThreads, 0, st>>>(pack.d_desc4, pack.d_chunk_desc, pack.nchunks,
-                                                            g.d_desc_set, g.d_sets, src, sp->S);
-  GBX_CUDA(cudaGetLastError());
-  gather_split_kernel<true><<<grid, kMoveThreads, 0, st>>>(pack.d_desc4, pack.d_chunk_desc, pack.nchunks,
-                                                           g.d_desc_set, g.d_sets, src, sp->S);
-  GBX_CUDA(cudaGetLastError());
   return GBX_OK;
 }
 

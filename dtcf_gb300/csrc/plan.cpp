@@ -741,7 +741,6 @@ int ContractionPlan::build(unsigned char* arena, unsigned char* static_scratch) 
     split_arena_cap = ws > off ? ws - off : 0;
     GBX_TRY(create_split_plan(sp, slices, &split, &mem));
   }
-  GBX_TRY(prepare_gather());
   // uploads and zero fills above ran on the legacy default stream: finish
   // them before any other stream touches the plan's buffers
   GBX_CUDA(cudaStreamSynchronize(cudaStreamLegacy));
@@ -805,8 +804,6 @@ int ContractionPlan::tune_split(cudaStream_t st, int reps) {
   split_width = best_w;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  // the gathered split belongs to the split plan kept
-  if (rc == GBX_OK) rc = prepare_gather();
   return rc;
 }
 
@@ -841,14 +838,6 @@ int ContractionPlan::stage(const double* dA, const double* dB, cudaStream_t st) 
   return GBX_OK;
 }
 
-int ContractionPlan::prepare_gather() {
-  gather_a = gather_b = false;
-  if (direct || !split || n_f64_groups > 0) return GBX_OK;
-  if (!a_static) GBX_TRY(split_gather_prepare(split, 0, packA, d_Abig, a_needs_zero, &gather_a));
-  if (!b_static) GBX_TRY(split_gather_prepare(split, 1, packB, d_Bbig, b_needs_zero, &gather_b));
-  return GBX_OK;
-}
-
 int ContractionPlan::execute(const double* dA, const double* dB, double* dC, double alpha, cudaStream_t st) {
   if (direct) {
     if (!dA || !dB || !dC) return fail(GBX_EINVAL, "contraction operand without device memory");
@@ -857,23 +846,16 @@ int ContractionPlan::execute(const double* dA, const double* dB, double* dC, dou
   if (f64.nprob == 0 && !split) return GBX_OK;
   const bool skipA = a_static && static_ready, skipB = b_static && static_ready;
   if ((!skipA && !dA) || (!skipB && !dB)) return fail(GBX_EINVAL, "contraction operand without device memory");
-  // an operand that only the split engine reads is split straight from its
-  // tiles (gathered split); otherwise it is packed first
-  const bool gA = !skipA && gather_a, gB = !skipB && gather_b;
-  if (!skipA && !gA) {
+  if (!skipA) {
     if (a_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Abig, 0, sizeof(double) * a_elems, st));
     GBX_TRY(run_moves(packA, dA, d_Abig, st));
   }
-  if (!skipB && !gB) {
+  if (!skipB) {
     if (b_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Bbig, 0, sizeof(double) * b_elems, st));
     GBX_TRY(run_moves(packB, dB, d_Bbig, st));
   }
   GBX_TRY(f64.run(st));
-  if (split) {
-    if (gA) GBX_TRY(split_gather(split, 0, packA, dA, st));
-    if (gB) GBX_TRY(split_gather(split, 1, packB, dB, st));
-    GBX_TRY(run_split_plan(split, !skipA && !gA, !skipB && !gB, st));
-  }
+  if (split) GBX_TRY(run_split_plan(split, !skipA, !skipB, st));
   return run_moves_scaled(unpackC, d_Cbig, dC, alpha, st);
 }
 

@@ -175,10 +175,6 @@ struct ContractionPlan {
   // fastest.  Call right after prepare_static, while the static scratch
   // still holds this plan's constant operands; timing runs on st.
   int tune_split(cudaStream_t st, int reps = 3);
-  // Changing operands read only by split groups are split straight from
-  // their tiles (no packed FP64 copy); set by build() and tune_split().
-  bool gather_a = false, gather_b = false;
-  int prepare_gather();
 
  private:
   void split_problems(std::vector<SplitProblem>& sp) const;

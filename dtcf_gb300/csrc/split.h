@@ -42,17 +42,6 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
 int run_split_plan(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st);
 // Only the split kernels (for operands that stay constant afterwards).
 int split_operands(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st);
-// Gathered split of one plan operand (side 0: the plan's A, 1: its B): the
-// slices and row exponents come straight from the operand's stored tiles
-// through the plan's pack moves, with no packed FP64 copy in between.
-// split_gather_prepare checks once that the pack fits (moves of at most four
-// dimensions that copy +-x, each inside one row set whose rows are the
-// packed rows) and uploads the move -> row set table; *ok = false means the
-// plan keeps packing.  packed_base: the packed buffer the row sets point
-// into; full_zero: the pack leaves elements unwritten (they split to zero).
-int split_gather_prepare(SplitPlan* sp, int side, const MoveSet& pack, const double* packed_base, bool full_zero,
-                         bool* ok);
-int split_gather(SplitPlan* sp, int side, const MoveSet& pack, const double* src, cudaStream_t st);
 void destroy_split_plan(SplitPlan* sp);
 // Force the output tile width of plans created afterwards (0 = model).
 int split_set_width(int bn);

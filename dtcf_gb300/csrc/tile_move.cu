@@ -16,7 +16,9 @@
 namespace gbx {
 
 namespace {
+constexpr int kMoveThreads = 256;
 constexpr int kMoveChunk = 2048;   // elements per CTA (general moves)
+constexpr int kMove4Chunk = 4096;  // elements per CTA (moves of at most four dimensions)
 }  // namespace
 
 MoveDesc make_move(int rank, const int64_t* ext, const int64_t* sstr, const int64_t* dstr, int64_t src,
