@@ -562,10 +562,13 @@ __global__ void __launch_bounds__(kThinThreads, 1) split_thin_kernel(const GemmP
   Sm& sm = *reinterpret_cast<Sm*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int S = P.S, L = P.L;
+  // a stage holds one tile's S (A slice, B slice) pairs, the B slices back
+  // to back, behind one full and one empty barrier
+  const int stages = kThinSlots / S;
   constexpr uint32_t kTx = (BM + kThinBN) * TBK * 2;
   constexpr uint32_t kCols = 512;
   if (threadIdx.x == 0) {
-    for (int i = 0; i < kThinSlots; ++i) {
+    for (int i = 0; i < stages; ++i) {
       mbar_init(&sm.full[i], 1);
       mbar_init(&sm.empty[i], 1);
     }
@@ -589,34 +592,34 @@ __global__ void __launch_bounds__(kThinThreads, 1) split_thin_kernel(const GemmP
 
   if (warp == 0) {
     if (lane == 0) {
-      int slot = 0;
+      int st = 0;
       uint32_t phase = 0;
       bool ok = true;
       for (int tile = blockIdx.x; tile < P.total_tiles && ok; tile += gridDim.x) {
         const TileInfo ti = decode_tile<kThinBN>(P, tile);
         const CUtensorMap* ma = P.maps + 2 * ti.p;
         const CUtensorMap* mb = P.maps + 2 * ti.p + 1;
+        if (!mbar_wait(&sm.empty[st], phase ^ 1, P.err, 11)) {
+          ok = false;
+          break;
+        }
+        mbar_expect_tx(&sm.full[st], (uint32_t)S * kTx);
         for (int s = 0; s < S; ++s) {
-          if (!mbar_wait(&sm.empty[slot], phase ^ 1, P.err, 11)) {
-            ok = false;
-            break;
-          }
-          mbar_expect_tx(&sm.full[slot], kTx);
-          tma_load_3d(sm.a[slot], ma, &sm.full[slot], 0, ti.m0, s);
-          tma_load_3d(sm.b[slot], mb, &sm.full[slot], 0, ti.n0, s);
-          if (++slot == kThinSlots) {
-            slot = 0;
-            phase ^= 1;
-          }
+          tma_load_3d(sm.a[st * S + s], ma, &sm.full[st], 0, ti.m0, s);
+          tma_load_3d(sm.b[st * S + s], mb, &sm.full[st], 0, ti.n0, s);
+        }
+        if (++st == stages) {
+          st = 0;
+          phase ^= 1;
         }
       }
-      for (int i = 0; i < kThinSlots; ++i) {
-        if (--slot < 0) {
-          slot = kThinSlots - 1;
+      for (int i = 0; i < stages; ++i) {
+        if (--st < 0) {
+          st = stages - 1;
           phase ^= 1;
         }
         long long t0 = clock64();
-        while (!mbar_try_wait(&sm.full[slot], phase) && !mbar_try_wait(&sm.empty[slot], phase)) {
+        while (!mbar_try_wait(&sm.full[st], phase) && !mbar_try_wait(&sm.empty[st], phase)) {
           if (clock64() - t0 > kWaitCycles) {
             atomicCAS(P.err, 0, 15);
             break;
@@ -626,44 +629,35 @@ __global__ void __launch_bounds__(kThinThreads, 1) split_thin_kernel(const GemmP
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      int slot = 0, buf = 0;
+      int st = 0, buf = 0;
       uint32_t phase = 0, aphase = 0;
       bool ok = true;
-      constexpr uint32_t idesc = idesc_bf16<kThinBN>();
       for (int tile = blockIdx.x; tile < P.total_tiles && ok; tile += gridDim.x) {
-        // the tile's S slices occupy S consecutive ring slots
-        int sl[8];
-        for (int s = 0; s < S; ++s) {
-          sl[s] = slot;
-          if (!mbar_wait(&sm.full[slot], phase, P.err, 13)) {
-            ok = false;
-            break;
-          }
-          if (++slot == kThinSlots) {
-            slot = 0;
-            phase ^= 1;
-          }
-        }
-        if (!ok) break;
+        if (!mbar_wait(&sm.full[st], phase, P.err, 13)) break;
         if (!mbar_wait(&sm.accempty[buf], aphase ^ 1, P.err, 12)) break;
         tc_fence_after();
-        for (int l = 0; l <= L; ++l) {
-          const uint32_t d = tmem + (uint32_t)buf * buf_cols + (uint32_t)(l * kThinBN);
-          bool first = true;
-          for (int s = max(1, l + 2 - S); s <= min(S, l + 1); ++s) {
-            const int t = l + 2 - s;
-            const uint32_t as = smem_u32(sm.a[sl[s - 1]]), bs = smem_u32(sm.b[sl[t - 1]]);
-            const uint64_t a0 = TBK == 64 ? sdesc(as) : sdesc64(as);
-            const uint64_t b0 = TBK == 64 ? sdesc(bs) : sdesc64(bs);
+        // one UMMA per A slice s and K step over B slices 1 .. S + 1 - s
+        // (N = 32 (S + 1 - s)) with D at column 32 (s - 1): product (s, t)
+        // lands in level s + t - 2's columns; the first (s = 1, k = 0) spans
+        // every level and starts them from zero
+        const int base = st * S;
+        const uint32_t bs = smem_u32(sm.b[base]);
+        const uint64_t b0 = TBK == 64 ? sdesc(bs) : sdesc64(bs);
+        for (int s = 1; s <= S; ++s) {
+          const uint32_t d = tmem + (uint32_t)buf * buf_cols + (uint32_t)((s - 1) * kThinBN);
+          const uint32_t as = smem_u32(sm.a[base + s - 1]);
+          const uint64_t a0 = TBK == 64 ? sdesc(as) : sdesc64(as);
+          const uint32_t idesc = idesc_bf16_n(kThinBN * (S + 1 - s));
 #pragma unroll
-            for (int k = 0; k < TBK / 16; ++k) {
-              umma(d, a0 + (uint64_t)(k * 2), b0 + (uint64_t)(k * 2), idesc, first ? 0u : 1u);
-              first = false;
-            }
-          }
+          for (int k = 0; k < TBK / 16; ++k)
+            umma(d, a0 + (uint64_t)(k * 2), b0 + (uint64_t)(k * 2), idesc, (s == 1 && k == 0) ? 0u : 1u);
         }
-        for (int s = 0; s < S; ++s) umma_commit(&sm.empty[sl[s]]);
+        umma_commit(&sm.empty[st]);
         umma_commit(&sm.accfull[buf]);
+        if (++st == stages) {
+          st = 0;
+          phase ^= 1;
+        }
         if (++buf == 2) {
           buf = 0;
           aphase ^= 1;
