@@ -105,6 +105,12 @@ int MoveSet::upload() {
       q.n = m.n;
       q.op = m.op;
       q.scale = m.scale;
+      // moves whose innermost run is contiguous on both sides, of even
+      // length, starting at even offsets with even outer strides go two
+      // elements at a time (16-byte loads and stores)
+      bool pair = q.ext[3] % 2 == 0 && q.sstr[3] == 1 && q.dstr[3] == 1 && m.src % 2 == 0 && m.dst % 2 == 0;
+      for (int d = 0; d < 3 && pair; ++d) pair = q.sstr[d] % 2 == 0 && q.dstr[d] % 2 == 0;
+      q.pad = pair ? 1 : 0;
       q.first = (uint32_t)c;
       const uint64_t nc = (m.n + kMove4Chunk - 1) / kMove4Chunk;
       c += nc;
@@ -232,11 +238,14 @@ __global__ void __launch_bounds__(kMoveThreads) tile_move_kernel(const MoveDesc*
 // decode is fully unrolled (three multiply-high divisions per element), so
 // the kernel issues a few tens of instructions per element and streams at
 // memory speed.  Each thread handles kMove4Chunk / kMoveThreads elements in
-// two batches, addresses first, then every load, then every store.
+// two batches, addresses first, then every load, then every store.  A move
+// marked for pairs (contiguous even inner runs at even offsets) goes two
+// elements per index decode with 16-byte loads and stores.
 __global__ void __launch_bounds__(kMoveThreads) tile_move4_kernel(const MoveDesc4* __restrict__ descs,
                                                                   const uint32_t* __restrict__ chunk_desc,
                                                                   uint32_t nchunks, const double* __restrict__ src,
-                                                                  double* __restrict__ dst, double alpha) {
+                                                                  double* __restrict__ dst, double alpha,
+                                                                  int allow_pairs) {
   constexpr int kPer = 8;
   constexpr int kBatches = kMove4Chunk / (kMoveThreads * kPer);
   for (uint32_t chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
@@ -256,6 +265,50 @@ __global__ void __launch_bounds__(kMoveThreads) tile_move4_kernel(const MoveDesc
     const unsigned long long sb = (unsigned long long)__double_as_longlong(scale);
     const bool unit = op == 0 && (sb & 0x7FFFFFFFFFFFFFFFull) == 0x3FF0000000000000ull;
     const long long flip = (long long)(sb & 0x8000000000000000ull);
+    if (allow_pairs && md->pad == 1) {
+      // pairs (2e, 2e + 1): the chunk's kMove4Chunk elements in one batch of
+      // kPer pairs per thread
+      int64_t so[kPer], to[kPer];
+      bool in[kPer];
+#pragma unroll
+      for (int k = 0; k < kPer; ++k) {
+        const uint32_t e = base + 2u * ((uint32_t)(k * kMoveThreads) + threadIdx.x);
+        in[k] = e < n;
+        const uint32_t r = in[k] ? e : 0;
+        const uint32_t q3 = d3.div(r), c3 = r - q3 * d3.d;
+        const uint32_t q2 = d2.div(q3), c2 = q3 - q2 * d2.d;
+        const uint32_t c0 = d1.div(q2), c1 = q2 - c0 * d1.d;
+        so[k] = (int64_t)c0 * s0 + (int64_t)c1 * s1 + (int64_t)c2 * s2 + (int64_t)c3 * s3;
+        to[k] = (int64_t)c0 * t0 + (int64_t)c1 * t1 + (int64_t)c2 * t2 + (int64_t)c3 * t3;
+      }
+      double2 x[kPer];
+#pragma unroll
+      for (int k = 0; k < kPer; ++k)
+        x[k] = in[k] ? __ldg(reinterpret_cast<const double2*>(s + so[k])) : make_double2(0.0, 0.0);
+      if (unit) {
+#pragma unroll
+        for (int k = 0; k < kPer; ++k)
+          if (in[k])
+            *reinterpret_cast<double2*>(t + to[k]) =
+                make_double2(__longlong_as_double(__double_as_longlong(x[k].x) ^ flip),
+                             __longlong_as_double(__double_as_longlong(x[k].y) ^ flip));
+      } else if (op == 0) {
+#pragma unroll
+        for (int k = 0; k < kPer; ++k)
+          if (in[k]) *reinterpret_cast<double2*>(t + to[k]) = make_double2(__dmul_rn(scale, x[k].x), __dmul_rn(scale, x[k].y));
+      } else {
+        double2 y[kPer];
+#pragma unroll
+        for (int k = 0; k < kPer; ++k)
+          y[k] = in[k] ? *reinterpret_cast<const double2*>(t + to[k]) : make_double2(0.0, 0.0);
+#pragma unroll
+        for (int k = 0; k < kPer; ++k)
+          if (in[k])
+            *reinterpret_cast<double2*>(t + to[k]) =
+                make_double2(__fma_rn(scale, x[k].x, y[k].x), __fma_rn(scale, x[k].y, y[k].y));
+      }
+      continue;
+    }
 #pragma unroll 1
     for (int bt = 0; bt < kBatches; ++bt) {
       int64_t so[kPer], to[kPer];
@@ -298,7 +351,10 @@ int run_moves_scaled(const MoveSet& ms, const double* src, double* dst, double a
   if (ms.ndesc == 0 || ms.nchunks == 0) return GBX_OK;
   if (ms.d_desc4) {
     const int grid = (int)std::min<uint32_t>(ms.nchunks, 152u * 8u);
-    tile_move4_kernel<<<grid, kMoveThreads, 0, st>>>(ms.d_desc4, ms.d_chunk_desc, ms.nchunks, src, dst, alpha);
+    // pairs need 16-byte aligned buffer bases (descriptor offsets are even)
+    const int pairs = (((uintptr_t)src | (uintptr_t)dst) & 15) == 0 ? 1 : 0;
+    tile_move4_kernel<<<grid, kMoveThreads, 0, st>>>(ms.d_desc4, ms.d_chunk_desc, ms.nchunks, src, dst, alpha,
+                                                     pairs);
     GBX_CUDA(cudaGetLastError());
     return GBX_OK;
   }
