@@ -1076,57 +1076,30 @@ __global__ void __launch_bounds__(256) digits_kernel(const SplitRowSet* __restri
 }
 
 // Short rows: one warp handles a whole row (exponent by warp shuffles, then
-// the digits); the row sets here carry first_row in rows.  A warp takes four
-// rows at a time and, for rows of at most 32 elements, issues the four rows'
-// loads before it reduces any of them (the loop is bound by load latency).
+// the digits); the row sets here carry first_row in rows.
 __global__ void __launch_bounds__(256) split_short_rows_kernel(const SplitRowSet* __restrict__ sets, int nsets,
                                                                int64_t total_rows, int S) {
   const int F = 7 + 8 * (S - 1);
   const int lane = threadIdx.x & 31;
-  const int64_t nwarps = (int64_t)gridDim.x * 8;
-  for (int64_t rg0 = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5); rg0 < total_rows; rg0 += 4 * nwarps) {
-    int set[4];
-    long long v[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int64_t rg = rg0 + u * nwarps;
-      set[u] = -1;
-      v[u] = 0;
-      if (rg >= total_rows) continue;
-      int lo = 0, hi = nsets - 1;
-      while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (sets[mid].first_row <= rg) lo = mid; else hi = mid - 1;
-      }
-      set[u] = lo;
-      const SplitRowSet& rs = sets[lo];
-      if (rs.K <= 32 && lane < rs.K) v[u] = __double_as_longlong(__ldg(rs.src + (rg - rs.first_row) * rs.ld + lane));
+  for (int64_t rg = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5); rg < total_rows; rg += (int64_t)gridDim.x * 8) {
+    int lo = 0, hi = nsets - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (sets[mid].first_row <= rg) lo = mid; else hi = mid - 1;
     }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      if (set[u] < 0) continue;  // the same for the whole warp
-      const SplitRowSet& rs = sets[set[u]];
-      const int64_t row = rg0 + u * nwarps - rs.first_row;
-      const double* src = rs.src + row * rs.ld;
-      __nv_bfloat16* dst = rs.dst + row * rs.Kp;
-      uint32_t emax = 0;
-      if (rs.K <= 32) {
-        emax = (uint32_t)((v[u] >> 52) & 0x7FF);
-      } else {
-        for (int64_t k = lane; k < rs.K; k += 32)
-          emax = max(emax, (uint32_t)((__double_as_longlong(__ldg(src + k)) >> 52) & 0x7FF));
-      }
-      for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
-      if (lane == 0) rs.exps[row] = (int)emax;
-      if (rs.K <= 32) {
-        if (lane < rs.K) write_digits(v[u], emax, F, S, dst + lane, rs.slice_stride);
-      } else {
-        for (int64_t k = lane; k < rs.K; k += 32)
-          write_digits(__double_as_longlong(__ldg(src + k)), emax, F, S, dst + k, rs.slice_stride);
-      }
-      for (int64_t k = rs.K + lane; k < rs.Kp; k += 32)
-        for (int s = 0; s < S; ++s) dst[s * rs.slice_stride + k] = __int2bfloat16_rn(0);
-    }
+    const SplitRowSet& rs = sets[lo];
+    const int64_t row = rg - rs.first_row;
+    const double* src = rs.src + row * rs.ld;
+    uint32_t emax = 0;
+    for (int64_t k = lane; k < rs.K; k += 32)
+      emax = max(emax, (uint32_t)((__double_as_longlong(__ldg(src + k)) >> 52) & 0x7FF));
+    for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+    if (lane == 0) rs.exps[row] = (int)emax;
+    __nv_bfloat16* dst = rs.dst + row * rs.Kp;
+    for (int64_t k = lane; k < rs.K; k += 32)
+      write_digits(__double_as_longlong(__ldg(src + k)), emax, F, S, dst + k, rs.slice_stride);
+    for (int64_t k = rs.K + lane; k < rs.Kp; k += 32)
+      for (int s = 0; s < S; ++s) dst[s * rs.slice_stride + k] = __int2bfloat16_rn(0);
   }
 }
 
