@@ -46,7 +46,12 @@ def parse():
                         "iterations of the default workload, inside the 1e-10 Eh bound; 6: ~1e-16)")
     p.add_argument("--autotune", type=int, default=1,
                    help="1: the split job times each contraction's output tile widths when it is built")
+    p.add_argument("--graph", type=int, default=2, choices=[1, 2],
+                   help="1: one CUDA graph of the iteration's kernels; 2: the persistent program (a few "
+                        "persistent launches off a device-side work queue, captured as the graph)")
     p.add_argument("--profile", action="store_true", help="print the per-step breakdown to stderr")
+    p.add_argument("--quick", action="store_true",
+                   help="the GPU line only: no serving run, CPU baseline or oracle comparison")
     p.add_argument("--kernel", choices=["ladder", "thin"], default=None,
                    help="time one split GEMM alone: 'ladder' = one irrep block of the canonical-tile "
                         "<ab||ef> ladder of this workload (3600 x 144 x 7200); 'thin' = one irrep block of t_i^e <ab||ej> "
@@ -75,7 +80,8 @@ def workload(a):
     return {"workload": "ccsd_8irrep_o%d_v%d" % (a.nocc, a.nvir), "method": "CCSD spin-orbital (Jacobi)",
             "nocc": a.nocc, "nvir": a.nvir, "nirrep": a.nirrep, "block_min": a.min_block, "block_max": a.max_block,
             "seed": a.seed, "l2": "inputs larger than L2 (integrals resident, > 3 GB)", "parallelism": "replicas",
-            "split_slices": a.slices, "split_autotune": a.autotune}
+            "split_slices": a.slices, "split_autotune": a.autotune,
+            "iteration": "persistent program" if getattr(a, "graph", 1) == 2 else "kernel graph"}
 
 
 class Clocks:
@@ -467,7 +473,7 @@ def main():
     from dtcf_gb300.replicas import barrier, max_over_ranks, sum_over_ranks
 
     common = dict(nocc=a.nocc, nvir=a.nvir, nirrep=a.nirrep, max_block=a.max_block, min_block=a.min_block,
-                  seed=a.seed, method="ccsd", slices=a.slices)
+                  seed=a.seed, method="ccsd", slices=a.slices, use_graph=a.graph)
     engines = {"auto": ["split", "fp64"], "split": ["split"], "fp64": ["fp64"]}[a.engine]
     stream = torch.cuda.current_stream()
 
@@ -604,7 +610,7 @@ def main():
     # Poisson stream at 20 requests/s (above what the server completes, so
     # the GPU stays saturated), 160 GB admission budget, 4 stream slots, the
     # split engine (5 slices); one process on one GPU
-    if world == 1 and primary == "split":
+    if world == 1 and primary == "split" and not a.quick:
         for R in results.values():
             R["job"].close()
         sa = argparse.Namespace(**vars(a))
@@ -630,7 +636,9 @@ def main():
         line["energy_err_vs_fp64_eh"] = float(np.max(err))
         line["energy_err_per_iter_eh"] = [float(x) for x in err]
         line["energy_iterations_compared"] = int(len(err))
-    if rank == 0:
+    if rank == 0 and a.quick:
+        print(json.dumps(line))
+    elif rank == 0:
         try:
             cb = cpu_arm(a, 5, 1, one_core=True)
             line["cpu_baseline"] = {"value": cb["value"], "unit": "iter/s", "cores": cb["cores"], "kind": cb["kind"],

@@ -64,6 +64,8 @@ SIGNATURES = {
     "gbx_cc_profile": (_i, [_p, _i, _p, _p, _p, _p, _p, _p, _i, _ip, _p]),
     "gbx_cc_time_gemm": (_i, [_p, _i, _i, _p, _p, _p, _p, _p]),
     "gbx_cc_contraction_error": (_i, [_p, _i, _p, _p, _p]),
+    "gbx_cc_program_info": (_i, [_p, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)]),
+    "gbx_cc_program_selftest": (_i, [ctypes.c_longlong, _p]),
     "gbx_dltc_mul_orders": (_i, [_i, _p, _i, _p, _p, _p, _p, _p, _p, _p]),
     "gbx_dltc_task_mul": (_i, [_d, _i, _p, _p, _i, _p, _p, _i, _p, _p, _p, _p, _p, _i, _p]),
     "gbx_dltc_task_sum": (_i, [_d, _i, _p, _p, _i, _p, _p, _p, _p, _p, _p]),

@@ -151,6 +151,12 @@ class Job:
                                              _stream(stream)))
         return rel.value, mx.value
 
+    def program_info(self):
+        """dict(records, levels, launches) of the persistent program (use_graph=2; zeros otherwise)."""
+        v = [ctypes.c_int() for _ in range(3)]
+        check(lib().gbx_cc_program_info(self.handle, *[ctypes.byref(x) for x in v]))
+        return dict(zip(("records", "levels", "launches"), (x.value for x in v)))
+
     def close(self):
         if getattr(self, "handle", None) and self.handle.value:
             lib().gbx_cc_destroy(self.handle)
@@ -158,3 +164,8 @@ class Job:
 
     def __del__(self):
         self.close()
+
+
+def program_selftest(limit_cycles, stream=None):
+    """Status of gbx_cc_program_selftest (GBX_ETIMEOUT when the bounded wait ran out, as it must)."""
+    return lib().gbx_cc_program_selftest(limit_cycles, _stream(stream))

@@ -2,6 +2,7 @@
 // the device, plans every contraction of one CCD / CCSD iteration once, and
 // replays the iteration (optionally as one CUDA graph).
 #include "cc.h"
+#include "program.h"
 #include "split.h"
 
 #include <nvtx3/nvToolsExt.h>
@@ -122,10 +123,17 @@ struct gbx_cc_job {
   int iter_plan_begin = 0;  // plans before this index serve only the initial guess
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  // use_graph 2: the iteration as a persistent program (a few persistent
+  // launches off a device-side work queue), itself captured as the graph
+  ProgramPtr prog;
+
+  bool persistent() const { return cfg.use_graph == 2; }
+  int record_program();
 
   ~gbx_cc_job() {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
+    prog.reset();
     cplans.clear();
     fplans.clear();
     amp.release();
@@ -311,10 +319,7 @@ struct gbx_cc_job {
     CCTensor* C = get(c);
     size_t bytes = sizeof(double) * C->L.nelem;
     dynamic_use.insert(c);
-    steps.push_back([=](cudaStream_t st) {
-      GBX_CUDA(cudaMemsetAsync(C->d, 0, bytes, st));
-      return GBX_OK;
-    });
+    steps.push_back([=](cudaStream_t st) { return zero_async(C->d, bytes, st); });
     info.push_back({std::string("zero ") + c, 2, 0.0, (double)bytes});
     launches += 1;
     return GBX_OK;
@@ -556,7 +561,9 @@ int gbx_cc_job::footprint(double* resident, double* peak) const {
     size_t k = 0, w = 0, sc = 0;
     GBX_TRY(p->sizes(&k, &w, &sc));
     keep += (double)k + p->f64_workspace_estimate();
-    ws = std::max(ws, (double)w);
+    // a persistent program runs contractions side by side: each plan keeps
+    // its own region of the arena
+    ws = persistent() ? ws + up256d((double)w) : std::max(ws, (double)w);
     scratch = std::max(scratch, (double)sc);
   }
   for (auto& p : fplans) keep += up256d((double)(p->items.size() * sizeof(FsItem))) + up256d((double)(p->terms.size() * sizeof(FsTerm)));
@@ -622,10 +629,16 @@ int gbx_cc_job::materialize(cudaStream_t st) {
   // scratch is released
   arena_bytes = 0;
   size_t scratch_bytes = 0;
-  for (auto& p : cplans) {
+  std::vector<size_t> arena_off(cplans.size(), 0);
+  for (size_t i = 0; i < cplans.size(); ++i) {
     size_t k = 0, w = 0, sc = 0;
-    GBX_TRY(p->sizes(&k, &w, &sc));
-    arena_bytes = std::max(arena_bytes, w);
+    GBX_TRY(cplans[i]->sizes(&k, &w, &sc));
+    if (persistent()) {  // a region per plan (they run side by side)
+      arena_off[i] = arena_bytes;
+      arena_bytes += (w + 255) / 256 * 256;
+    } else {
+      arena_bytes = std::max(arena_bytes, w);
+    }
     scratch_bytes = std::max(scratch_bytes, sc);
   }
   if (arena_bytes) {
@@ -638,7 +651,7 @@ int gbx_cc_job::materialize(cudaStream_t st) {
   if (!amp_items.empty()) GBX_TRY(amp.upload(amp_tiles, amp_items));
   for (size_t i = 0; i < cplans.size(); ++i) {
     ContractionPlan* p = cplans[i].get();
-    int rc = p->build(d_arena, d_scratch);
+    int rc = p->build(d_arena ? d_arena + arena_off[i] : nullptr, d_scratch);
     if (rc == GBX_OK && (p->a_static || p->b_static))
       rc = p->prepare_static(plan_operands[i].first->d, plan_operands[i].second->d, st);
     if (rc == GBX_OK && cfg.autotune) rc = p->tune_split(st);
@@ -743,16 +756,43 @@ int gbx_cc_create(const gbx_cc_config* cfg, void* stream, gbx_cc_job** out) {
   return GBX_OK;
 }
 
+// Records the iteration's steps into the persistent program: the job's
+// tensors are the buffers whose conflicts order the records of different
+// steps (every other buffer a step touches belongs to that step's plan).
+int gbx_cc_job::record_program() {
+  std::vector<ProgBuffer> bufs;
+  for (auto& kv : T)
+    if (kv.second->d) bufs.push_back({kv.second->d, sizeof(double) * (size_t)std::max<int64_t>(1, kv.second->L.nelem)});
+  ProgRecorder* rec = nullptr;
+  GBX_TRY(prog_begin(bufs, &rec));
+  int rc = GBX_OK;
+  for (size_t i = 0; i < steps.size() && rc == GBX_OK; ++i) {
+    prog_step(rec, (int)i);
+    rc = steps[i](prog_stream(rec));
+  }
+  ProgramPtr p;
+  const int frc = prog_finish(rec, p);
+  if (rc != GBX_OK) return rc;
+  GBX_TRY(frc);
+  prog = std::move(p);
+  return GBX_OK;
+}
+
 int gbx_cc_capture(gbx_cc_job* job) {
   if (!job) return fail(GBX_EINVAL, "null job");
   if (!job->cfg.use_graph || job->exec) return GBX_OK;
+  if (job->persistent() && !job->prog) GBX_TRY(job->record_program());
   cudaStream_t cap;
   GBX_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
   GBX_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
   int rc = GBX_OK;
-  for (auto& s : job->steps) {
-    rc = s(cap);
-    if (rc != GBX_OK) break;
+  if (job->prog) {
+    rc = prog_run(*job->prog, cap);
+  } else {
+    for (auto& s : job->steps) {
+      rc = s(cap);
+      if (rc != GBX_OK) break;
+    }
   }
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamEndCapture(cap, &g);
@@ -788,6 +828,29 @@ int gbx_cc_check(gbx_cc_job* job) {
     int err = split_plan_error(p->split);
     if (err != 0) return fail(GBX_ETIMEOUT, "split GEMM: a bounded device wait ran out (stage %d)", err);
   }
+  if (job->prog) {
+    const int err = prog_error(*job->prog);
+    if (err != 0) return fail(GBX_ETIMEOUT, "persistent iteration: a bounded device wait ran out (code %d)", err);
+  }
+  return GBX_OK;
+}
+
+int gbx_cc_program_info(gbx_cc_job* job, int* records, int* levels, int* launches) {
+  if (!job) return fail(GBX_EINVAL, "null job");
+  if (job->persistent() && !job->exec) GBX_TRY(gbx_cc_capture(job));
+  ProgStats s{};
+  if (job->prog) prog_stats(*job->prog, &s);
+  if (records) *records = s.records;
+  if (levels) *levels = s.levels;
+  if (launches) *launches = s.launches;
+  return GBX_OK;
+}
+
+int gbx_cc_program_selftest(long long limit_cycles, void* stream) {
+  if (limit_cycles <= 0) return fail(GBX_EINVAL, "bad wait limit");
+  int err = 0;
+  GBX_TRY(prog_wait_selftest(limit_cycles, (cudaStream_t)stream, &err));
+  if (err != 0) return fail(GBX_ETIMEOUT, "persistent iteration: a bounded device wait ran out (code %d)", err);
   return GBX_OK;
 }
 

@@ -7,13 +7,15 @@
 // extents and the global orbital index of the first orbital of each block.
 #include <algorithm>
 
+#include "bodies.cuh"
 #include "cc.h"
+#include "program.h"
 
 namespace gbx {
 
 namespace {
-constexpr int kThreads = 256;
-constexpr int kChunk = 2048;
+constexpr int kThreads = dev::kCcThreads;
+constexpr int kChunk = dev::kCcChunk;
 
 __device__ __forceinline__ uint64_t mix64(uint64_t z) {
   z ^= z >> 30;
@@ -88,8 +90,7 @@ __global__ void __launch_bounds__(kThreads) cc_tile_kernel(const CCTile* __restr
 
 __global__ void __launch_bounds__(kThreads) mul_kernel(const double* __restrict__ a, const double* __restrict__ b,
                                                        double* __restrict__ out, int64_t n) {
-  for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kThreads)
-    out[i] = __dmul_rn(a[i], b[i]);
+  dev::mul_body<false>(a, b, out, n, blockIdx.x, gridDim.x);
 }
 
 // Per-CTA partial sums of x*y over n elements, in a fixed order.
@@ -97,17 +98,7 @@ __global__ void __launch_bounds__(kThreads) dot_partial_kernel(const double* __r
                                                                const double* __restrict__ y, int64_t n,
                                                                double* __restrict__ partial) {
   __shared__ double red[kThreads];
-  double s = 0.0;
-  int64_t per = (n + gridDim.x - 1) / gridDim.x;
-  int64_t lo = per * blockIdx.x, hi = min(n, lo + per);
-  for (int64_t i = lo + threadIdx.x; i < hi; i += kThreads) s = fma(x[i], y[i], s);
-  red[threadIdx.x] = s;
-  __syncthreads();
-  for (int w = kThreads / 2; w > 0; w >>= 1) {
-    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+  dev::dot_partial_body<false>(x, y, n, partial, blockIdx.x, gridDim.x, red);
 }
 
 __global__ void dot_final_kernel(const double* __restrict__ partial, int np, double scale, double* __restrict__ out) {
@@ -118,22 +109,25 @@ __global__ void dot_final_kernel(const double* __restrict__ partial, int np, dou
   }
 }
 
-__global__ void energy_final_kernel(const double* __restrict__ partial, int np, double scale, double* __restrict__ hist,
-                                    int* __restrict__ count, int cap) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    double s = 0.0;
-    for (int i = 0; i < np; ++i) s += partial[i];
-    int k = *count;
-    if (k < cap) hist[k] = s * scale;
-    *count = k + 1;
-  }
+__global__ void __launch_bounds__(kThreads) energy_final_kernel(const double* __restrict__ partial, int np,
+                                                                double scale, double* __restrict__ hist,
+                                                                int* __restrict__ count, int cap) {
+  __shared__ double stage[kThreads];
+  dev::energy_final_body<false>(partial, np, scale, hist, count, cap, blockIdx.x, stage);
 }
 
 int run_energy(const double* V, const double* tau, int64_t n, double* partial, int npartial, double* hist, int* count,
                int cap, cudaStream_t st) {
+  if (ProgRecorder* rec = prog_recording()) {
+    ProgArgs a;
+    a.dot = {V, tau, partial, n};
+    GBX_TRY(prog_mem(rec, PK_DOTPART, (uint32_t)npartial, a, {{V, false}, {tau, false}, {partial, true}}));
+    a.efin = {partial, hist, count, 0.25, npartial, cap};
+    return prog_mem(rec, PK_ENERGYFIN, 1, a, {{partial, false}, {hist, true}, {count, true}});
+  }
   dot_partial_kernel<<<npartial, kThreads, 0, st>>>(V, tau, n, partial);
   GBX_CUDA(cudaGetLastError());
-  energy_final_kernel<<<1, 32, 0, st>>>(partial, npartial, 0.25, hist, count, cap);
+  energy_final_kernel<<<1, kThreads, 0, st>>>(partial, npartial, 0.25, hist, count, cap);
   GBX_CUDA(cudaGetLastError());
   return GBX_OK;
 }
@@ -171,52 +165,7 @@ __global__ void __launch_bounds__(kThreads) cc_amp_kernel(const CCAmpTile* __res
                                                          const double* __restrict__ t1,
                                                          const double* __restrict__ t2, double* __restrict__ tau,
                                                          double* __restrict__ taut, double* __restrict__ Q) {
-  constexpr int kPer = kChunk / kThreads;
-  for (int i = blockIdx.x; i < nitems; i += gridDim.x) {
-    const CCAmpItem it = items[i];
-    const CCAmpTile& tl = tiles[it.tile];
-    const uint32_t ej = tl.fj.d, ea = tl.fa.d, eb = tl.fb.d;
-    const int64_t o_ia = tl.t1[0], o_jb = tl.t1[1], o_ib = tl.t1[2], o_ja = tl.t1[3];
-    const bool h1 = o_ia >= 0 && o_jb >= 0, h2 = o_ib >= 0 && o_ja >= 0;
-    double x[kPer], p1[kPer], p2[kPer];
-#pragma unroll
-    for (int k = 0; k < kPer; ++k) {
-      const uint32_t e = min((uint32_t)(threadIdx.x + k * kThreads), it.n - 1);
-      const uint32_t f = it.f0 + e;
-      const uint32_t r1 = tl.fb.div(f), b = f - r1 * eb;
-      const uint32_t r2 = tl.fa.div(r1), a = r1 - r2 * ea;
-      const uint32_t ii = tl.fj.div(r2), j = r2 - ii * ej;
-      x[k] = __ldg(t2 + tl.off + f);
-      p1[k] = h1 ? __dmul_rn(__ldg(t1 + o_ia + (int64_t)ii * ea + a), __ldg(t1 + o_jb + (int64_t)j * eb + b)) : 0.0;
-      p2[k] = h2 ? __dmul_rn(__ldg(t1 + o_ib + (int64_t)ii * eb + b), __ldg(t1 + o_ja + (int64_t)j * ea + a)) : 0.0;
-    }
-    // seven FP64 instructions per element (the FP64 pipe, not HBM, bounds
-    // element-wise FP64 work on this part): the products p1, p2; tau as
-    // (t2 + p1) - p2; taut and Q with fused multiply-adds by 1/2 -- each the
-    // separately rounded product and sum, 0.5 x being exact
-#pragma unroll
-    for (int k = 0; k < kPer; ++k) {
-      const uint32_t e = threadIdx.x + k * kThreads;
-      if (e >= it.n) continue;
-      const int64_t at = tl.off + it.f0 + e;
-      // 0 + t2 (turns -0 into +0) on the bits
-      const unsigned long long xb = (unsigned long long)__double_as_longlong(x[k]);
-      const double x0 = __longlong_as_double((long long)(xb == 0x8000000000000000ull ? 0ull : xb));
-      double a1 = x0, a2 = x0;
-      double q = __fma_rn(0.5, x[k], h1 ? p1[k] : 0.0);
-      if (h1) {
-        a1 = __dadd_rn(a1, p1[k]);
-        a2 = __fma_rn(0.5, p1[k], a2);
-      }
-      if (h2) {
-        a1 = __dsub_rn(a1, p2[k]);
-        a2 = __fma_rn(-0.5, p2[k], a2);
-      }
-      tau[at] = a1;
-      taut[at] = a2;
-      Q[at] = q;
-    }
-  }
+  dev::cc_amp_body<false>(tiles, items, nitems, t1, t2, tau, taut, Q, blockIdx.x, gridDim.x);
 }
 
 int CCAmpSet::upload(const std::vector<CCAmpTile>& tiles, const std::vector<CCAmpItem>& items) {
@@ -243,6 +192,12 @@ int run_cc_amp(const CCAmpSet& s, const double* t1, const double* t2, double* ta
                cudaStream_t st) {
   if (s.nitems == 0) return GBX_OK;
   const int grid = std::min(s.nitems, 152 * 8);
+  if (ProgRecorder* rec = prog_recording()) {
+    ProgArgs a;
+    a.amp = {s.d_tiles, s.d_items, t1, t2, tau, taut, Q, s.nitems};
+    return prog_mem(rec, PK_AMP, (uint32_t)grid, a,
+                    {{t1, false}, {t2, false}, {tau, true}, {taut, true}, {Q, true}});
+  }
   cc_amp_kernel<<<grid, kThreads, 0, st>>>(s.d_tiles, s.d_items, s.nitems, t1, t2, tau, taut, Q);
   GBX_CUDA(cudaGetLastError());
   return GBX_OK;
@@ -251,6 +206,11 @@ int run_cc_amp(const CCAmpSet& s, const double* t1, const double* t2, double* ta
 int run_mul(const double* a, const double* b, double* out, int64_t n, cudaStream_t st) {
   if (n <= 0) return GBX_OK;
   const int grid = (int)std::min<int64_t>((n + kThreads - 1) / kThreads, 152 * 16);
+  if (ProgRecorder* rec = prog_recording()) {
+    ProgArgs pa;
+    pa.mul = {a, b, out, n};
+    return prog_mem(rec, PK_MUL, (uint32_t)grid, pa, {{a, false}, {b, false}, {out, true}});
+  }
   mul_kernel<<<grid, kThreads, 0, st>>>(a, b, out, n);
   GBX_CUDA(cudaGetLastError());
   return GBX_OK;

@@ -222,6 +222,8 @@ struct F64Gemm {
   int build(const std::vector<GemmProblem>& probs, bool async = false, cudaStream_t st = nullptr,
             const std::vector<int>* variants = nullptr);
   int run(cudaStream_t st) const;
+  // One shape's launch (its work-queue ticket reset first).
+  static int run_sub(const Sub& sb, cudaStream_t st);
   // One launch per problem (static schedule), then the split-K reduction:
   // the per-launch baseline against the single persistent launch of run().
   int run_each(cudaStream_t st) const;

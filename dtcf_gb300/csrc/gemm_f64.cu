@@ -17,7 +17,9 @@
 #include <cstring>
 #include <mutex>
 
+#include "bodies.cuh"
 #include "common.h"
+#include "program.h"
 
 namespace gbx {
 
@@ -27,15 +29,15 @@ constexpr int kThreads = 128;
 constexpr int kPad = 1;               // pad rows to spread shared-memory banks
 constexpr int kFillTiles = 152 * 3;   // work items that keep every SM busy
 constexpr int kMinChunk = 256;        // smallest K range of a split
-constexpr int kRedThreads = 256;
-constexpr int kRedChunk = 2048;
+constexpr int kRedThreads = dev::kRedThreads;
+constexpr int kRedChunk = dev::kRedChunk;
 constexpr int kThinN = 32, kThinK = 64, kThinMinWide = 16384;
-constexpr int kSmallK = 8;
-constexpr int kSmallKElems = 2048;  // output elements per CTA
-constexpr int kSmallOutDim = 16;    // small outputs: at most 16 x 16 ...
+constexpr int kSmallK = dev::kSmallK;
+constexpr int kSmallKElems = dev::kSmallKElems;  // output elements per CTA
+constexpr int kSmallOutDim = dev::kSmallOutDim;  // small outputs: at most 16 x 16 ...
 constexpr int kSmallOutMinK = 4096;  // ... with at least this K
 constexpr int kSmallOutChunk = 4096;  // K per work item
-constexpr int kGemvDim = 2;           // matrix-vector problems: one side at most this ...
+constexpr int kGemvDim = dev::kGemvDim;  // matrix-vector problems: one side at most this ...
 constexpr int kGemvMinK = 64;         // ... with K above this
 constexpr int kGemvItems = 152 * 4;   // work items that keep every SM busy
 constexpr int kGemvMinChunk = 1024;   // smallest K range of a split
@@ -126,67 +128,10 @@ __global__ void __launch_bounds__(256) thin_gemm_f64_kernel(const GemmProblem* _
   }
 }
 
-// Matrix-vector shapes (variant 8): one warp per output of the wide side --
-// column j of C when A is the thin operand (m <= 2), row i when B is (n <=
-// 2).  The lanes stride K, so the wide operand's row is read once and
-// coalesced when its K stride is 1; each lane keeps one partial sum per thin
-// row, and the warp adds them in a fixed butterfly order (deterministic).
-// Eight warps per CTA: a work item is eight consecutive wide-side outputs
-// over one K range; with several ranges (few outputs, long K) each writes
-// its raw sums to a partial slab that the split-K reduction adds in order.
+// Matrix-vector shapes (variant 8): dev::gemv_body.
 __global__ void __launch_bounds__(256) gemv_f64_kernel(const GemmProblem* __restrict__ probs, int nprob,
                                                        const int* __restrict__ block_first, int total_blocks) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int blk = blockIdx.x; blk < total_blocks; blk += gridDim.x) {
-    int lo = 0, hi = nprob - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (block_first[mid] <= blk) lo = mid; else hi = mid - 1;
-    }
-    const GemmProblem& p = probs[lo];
-    const bool a_thin = p.m <= kGemvDim && p.m <= p.n;
-    const int tn = a_thin ? p.m : p.n;
-    const int64_t wide = a_thin ? p.n : p.m;
-    const int64_t groups = (wide + 7) / 8;
-    const int64_t local = blk - block_first[lo];
-    const int kc = (int)(local / groups);
-    const int64_t w = (local - kc * groups) * 8 + warp;
-    if (w >= wide) continue;
-    const int64_t k0 = (int64_t)kc * p.kchunk, k1 = min((int64_t)p.k, k0 + p.kchunk);
-    const double* W = a_thin ? p.B + w * p.b_rs : p.A + w * p.a_rs;
-    const int64_t wcs = a_thin ? p.b_cs : p.a_cs;
-    const double* T = a_thin ? p.A : p.B;
-    const int64_t trs = a_thin ? p.a_rs : p.b_rs, tcs = a_thin ? p.a_cs : p.b_cs;
-    double acc[kGemvDim];
-#pragma unroll
-    for (int j = 0; j < kGemvDim; ++j) acc[j] = 0.0;
-    for (int64_t k = k0 + lane; k < k1; k += 32) {
-      const double x = __ldg(W + k * wcs);
-#pragma unroll
-      for (int j = 0; j < kGemvDim; ++j)
-        if (j < tn) acc[j] = fma(x, __ldg(T + j * trs + k * tcs), acc[j]);
-    }
-#pragma unroll
-    for (int j = 0; j < kGemvDim; ++j) {
-      if (j >= tn) break;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], o);
-    }
-    if (lane == 0) {
-#pragma unroll
-      for (int j = 0; j < kGemvDim; ++j) {
-        if (j >= tn) break;
-        const int64_t row = a_thin ? j : w, col = a_thin ? w : j;
-        if (p.ksplit > 1) {
-          p.partial[(int64_t)kc * p.m * p.n + row * p.n + col] = acc[j];
-        } else {
-          double* c = p.C + row * p.c_rs + col;
-          const double v = __dmul_rn(p.alpha, acc[j]);
-          *c = p.accumulate ? __dadd_rn(*c, v) : v;
-        }
-      }
-    }
-  }
+  dev::gemv_body<false>(probs, nprob, block_first, total_blocks, blockIdx.x, gridDim.x);
 }
 
 __device__ __forceinline__ void dmma884(double (&c)[2], double a, double b) {
@@ -319,88 +264,17 @@ __global__ void __launch_bounds__(kThreads) grouped_gemm_f64_kernel(const GemmPr
   }
 }
 
-// K <= 8: every output element is its own k-ordered FMA chain (outer
-// products and other tiny-K contractions), written coalesced along columns.
+// K <= 8 (dev::small_k_body).
 __global__ void __launch_bounds__(256) small_k_gemm_f64_kernel(const GemmProblem* __restrict__ probs, int nprob,
                                                                const int* __restrict__ block_first, int total_blocks) {
-  for (int blk = blockIdx.x; blk < total_blocks; blk += gridDim.x) {
-    int lo = 0, hi = nprob - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (block_first[mid] <= blk) lo = mid; else hi = mid - 1;
-    }
-    const GemmProblem& p = probs[lo];
-    const int64_t mn = (int64_t)p.m * p.n;
-    const int64_t e0 = (int64_t)(blk - block_first[lo]) * kSmallKElems;
-    for (int r = 0; r < kSmallKElems / 256; ++r) {
-      const int64_t e = e0 + r * 256 + threadIdx.x;
-      if (e >= mn) break;
-      const int64_t i = e / p.n, j = e - i * p.n;
-      double acc = 0.0;
-      for (int k = 0; k < p.k; ++k)
-        acc = fma(__ldg(p.A + i * p.a_rs + (int64_t)k * p.a_cs), __ldg(p.B + j * p.b_rs + (int64_t)k * p.b_cs), acc);
-      double* c = p.C + i * p.c_rs + j;
-      const double v = __dmul_rn(p.alpha, acc);
-      *c = p.accumulate ? __dadd_rn(*c, v) : v;
-    }
-  }
+  dev::small_k_body<false>(probs, nprob, block_first, total_blocks, blockIdx.x, gridDim.x);
 }
 
-// Small output, long K (variant 7): work item = one K chunk of one problem;
-// the CTA stages 64-wide K slices of all m rows of A and n rows of B in
-// shared memory, thread t accumulates output t % (m n) over every
-// (256 / (m n))-th k of the slice, and the lanes of an output are summed in
-// a fixed order into the chunk's partial (or C when there is one chunk).
+// Small output, long K (variant 7, dev::small_out_body).
 __global__ void __launch_bounds__(256) small_out_gemm_f64_kernel(const GemmProblem* __restrict__ probs, int nprob,
                                                                  const int* __restrict__ item_first, int total) {
-  __shared__ double As[kSmallOutDim][65];
-  __shared__ double Bs[kSmallOutDim][65];
-  __shared__ double red[256];
-  const int tid = threadIdx.x;
-  for (int item = blockIdx.x; item < total; item += gridDim.x) {
-    int lo = 0, hi = nprob - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (item_first[mid] <= item) lo = mid; else hi = mid - 1;
-    }
-    const GemmProblem& p = probs[lo];
-    const int c = item - item_first[lo];
-    const int P = p.m * p.n, lanes = 256 / P;
-    const int out = tid % P, lane = tid / P;
-    const bool active = lane < lanes;
-    const int i = out / p.n, j = out - i * p.n;
-    const int k0 = c * p.kchunk, k1 = min(p.k, k0 + p.kchunk);
-    double acc = 0.0;
-    for (int kk = k0; kk < k1; kk += 64) {
-      const int kc = min(64, k1 - kk);
-      __syncthreads();
-      for (int e = tid; e < p.m * 64; e += 256) {
-        const int r = e >> 6, q = e & 63;
-        As[r][q] = q < kc ? __ldg(p.A + (int64_t)r * p.a_rs + (int64_t)(kk + q) * p.a_cs) : 0.0;
-      }
-      for (int e = tid; e < p.n * 64; e += 256) {
-        const int r = e >> 6, q = e & 63;
-        Bs[r][q] = q < kc ? __ldg(p.B + (int64_t)r * p.b_rs + (int64_t)(kk + q) * p.b_cs) : 0.0;
-      }
-      __syncthreads();
-      if (active)
-        for (int q = lane; q < kc; q += lanes) acc = fma(As[i][q], Bs[j][q], acc);
-    }
-    __syncthreads();
-    red[tid] = active ? acc : 0.0;
-    __syncthreads();
-    if (tid < P) {
-      double sum = 0.0;
-      for (int l = 0; l < lanes; ++l) sum = __dadd_rn(sum, red[l * P + tid]);
-      if (p.ksplit > 1) {
-        p.partial[(int64_t)c * P + tid] = sum;
-      } else {
-        double* cp = p.C + (int64_t)i * p.c_rs + j;
-        const double v = __dmul_rn(p.alpha, sum);
-        *cp = p.accumulate ? __dadd_rn(*cp, v) : v;
-      }
-    }
-  }
+  __shared__ dev::SmallOutSmem sm;
+  dev::small_out_body<false>(probs, nprob, item_first, total, blockIdx.x, gridDim.x, sm);
 }
 
 // Fixed-order reduction of split-K partials into C.
@@ -408,26 +282,7 @@ __global__ void __launch_bounds__(kRedThreads) splitk_reduce_kernel(const GemmPr
                                                                     const int* __restrict__ red_prob,
                                                                     const uint32_t* __restrict__ red_first, int nred,
                                                                     uint32_t nchunks) {
-  for (uint32_t chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
-    int lo = 0, hi = nred - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (red_first[mid] <= chunk) lo = mid; else hi = mid - 1;
-    }
-    const GemmProblem& p = probs[red_prob[lo]];
-    const int64_t mn = (int64_t)p.m * p.n;
-    const int64_t base = (int64_t)(chunk - red_first[lo]) * kRedChunk;
-    for (int k = 0; k < kRedChunk / kRedThreads; ++k) {
-      int64_t e = base + k * kRedThreads + threadIdx.x;
-      if (e >= mn) break;
-      double s = 0.0;
-      for (int c = 0; c < p.ksplit; ++c) s = __dadd_rn(s, p.partial[(int64_t)c * mn + e]);
-      int64_t row = e / p.n, col = e - row * p.n;
-      double* cp = p.C + row * p.c_rs + col;
-      double v = __dmul_rn(p.alpha, s);
-      *cp = p.accumulate ? __dadd_rn(*cp, v) : v;
-    }
-  }
+  dev::splitk_reduce_body<false>(probs, red_prob, red_first, nred, nchunks, blockIdx.x, gridDim.x);
 }
 
 void F64Gemm::release() {
@@ -658,54 +513,79 @@ int F64Gemm::build(const std::vector<GemmProblem>& in, bool async, cudaStream_t 
 
 int F64Gemm::run(cudaStream_t st) const {
   if (nprob == 0) return GBX_OK;
-  for (const Sub& sb : subs) {
-    GBX_CUDA(cudaMemsetAsync(sb.d_ticket, 0, sizeof(int), st));
-    int grid = std::min(sb.total_tiles, 152 * 4);
-    switch (sb.variant) {
-      case 0:
-        grouped_gemm_f64_kernel<64, 64><<<grid, kThreads, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first, sb.total_tiles,
-                                                                   sb.d_ticket);
-        break;
-      case 1:
-        grouped_gemm_f64_kernel<64, 16><<<grid, kThreads, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first, sb.total_tiles,
-                                                                   sb.d_ticket);
-        break;
-      case 2:
-        grouped_gemm_f64_kernel<16, 64><<<grid, kThreads, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first, sb.total_tiles,
-                                                                   sb.d_ticket);
-        break;
-      case 3:
-        grouped_gemm_f64_kernel<16, 16><<<grid, kThreads, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first, sb.total_tiles,
-                                                                   sb.d_ticket);
-        break;
-      case 4:
-        thin_gemm_f64_kernel<true><<<std::min(sb.total_tiles, 152 * 8), 256, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first,
-                                                                                      sb.total_tiles);
-        break;
-      case 6:
-        small_k_gemm_f64_kernel<<<std::min(sb.total_tiles, 152 * 8), 256, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first,
-                                                                                   sb.total_tiles);
-        break;
-      case 7:
-        small_out_gemm_f64_kernel<<<std::min(sb.total_tiles, 152 * 8), 256, 0, st>>>(sb.d_probs, sb.nprob,
-                                                                                     sb.d_first, sb.total_tiles);
-        break;
-      case 8:
-        gemv_f64_kernel<<<std::min(sb.total_tiles, 152 * 8), 256, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first,
-                                                                           sb.total_tiles);
-        break;
-      default:
-        thin_gemm_f64_kernel<false><<<std::min(sb.total_tiles, 152 * 8), 256, 0, st>>>(sb.d_probs, sb.nprob,
-                                                                                       sb.d_first, sb.total_tiles);
-        break;
+  if (ProgRecorder* rec = prog_recording()) {
+    // the CUDA-core shapes become records of the persistent program (static
+    // schedule over their work items); the DMMA tile shapes and the thin
+    // kernels keep their own launches
+    for (const Sub& sb : subs) {
+      const int kind = sb.variant == 6 ? PK_SMALLK : sb.variant == 7 ? PK_SMALLOUT : sb.variant == 8 ? PK_GEMV : -1;
+      if (kind >= 0) {
+        ProgArgs a;
+        a.gemm = {sb.d_probs, sb.d_first, sb.nprob, sb.total_tiles};
+        GBX_TRY(prog_mem(rec, kind, (uint32_t)std::min(sb.total_tiles, 152 * 8), a, {}));
+        continue;
+      }
+      const Sub* psb = &sb;
+      GBX_TRY(prog_ext(rec, [psb](cudaStream_t s2) { return run_sub(*psb, s2); }, {}));
     }
-    GBX_CUDA(cudaGetLastError());
+    if (nred) {
+      ProgArgs a;
+      a.kred = {d_all, d_red_prob, d_red_first, nred, red_chunks};
+      GBX_TRY(prog_mem(rec, PK_SPLITKRED, std::min<uint32_t>(red_chunks, 152u * 8u), a, {}));
+    }
+    return GBX_OK;
   }
+  for (const Sub& sb : subs) GBX_TRY(run_sub(sb, st));
   if (nred) {
     int rg = (int)std::min<uint32_t>(red_chunks, 152u * 8u);
     splitk_reduce_kernel<<<rg, kRedThreads, 0, st>>>(d_all, d_red_prob, d_red_first, nred, red_chunks);
     GBX_CUDA(cudaGetLastError());
   }
+  return GBX_OK;
+}
+
+int F64Gemm::run_sub(const Sub& sb, cudaStream_t st) {
+  GBX_CUDA(cudaMemsetAsync(sb.d_ticket, 0, sizeof(int), st));
+  int grid = std::min(sb.total_tiles, 152 * 4);
+  switch (sb.variant) {
+    case 0:
+      grouped_gemm_f64_kernel<64, 64><<<grid, kThreads, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first, sb.total_tiles,
+                                                                 sb.d_ticket);
+      break;
+    case 1:
+      grouped_gemm_f64_kernel<64, 16><<<grid, kThreads, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first, sb.total_tiles,
+                                                                 sb.d_ticket);
+      break;
+    case 2:
+      grouped_gemm_f64_kernel<16, 64><<<grid, kThreads, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first, sb.total_tiles,
+                                                                 sb.d_ticket);
+      break;
+    case 3:
+      grouped_gemm_f64_kernel<16, 16><<<grid, kThreads, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first, sb.total_tiles,
+                                                                 sb.d_ticket);
+      break;
+    case 4:
+      thin_gemm_f64_kernel<true><<<std::min(sb.total_tiles, 152 * 8), 256, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first,
+                                                                                    sb.total_tiles);
+      break;
+    case 6:
+      small_k_gemm_f64_kernel<<<std::min(sb.total_tiles, 152 * 8), 256, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first,
+                                                                                 sb.total_tiles);
+      break;
+    case 7:
+      small_out_gemm_f64_kernel<<<std::min(sb.total_tiles, 152 * 8), 256, 0, st>>>(sb.d_probs, sb.nprob,
+                                                                                   sb.d_first, sb.total_tiles);
+      break;
+    case 8:
+      gemv_f64_kernel<<<std::min(sb.total_tiles, 152 * 8), 256, 0, st>>>(sb.d_probs, sb.nprob, sb.d_first,
+                                                                         sb.total_tiles);
+      break;
+    default:
+      thin_gemm_f64_kernel<false><<<std::min(sb.total_tiles, 152 * 8), 256, 0, st>>>(sb.d_probs, sb.nprob,
+                                                                                     sb.d_first, sb.total_tiles);
+      break;
+  }
+  GBX_CUDA(cudaGetLastError());
   return GBX_OK;
 }
 

@@ -38,7 +38,10 @@
 #include <cstring>
 #include <memory>
 
+#include "bodies.cuh"
+#include "program.h"
 #include "split.h"
+#include "split_dev.h"
 
 namespace gbx {
 
@@ -52,26 +55,8 @@ constexpr int kFoldChunks = 127;   // int32 drain sums fold into FP64 before ove
 constexpr long long kWaitCycles = 2000000000ll;  // ~1 s at 2 GHz
 constexpr int kSplitFill = 152 * 2;  // work items that keep every SM busy
 
-struct SplitRowSet {   // one operand of one problem for the split kernel
-  const double* src;
-  int64_t rows, K;     // source rows (M or N) and row length
-  __nv_bfloat16* dst;  // slice 0, row 0
-  int64_t slice_stride, Kp;
-  int* exps;
-  int64_t first_row;   // first (row, K chunk) work item of this set
-  int64_t ld;          // source row stride (elements)
-};
-
-struct DevProblem {
-  int M, N, K, nkb;
-  int tiles_m, tiles_n;
-  int ksplit, kb_per_split;  // K split into ranges of kb_per_split k-blocks
-  const int* eA;
-  const int* eB;
-  double* C;        // ksplit == 1: output
-  double* partial;  // ksplit > 1: ksplit x M x N raw contributions
-  int64_t ldc;
-};
+using dev::kShortRow;
+using dev::kSplitChunk;
 
 struct GemmParams {
   const DevProblem* probs;
@@ -940,167 +925,24 @@ __global__ void __launch_bounds__(256) split_reduce_kernel(const DevProblem* __r
                                                            const int* __restrict__ red_prob,
                                                            const int64_t* __restrict__ red_first, int nred,
                                                            int64_t total) {
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    int lo = 0, hi = nred - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (red_first[mid] <= e) lo = mid; else hi = mid - 1;
-    }
-    const DevProblem& p = probs[red_prob[lo]];
-    const int64_t i = e - red_first[lo];
-    const int64_t mn = (int64_t)p.M * p.N;
-    double acc = 0.0;
-    for (int c = 0; c < p.ksplit; ++c) acc += p.partial[c * mn + i];
-    const int64_t row = i / p.N, col = i - row * p.N;
-    p.C[row * p.ldc + col] = acc;
-  }
+  dev::split_reduce_body<false>(probs, red_prob, red_first, nred, total, blockIdx.x, gridDim.x);
 }
 
-// Splitting runs in two passes over (row, K chunk) work items so that rows
-// with very long K spread over the whole GPU.  Pass 1 takes the largest biased
-// exponent of each row chunk and folds it into the row with atomicMax (exact,
-// order independent); pass 2 writes the digits.
-constexpr int kSplitChunk = 2048;
-constexpr int64_t kShortRow = 1024;  // rows up to this length: one warp per row, both passes fused
-
-__device__ __forceinline__ void locate_chunk(const SplitRowSet* __restrict__ sets, int nsets, int64_t chunk,
-                                             int& set, int64_t& row, int64_t& k0) {
-  int lo = 0, hi = nsets - 1;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (sets[mid].first_row <= chunk) lo = mid; else hi = mid - 1;
-  }
-  set = lo;
-  const SplitRowSet& rs = sets[lo];
-  const int64_t per_row = (rs.K + kSplitChunk - 1) / kSplitChunk;
-  const int64_t local = chunk - rs.first_row;
-  row = local / per_row;
-  k0 = (local - row * per_row) * kSplitChunk;
-}
-
-// One element's S slices: X = the element scaled by 2^-(emax - 1022 - F +
-// 53) and rounded half up to an integer of F = 7 + 8 (S - 1) bits, cut into
-// balanced base-256 digits (the digits of |X|, with X's sign), least
-// significant in slice S - 1.  For S <= 4 (F <= 31) |X| <= 2^31 and the
-// digits come from 32-bit arithmetic: d = ((U + 128) & 255) - 128 and
-// U <- (U + 128) >> 8, since U - d = (U + 128) rounded down to a multiple of
-// 256.  Larger S keeps 64-bit arithmetic.
-__device__ __forceinline__ void write_digits(long long bits, uint32_t emax, int F, int S, __nv_bfloat16* out,
-                                             int64_t stride) {
-  const uint32_t e = (uint32_t)((bits >> 52) & 0x7FF);
-  const bool neg = bits < 0;
-  unsigned long long U = 0;
-  if (e != 0 && emax != 0) {
-    const unsigned long long mant = ((unsigned long long)bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    const int sh = 53 + (int)(emax - e) - F;  // U = mant * 2^-sh, rounded half up
-    if (sh <= 0) U = mant << (-sh);
-    else if (sh < 64) U = (mant + (1ull << (sh - 1))) >> sh;
-  }
-  if (F <= 31) {
-    uint32_t u = (uint32_t)U;  // <= 2^31
-    for (int s = S - 1; s >= 1; --s) {
-      const int d = (int)((u + 128u) & 255u) - 128;
-      u = (u + 128u) >> 8;
-      out[s * stride] = __int2bfloat16_rn(neg ? -d : d);
-    }
-    out[0] = __int2bfloat16_rn(neg ? -(int)u : (int)u);
-  } else {
-    unsigned long long u = U;
-    for (int s = S - 1; s >= 1; --s) {
-      const int d = (int)((u + 128ull) & 255ull) - 128;
-      u = (u + 128ull) >> 8;
-      out[s * stride] = __int2bfloat16_rn(neg ? -d : d);
-    }
-    out[0] = __int2bfloat16_rn(neg ? -(int)u : (int)u);
-  }
-}
-
+// Operand splits (dev::row_exponent_body, dev::digits_body, dev::short_rows_body).
 __global__ void __launch_bounds__(256) row_exponent_kernel(const SplitRowSet* __restrict__ sets, int nsets,
                                                            int64_t total_chunks) {
   __shared__ uint32_t red[8];
-  for (int64_t chunk = blockIdx.x; chunk < total_chunks; chunk += gridDim.x) {
-    int set;
-    int64_t row, k0;
-    locate_chunk(sets, nsets, chunk, set, row, k0);
-    const SplitRowSet& rs = sets[set];
-    const double* src = rs.src + row * rs.ld;
-    const int64_t k1 = min(rs.K, k0 + kSplitChunk);
-    uint32_t emax = 0;
-    // four loads in flight per thread (the loop is bound by load latency)
-    for (int64_t k = k0 + threadIdx.x; k < k1; k += 4 * 256) {
-      long long v[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) v[u] = k + u * 256 < k1 ? __double_as_longlong(__ldg(src + k + u * 256)) : 0;
-#pragma unroll
-      for (int u = 0; u < 4; ++u) emax = max(emax, (uint32_t)((v[u] >> 52) & 0x7FF));
-    }
-    for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = emax;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      uint32_t m = 0;
-      for (int w = 0; w < 8; ++w) m = max(m, red[w]);
-      if (m) atomicMax((unsigned int*)(rs.exps + row), m);
-    }
-    __syncthreads();
-  }
+  dev::row_exponent_body<false>(sets, nsets, total_chunks, blockIdx.x, gridDim.x, red);
 }
 
-// exps hold the largest biased exponent of each row (0 for an all-zero row).
 __global__ void __launch_bounds__(256) digits_kernel(const SplitRowSet* __restrict__ sets, int nsets,
                                                      int64_t total_chunks, int S) {
-  const int F = 7 + 8 * (S - 1);
-  for (int64_t chunk = blockIdx.x; chunk < total_chunks; chunk += gridDim.x) {
-    int set;
-    int64_t row, k0;
-    locate_chunk(sets, nsets, chunk, set, row, k0);
-    const SplitRowSet& rs = sets[set];
-    const double* src = rs.src + row * rs.ld;
-    __nv_bfloat16* dst = rs.dst + row * rs.Kp;
-    const uint32_t emax = (uint32_t)rs.exps[row];
-    const int64_t k1 = min(rs.K, k0 + kSplitChunk);
-    for (int64_t k = k0 + threadIdx.x; k < k1; k += 4 * 256) {
-      long long v[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) v[u] = k + u * 256 < k1 ? __double_as_longlong(__ldg(src + k + u * 256)) : 0;
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-        if (k + u * 256 < k1) write_digits(v[u], emax, F, S, dst + k + u * 256, rs.slice_stride);
-    }
-    // the row's last chunk also clears its K padding (the slice buffers may be
-    // an arena shared with other plans, so nothing else keeps it zero)
-    if (k1 == rs.K)
-      for (int64_t k = rs.K + threadIdx.x; k < rs.Kp; k += 256)
-        for (int s = 0; s < S; ++s) dst[s * rs.slice_stride + k] = __int2bfloat16_rn(0);
-  }
+  dev::digits_body<false>(sets, nsets, total_chunks, S, blockIdx.x, gridDim.x);
 }
 
-// Short rows: one warp handles a whole row (exponent by warp shuffles, then
-// the digits); the row sets here carry first_row in rows.
 __global__ void __launch_bounds__(256) split_short_rows_kernel(const SplitRowSet* __restrict__ sets, int nsets,
                                                                int64_t total_rows, int S) {
-  const int F = 7 + 8 * (S - 1);
-  const int lane = threadIdx.x & 31;
-  for (int64_t rg = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5); rg < total_rows; rg += (int64_t)gridDim.x * 8) {
-    int lo = 0, hi = nsets - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (sets[mid].first_row <= rg) lo = mid; else hi = mid - 1;
-    }
-    const SplitRowSet& rs = sets[lo];
-    const int64_t row = rg - rs.first_row;
-    const double* src = rs.src + row * rs.ld;
-    uint32_t emax = 0;
-    for (int64_t k = lane; k < rs.K; k += 32)
-      emax = max(emax, (uint32_t)((__double_as_longlong(__ldg(src + k)) >> 52) & 0x7FF));
-    for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
-    if (lane == 0) rs.exps[row] = (int)emax;
-    __nv_bfloat16* dst = rs.dst + row * rs.Kp;
-    for (int64_t k = lane; k < rs.K; k += 32)
-      write_digits(__double_as_longlong(__ldg(src + k)), emax, F, S, dst + k, rs.slice_stride);
-    for (int64_t k = rs.K + lane; k < rs.Kp; k += 32)
-      for (int s = 0; s < S; ++s) dst[s * rs.slice_stride + k] = __int2bfloat16_rn(0);
-  }
+  dev::short_rows_body<false>(sets, nsets, total_rows, S, blockIdx.x, gridDim.x);
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
@@ -1169,6 +1011,10 @@ struct SplitLaunch {  // the problems of one output tile width
   int* d_tile_first = nullptr;
   CUtensorMap* d_maps = nullptr;
   int nprob = 0, total_tiles = 0;
+  // host copies (merged launches of the persistent iteration program)
+  std::vector<DevProblem> hp;
+  std::vector<CUtensorMap> hm;
+  std::vector<int> hfirst;
 };
 
 struct SplitPlan {
@@ -1484,7 +1330,10 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
     GBX_TRY(up(lp.data(), sizeof(DevProblem) * lp.size(), (void**)&L.d_probs));
     GBX_TRY(up(first.data(), sizeof(int) * first.size(), (void**)&L.d_tile_first));
     GBX_TRY(up(lm.data(), sizeof(CUtensorMap) * lm.size(), (void**)&L.d_maps));
-    sp->launches.push_back(L);
+    L.hp = lp;
+    L.hm = lm;
+    L.hfirst = first;
+    sp->launches.push_back(std::move(L));
   }
   GBX_TRY(dev_alloc((void**)&sp->d_err, sizeof(int)));
   GBX_CUDA(cudaMemset(sp->d_err, 0, sizeof(int)));
@@ -1508,25 +1357,38 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
 
 int split_operands(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st) {
   if (!sp || sp->nsets == 0) return GBX_OK;
+  ProgRecorder* rec = prog_recording();
   for (int side = 0; side < 2; ++side) {
     if ((side == 0 && !plan_a) || (side == 1 && !plan_b)) continue;
     const int64_t chunks = side == 0 ? sp->rows_a : sp->rows_b;
     if (chunks > 0) {
       const SplitRowSet* sets = side == 0 ? sp->d_sets_a : sp->d_sets_b;
       const int nsets = side == 0 ? sp->nlong_a : sp->nlong_b;
-      for (auto& z : (side == 0 ? sp->exp_ranges_a : sp->exp_ranges_b))
-        GBX_CUDA(cudaMemsetAsync(z.first, 0, z.second, st));
+      for (auto& z : (side == 0 ? sp->exp_ranges_a : sp->exp_ranges_b)) GBX_TRY(zero_async(z.first, z.second, st));
       const int grid = (int)std::min<int64_t>(chunks, 152 * 16);
-      row_exponent_kernel<<<grid, 256, 0, st>>>(sets, nsets, chunks);
-      GBX_CUDA(cudaGetLastError());
-      digits_kernel<<<grid, 256, 0, st>>>(sets, nsets, chunks, sp->S);
-      GBX_CUDA(cudaGetLastError());
+      if (rec) {
+        ProgArgs a;
+        a.sets = {sets, chunks, nsets, sp->S};
+        GBX_TRY(prog_mem(rec, PK_ROWEXP, (uint32_t)grid, a, {}));
+        GBX_TRY(prog_mem(rec, PK_DIGITS, (uint32_t)grid, a, {}));
+      } else {
+        row_exponent_kernel<<<grid, 256, 0, st>>>(sets, nsets, chunks);
+        GBX_CUDA(cudaGetLastError());
+        digits_kernel<<<grid, 256, 0, st>>>(sets, nsets, chunks, sp->S);
+        GBX_CUDA(cudaGetLastError());
+      }
     }
     const int64_t srows = side == 0 ? sp->short_rows_a : sp->short_rows_b;
     if (srows > 0) {
       const SplitRowSet* sets = side == 0 ? sp->d_short_a : sp->d_short_b;
       const int nsets = side == 0 ? sp->nshort_a : sp->nshort_b;
       const int grid = (int)std::min<int64_t>((srows + 7) / 8, 152 * 32);
+      if (rec) {
+        ProgArgs a;
+        a.sets = {sets, srows, nsets, sp->S};
+        GBX_TRY(prog_mem(rec, PK_SHORTROWS, (uint32_t)grid, a, {}));
+        continue;
+      }
       split_short_rows_kernel<<<grid, 256, 0, st>>>(sets, nsets, srows, sp->S);
       GBX_CUDA(cudaGetLastError());
     }
@@ -1534,8 +1396,59 @@ int split_operands(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st) {
   return GBX_OK;
 }
 
+namespace {
+
 template <int BN>
-int launch_width(const SplitPlan* sp, const SplitLaunch& L, int nsm, cudaStream_t st) {
+int launch_width(const GemmParams& P, int nsm, cudaStream_t st) {
+  const int grid = std::min(P.total_tiles, nsm * SplitCfg<BN>::kCtasPerSm);
+  split_gemm_kernel<BN><<<grid, SplitCfg<BN>::kThreads, sizeof(Smem<BN>) + 1024, st>>>(P);
+  GBX_CUDA(cudaGetLastError());
+  return GBX_OK;
+}
+
+// The GEMM kernel of one launch class -- bn 0 / 1: thin-K with a 64 / 32
+// element k-block; 64 with S <= 4: k-stationary; else the pair-by-pair
+// kernel of that output tile width -- over the problems of P.
+int launch_split_gemm(int bn, const GemmParams& P, cudaStream_t st) {
+  if (P.total_tiles <= 0) return GBX_OK;
+  int dev = 0, nsm = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (bn <= 1) {
+    if (bn == 0)
+      split_thin_kernel<64><<<std::min(P.total_tiles, nsm), kThinThreads, sizeof(ThinSmem<64>) + 1024, st>>>(P);
+    else
+      split_thin_kernel<32><<<std::min(P.total_tiles, nsm), kThinThreads, sizeof(ThinSmem<32>) + 1024, st>>>(P);
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) {
+      cudaFuncAttributes fa;
+      std::memset(&fa, 0, sizeof(fa));
+      cudaFuncGetAttributes(&fa, bn == 0 ? (const void*)split_thin_kernel<64> : (const void*)split_thin_kernel<32>);
+      return fail(GBX_ECUDA, "thin-K launch (k-block %d): %s; dynamic smem %zu (max %d), static %zu, regs %d, max threads %d",
+                  bn == 0 ? 64 : 32, cudaGetErrorString(le), (bn == 0 ? sizeof(ThinSmem<64>) : sizeof(ThinSmem<32>)) + 1024,
+                  fa.maxDynamicSharedSizeBytes, fa.sharedSizeBytes, fa.numRegs, fa.maxThreadsPerBlock);
+    }
+    return GBX_OK;
+  }
+  switch (bn) {
+    case 32: return launch_width<32>(P, nsm, st);
+    case 64:
+      if (P.S <= kKsMaxS) {
+        const int g = std::min(P.total_tiles, nsm);
+        const size_t sh = sizeof(KsSmem) + 1024;
+        if (P.S == 2) split_ks_kernel<2><<<g, kKsThreads, sh, st>>>(P);
+        else if (P.S == 3) split_ks_kernel<3><<<g, kKsThreads, sh, st>>>(P);
+        else split_ks_kernel<4><<<g, kKsThreads, sh, st>>>(P);
+        GBX_CUDA(cudaGetLastError());
+        return GBX_OK;
+      }
+      return launch_width<64>(P, nsm, st);
+    case 128: return launch_width<128>(P, nsm, st);
+    default: return launch_width<256>(P, nsm, st);
+  }
+}
+
+GemmParams params_of(const SplitPlan* sp, const SplitLaunch& L) {
   GemmParams P;
   P.probs = L.d_probs;
   P.tile_first = L.d_tile_first;
@@ -1545,79 +1458,99 @@ int launch_width(const SplitPlan* sp, const SplitLaunch& L, int nsm, cudaStream_
   P.S = sp->S;
   P.L = sp->L;
   P.err = sp->d_err;
-  const int grid = std::min(L.total_tiles, nsm * SplitCfg<BN>::kCtasPerSm);
-  split_gemm_kernel<BN><<<grid, SplitCfg<BN>::kThreads, sizeof(Smem<BN>) + 1024, st>>>(P);
-  GBX_CUDA(cudaGetLastError());
-  return GBX_OK;
+  return P;
 }
+
+}  // namespace
 
 int run_split_plan(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st) {
   if (!sp || sp->nsets == 0) return GBX_OK;
   GBX_TRY(split_operands(sp, plan_a, plan_b, st));
-  int dev = 0, nsm = 152;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  for (const SplitLaunch& L : sp->launches) {
+  ProgRecorder* rec = prog_recording();
+  for (size_t i = 0; i < sp->launches.size(); ++i) {
+    const SplitLaunch& L = sp->launches[i];
     if (L.total_tiles <= 0) continue;
-    if (L.bn <= 1) {
-      GemmParams P;
-      P.probs = L.d_probs;
-      P.tile_first = L.d_tile_first;
-      P.maps = L.d_maps;
-      P.nprob = L.nprob;
-      P.total_tiles = L.total_tiles;
-      P.S = sp->S;
-      P.L = sp->L;
-      P.err = sp->d_err;
-      if (L.bn == 0)
-        split_thin_kernel<64><<<std::min(L.total_tiles, nsm), kThinThreads, sizeof(ThinSmem<64>) + 1024, st>>>(P);
-      else
-        split_thin_kernel<32><<<std::min(L.total_tiles, nsm), kThinThreads, sizeof(ThinSmem<32>) + 1024, st>>>(P);
-      const cudaError_t le = cudaGetLastError();
-      if (le != cudaSuccess) {
-        cudaFuncAttributes fa;
-        std::memset(&fa, 0, sizeof(fa));
-        cudaFuncGetAttributes(&fa, L.bn == 0 ? (const void*)split_thin_kernel<64> : (const void*)split_thin_kernel<32>);
-        return fail(GBX_ECUDA, "thin-K launch (k-block %d): %s; dynamic smem %zu (max %d), static %zu, regs %d, max threads %d",
-                    L.bn == 0 ? 64 : 32, cudaGetErrorString(le), (L.bn == 0 ? sizeof(ThinSmem<64>) : sizeof(ThinSmem<32>)) + 1024,
-                    fa.maxDynamicSharedSizeBytes, fa.sharedSizeBytes, fa.numRegs, fa.maxThreadsPerBlock);
-      }
-      continue;
-    }
-    switch (L.bn) {
-      case 32: GBX_TRY(launch_width<32>(sp, L, nsm, st)); break;
-      case 64:
-        if (sp->S <= kKsMaxS) {
-          GemmParams P;
-          P.probs = L.d_probs;
-          P.tile_first = L.d_tile_first;
-          P.maps = L.d_maps;
-          P.nprob = L.nprob;
-          P.total_tiles = L.total_tiles;
-          P.S = sp->S;
-          P.L = sp->L;
-          P.err = sp->d_err;
-          const int g = std::min(L.total_tiles, nsm);
-          const size_t sh = sizeof(KsSmem) + 1024;
-          if (sp->S == 2) split_ks_kernel<2><<<g, kKsThreads, sh, st>>>(P);
-          else if (sp->S == 3) split_ks_kernel<3><<<g, kKsThreads, sh, st>>>(P);
-          else split_ks_kernel<4><<<g, kKsThreads, sh, st>>>(P);
-          GBX_CUDA(cudaGetLastError());
-        } else {
-          GBX_TRY(launch_width<64>(sp, L, nsm, st));
-        }
-        break;
-      case 128: GBX_TRY(launch_width<128>(sp, L, nsm, st)); break;
-      default: GBX_TRY(launch_width<256>(sp, L, nsm, st)); break;
-    }
+    if (rec) GBX_TRY(prog_split(rec, sp, (int)i));
+    else GBX_TRY(launch_split_gemm(L.bn, params_of(sp, L), st));
   }
   if (sp->nred > 0) {
     int rg = (int)std::min<int64_t>((sp->red_total + 255) / 256, 152 * 8);
+    if (rec) {
+      ProgArgs a;
+      a.splitred = {sp->d_all, sp->d_red_prob, sp->d_red_first, sp->red_total, sp->nred};
+      return prog_mem(rec, PK_SPLITRED, (uint32_t)rg, a, {});
+    }
     split_reduce_kernel<<<rg, 256, 0, st>>>(sp->d_all, sp->d_red_prob, sp->d_red_first, sp->nred, sp->red_total);
     GBX_CUDA(cudaGetLastError());
   }
   return GBX_OK;
 }
+
+// ---- merged launches of the persistent iteration program -------------------
+
+int split_launch_class(const SplitPlan* sp, int launch) {
+  if (!sp || launch < 0 || launch >= (int)sp->launches.size()) return -1;
+  const int bn = sp->launches[launch].bn;
+  return bn * 16 + sp->S;  // kernel and slice count
+}
+
+struct SplitMerged {
+  int bn = 0;
+  GemmParams P;
+  DevProblem* d_probs = nullptr;
+  int* d_first = nullptr;
+  CUtensorMap* d_maps = nullptr;
+  ~SplitMerged() {
+    dev_free(d_probs);
+    dev_free(d_first);
+    dev_free(d_maps);
+  }
+};
+
+int split_merge(const std::vector<std::pair<SplitPlan*, int>>& parts, int* err, SplitMerged** out) {
+  *out = nullptr;
+  if (parts.empty()) return fail(GBX_EINVAL, "split merge: no launches");
+  auto m = std::make_unique<SplitMerged>();
+  const int cls = split_launch_class(parts[0].first, parts[0].second);
+  std::vector<DevProblem> hp;
+  std::vector<CUtensorMap> hm;
+  std::vector<int> first;
+  int64_t tiles = 0;
+  for (auto& pr : parts) {
+    if (split_launch_class(pr.first, pr.second) != cls) return fail(GBX_EINVAL, "split merge: mixed launch classes");
+    const SplitLaunch& L = pr.first->launches[pr.second];
+    for (size_t i = 0; i < L.hp.size(); ++i) {
+      hp.push_back(L.hp[i]);
+      hm.push_back(L.hm[2 * i]);
+      hm.push_back(L.hm[2 * i + 1]);
+      first.push_back((int)(tiles + L.hfirst[i]));
+    }
+    tiles += L.total_tiles;
+  }
+  if (tiles >= (1ll << 31)) return fail(GBX_EUNSUPPORTED, "split merge: too many tiles");
+  GBX_TRY(dev_alloc((void**)&m->d_probs, sizeof(DevProblem) * hp.size()));
+  GBX_TRY(dev_alloc((void**)&m->d_first, sizeof(int) * first.size()));
+  GBX_TRY(dev_alloc((void**)&m->d_maps, sizeof(CUtensorMap) * hm.size()));
+  GBX_CUDA(cudaMemcpy(m->d_probs, hp.data(), sizeof(DevProblem) * hp.size(), cudaMemcpyHostToDevice));
+  GBX_CUDA(cudaMemcpy(m->d_first, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice));
+  GBX_CUDA(cudaMemcpy(m->d_maps, hm.data(), sizeof(CUtensorMap) * hm.size(), cudaMemcpyHostToDevice));
+  const SplitPlan* sp0 = parts[0].first;
+  m->bn = sp0->launches[parts[0].second].bn;
+  m->P.probs = m->d_probs;
+  m->P.tile_first = m->d_first;
+  m->P.maps = m->d_maps;
+  m->P.nprob = (int)hp.size();
+  m->P.total_tiles = (int)tiles;
+  m->P.S = sp0->S;
+  m->P.L = sp0->L;
+  m->P.err = err;
+  *out = m.release();
+  return GBX_OK;
+}
+
+int split_merged_run(const SplitMerged* m, cudaStream_t st) { return launch_split_gemm(m->bn, m->P, st); }
+
+void split_merged_destroy(SplitMerged* m) { delete m; }
 
 int split_plan_error(SplitPlan* sp) {
   if (!sp) return 0;

@@ -7,6 +7,7 @@
 #include <set>
 #include <tuple>
 
+#include "program.h"
 #include "split.h"
 
 namespace gbx {
@@ -810,11 +811,11 @@ int ContractionPlan::tune_split(cudaStream_t st, int reps) {
 int ContractionPlan::prepare_static(const double* dA, const double* dB, cudaStream_t st) {
   if (direct) return GBX_OK;  // reads its operands where they are stored
   if (a_static) {
-    if (a_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Abig, 0, sizeof(double) * a_elems, st));
+    if (a_needs_zero) GBX_TRY(zero_async(d_Abig, sizeof(double) * a_elems, st));
     GBX_TRY(run_moves(packA, dA, d_Abig, st));
   }
   if (b_static) {
-    if (b_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Bbig, 0, sizeof(double) * b_elems, st));
+    if (b_needs_zero) GBX_TRY(zero_async(d_Bbig, sizeof(double) * b_elems, st));
     GBX_TRY(run_moves(packB, dB, d_Bbig, st));
   }
   if (split) GBX_TRY(split_operands(split, a_static, b_static, st));
@@ -827,11 +828,11 @@ int ContractionPlan::stage(const double* dA, const double* dB, cudaStream_t st) 
   const bool skipA = a_static && static_ready, skipB = b_static && static_ready;
   if ((!skipA && !dA) || (!skipB && !dB)) return fail(GBX_EINVAL, "contraction operand without device memory");
   if (!skipA) {
-    if (a_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Abig, 0, sizeof(double) * a_elems, st));
+    if (a_needs_zero) GBX_TRY(zero_async(d_Abig, sizeof(double) * a_elems, st));
     GBX_TRY(run_moves(packA, dA, d_Abig, st));
   }
   if (!skipB) {
-    if (b_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Bbig, 0, sizeof(double) * b_elems, st));
+    if (b_needs_zero) GBX_TRY(zero_async(d_Bbig, sizeof(double) * b_elems, st));
     GBX_TRY(run_moves(packB, dB, d_Bbig, st));
   }
   if (split) GBX_TRY(split_operands(split, !skipA, !skipB, st));
@@ -847,11 +848,11 @@ int ContractionPlan::execute(const double* dA, const double* dB, double* dC, dou
   const bool skipA = a_static && static_ready, skipB = b_static && static_ready;
   if ((!skipA && !dA) || (!skipB && !dB)) return fail(GBX_EINVAL, "contraction operand without device memory");
   if (!skipA) {
-    if (a_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Abig, 0, sizeof(double) * a_elems, st));
+    if (a_needs_zero) GBX_TRY(zero_async(d_Abig, sizeof(double) * a_elems, st));
     GBX_TRY(run_moves(packA, dA, d_Abig, st));
   }
   if (!skipB) {
-    if (b_needs_zero) GBX_CUDA(cudaMemsetAsync(d_Bbig, 0, sizeof(double) * b_elems, st));
+    if (b_needs_zero) GBX_TRY(zero_async(d_Bbig, sizeof(double) * b_elems, st));
     GBX_TRY(run_moves(packB, dB, d_Bbig, st));
   }
   GBX_TRY(f64.run(st));

@@ -3,6 +3,7 @@
 // accumulation chunks, recombined in FP64 (gemm_split.cu).
 #pragma once
 #include <cstdint>
+#include <utility>
 #include <vector>
 
 #include "common.h"
@@ -50,5 +51,16 @@ double split_plan_bytes(const SplitPlan* sp);
 double split_plan_tensor_flops(const SplitPlan* sp);
 // Error word of the GEMM kernel (0 = ok, else the wait that ran out); syncs.
 int split_plan_error(SplitPlan* sp);
+
+// GEMM launches of several plans merged into one launch per kernel (the
+// persistent iteration program): launches of the same class run the same
+// kernel with the same slice count, so their problems can share a launch.
+int split_launch_class(const SplitPlan* sp, int launch);
+struct SplitMerged;
+// parts: (plan, launch index) pairs of one class; err: the merged launch's
+// error word (bounded waits that run out).
+int split_merge(const std::vector<std::pair<SplitPlan*, int>>& parts, int* err, SplitMerged** out);
+int split_merged_run(const SplitMerged* m, cudaStream_t st);
+void split_merged_destroy(SplitMerged* m);
 
 }  // namespace gbx

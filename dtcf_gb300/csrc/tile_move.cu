@@ -11,14 +11,16 @@
 #include <cstdio>
 #include <cstring>
 
+#include "bodies.cuh"
 #include "common.h"
+#include "program.h"
 
 namespace gbx {
 
 namespace {
-constexpr int kMoveThreads = 256;
-constexpr int kMoveChunk = 2048;   // elements per CTA (general moves)
-constexpr int kMove4Chunk = 4096;  // elements per CTA (moves of at most four dimensions)
+using dev::kMove4Chunk;
+using dev::kMoveChunk;
+using dev::kMoveThreads;
 }  // namespace
 
 MoveDesc make_move(int rank, const int64_t* ext, const int64_t* sstr, const int64_t* dstr, int64_t src,
@@ -170,195 +172,41 @@ __global__ void __launch_bounds__(kMoveThreads) tile_move_kernel(const MoveDesc*
                                                                  const uint32_t* __restrict__ first, int ndesc,
                                                                  uint32_t nchunks, const double* __restrict__ src,
                                                                  double* __restrict__ dst, double alpha) {
-  for (uint32_t chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
-    // binary search: last descriptor whose first chunk <= chunk
-    int lo = 0, hi = ndesc - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (__ldg(first + mid) <= chunk) lo = mid; else hi = mid - 1;
-    }
-    const MoveDesc& md = descs[lo];
-    const uint32_t base = (chunk - __ldg(first + lo)) * kMoveChunk;
-    const int rank = md.rank;
-    const uint32_t n = md.n;
-    const int op = md.op;
-    // accumulating moves take the run-time factor (a contraction's alpha)
-    const double scale = op == 0 ? md.scale : __dmul_rn(md.scale, alpha);
-    const double* __restrict__ s = src + md.src;
-    double* __restrict__ t = dst + md.dst;
-    // all addresses first, then every load, then every store: eight
-    // independent loads in flight per thread
-    constexpr int kPer = kMoveChunk / kMoveThreads;
-    int64_t so[kPer], to[kPer];
-    bool in[kPer];
-#pragma unroll
-    for (int k = 0; k < kPer; ++k) {
-      const uint32_t e = base + (uint32_t)(k * kMoveThreads) + threadIdx.x;
-      in[k] = e < n;
-      so[k] = 0;
-      to[k] = 0;
-      uint32_t rem = in[k] ? e : 0;
-      for (int d = rank - 1; d > 0; --d) {
-        const uint32_t q = md.div[d].div(rem);
-        const uint32_t i = rem - q * md.ext[d];
-        so[k] += (int64_t)i * md.sstr[d];
-        to[k] += (int64_t)i * md.dstr[d];
-        rem = q;
-      }
-      so[k] += (int64_t)rem * md.sstr[0];
-      to[k] += (int64_t)rem * md.dstr[0];
-    }
-    double x[kPer];
-#pragma unroll
-    for (int k = 0; k < kPer; ++k) x[k] = in[k] ? __ldg(s + so[k]) : 0.0;
-    const unsigned long long sb = (unsigned long long)__double_as_longlong(scale);
-    if (op == 0 && (sb & 0x7FFFFFFFFFFFFFFFull) == 0x3FF0000000000000ull) {
-      // +-x: a bit copy with the sign bit set on the integer pipe
-      const long long flip = (long long)(sb & 0x8000000000000000ull);
-#pragma unroll
-      for (int k = 0; k < kPer; ++k)
-        if (in[k]) t[to[k]] = __longlong_as_double(__double_as_longlong(x[k]) ^ flip);
-    } else if (op == 0) {
-#pragma unroll
-      for (int k = 0; k < kPer; ++k)
-        if (in[k]) t[to[k]] = __dmul_rn(scale, x[k]);
-    } else {
-      double y[kPer];
-#pragma unroll
-      for (int k = 0; k < kPer; ++k) y[k] = in[k] ? t[to[k]] : 0.0;
-#pragma unroll
-      for (int k = 0; k < kPer; ++k)
-        if (in[k]) t[to[k]] = __fma_rn(scale, x[k], y[k]);
-    }
-  }
+  dev::move_body<false>(descs, first, ndesc, nchunks, src, dst, alpha, blockIdx.x, gridDim.x);
 }
 
-// Moves of at most four dimensions: the chunk's descriptor comes from a
-// table, its fields are read once per chunk into registers and the index
-// decode is fully unrolled (three multiply-high divisions per element), so
-// the kernel issues a few tens of instructions per element and streams at
-// memory speed.  Each thread handles kMove4Chunk / kMoveThreads elements in
-// two batches, addresses first, then every load, then every store.  A move
-// marked for pairs (contiguous even inner runs at even offsets) goes two
-// elements per index decode with 16-byte loads and stores.
+// Moves of at most four dimensions (dev::move4_body).
 __global__ void __launch_bounds__(kMoveThreads) tile_move4_kernel(const MoveDesc4* __restrict__ descs,
                                                                   const uint32_t* __restrict__ chunk_desc,
                                                                   uint32_t nchunks, const double* __restrict__ src,
                                                                   double* __restrict__ dst, double alpha,
                                                                   int allow_pairs) {
-  constexpr int kPer = 8;
-  constexpr int kBatches = kMove4Chunk / (kMoveThreads * kPer);
-  for (uint32_t chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
-    const MoveDesc4* __restrict__ md = descs + __ldg(chunk_desc + chunk);
-    const uint32_t n = md->n;
-    const uint32_t base = (chunk - md->first) * kMove4Chunk;
-    const int op = md->op;
-    const double scale = op == 0 ? md->scale : __dmul_rn(md->scale, alpha);
-    const FastDiv d1 = md->div[1], d2 = md->div[2], d3 = md->div[3];
-    const int64_t s0 = md->sstr[0], s1 = md->sstr[1], s2 = md->sstr[2], s3 = md->sstr[3];
-    const int64_t t0 = md->dstr[0], t1 = md->dstr[1], t2 = md->dstr[2], t3 = md->dstr[3];
-    const double* __restrict__ s = src + md->src;
-    double* __restrict__ t = dst + md->dst;
-    // stores of +-x are bit copies with the sign bit set on the integer pipe
-    // (a select between x and scale * x would issue the multiply anyway, and
-    // FP64 instructions are scarce on this part)
-    const unsigned long long sb = (unsigned long long)__double_as_longlong(scale);
-    const bool unit = op == 0 && (sb & 0x7FFFFFFFFFFFFFFFull) == 0x3FF0000000000000ull;
-    const long long flip = (long long)(sb & 0x8000000000000000ull);
-    if (allow_pairs && md->pad == 1) {
-      // pairs (2e, 2e + 1): the chunk's kMove4Chunk elements in one batch of
-      // kPer pairs per thread
-      int64_t so[kPer], to[kPer];
-      bool in[kPer];
-#pragma unroll
-      for (int k = 0; k < kPer; ++k) {
-        const uint32_t e = base + 2u * ((uint32_t)(k * kMoveThreads) + threadIdx.x);
-        in[k] = e < n;
-        const uint32_t r = in[k] ? e : 0;
-        const uint32_t q3 = d3.div(r), c3 = r - q3 * d3.d;
-        const uint32_t q2 = d2.div(q3), c2 = q3 - q2 * d2.d;
-        const uint32_t c0 = d1.div(q2), c1 = q2 - c0 * d1.d;
-        so[k] = (int64_t)c0 * s0 + (int64_t)c1 * s1 + (int64_t)c2 * s2 + (int64_t)c3 * s3;
-        to[k] = (int64_t)c0 * t0 + (int64_t)c1 * t1 + (int64_t)c2 * t2 + (int64_t)c3 * t3;
-      }
-      double2 x[kPer];
-#pragma unroll
-      for (int k = 0; k < kPer; ++k)
-        x[k] = in[k] ? __ldg(reinterpret_cast<const double2*>(s + so[k])) : make_double2(0.0, 0.0);
-      if (unit) {
-#pragma unroll
-        for (int k = 0; k < kPer; ++k)
-          if (in[k])
-            *reinterpret_cast<double2*>(t + to[k]) =
-                make_double2(__longlong_as_double(__double_as_longlong(x[k].x) ^ flip),
-                             __longlong_as_double(__double_as_longlong(x[k].y) ^ flip));
-      } else if (op == 0) {
-#pragma unroll
-        for (int k = 0; k < kPer; ++k)
-          if (in[k]) *reinterpret_cast<double2*>(t + to[k]) = make_double2(__dmul_rn(scale, x[k].x), __dmul_rn(scale, x[k].y));
-      } else {
-        double2 y[kPer];
-#pragma unroll
-        for (int k = 0; k < kPer; ++k)
-          y[k] = in[k] ? *reinterpret_cast<const double2*>(t + to[k]) : make_double2(0.0, 0.0);
-#pragma unroll
-        for (int k = 0; k < kPer; ++k)
-          if (in[k])
-            *reinterpret_cast<double2*>(t + to[k]) =
-                make_double2(__fma_rn(scale, x[k].x, y[k].x), __fma_rn(scale, x[k].y, y[k].y));
-      }
-      continue;
-    }
-#pragma unroll 1
-    for (int bt = 0; bt < kBatches; ++bt) {
-      int64_t so[kPer], to[kPer];
-      bool in[kPer];
-#pragma unroll
-      for (int k = 0; k < kPer; ++k) {
-        const uint32_t e = base + (uint32_t)((bt * kPer + k) * kMoveThreads) + threadIdx.x;
-        in[k] = e < n;
-        const uint32_t r = in[k] ? e : 0;
-        const uint32_t q3 = d3.div(r), c3 = r - q3 * d3.d;
-        const uint32_t q2 = d2.div(q3), c2 = q3 - q2 * d2.d;
-        const uint32_t c0 = d1.div(q2), c1 = q2 - c0 * d1.d;
-        so[k] = (int64_t)c0 * s0 + (int64_t)c1 * s1 + (int64_t)c2 * s2 + (int64_t)c3 * s3;
-        to[k] = (int64_t)c0 * t0 + (int64_t)c1 * t1 + (int64_t)c2 * t2 + (int64_t)c3 * t3;
-      }
-      double x[kPer];
-#pragma unroll
-      for (int k = 0; k < kPer; ++k) x[k] = in[k] ? __ldg(s + so[k]) : 0.0;
-      if (unit) {
-#pragma unroll
-        for (int k = 0; k < kPer; ++k)
-          if (in[k]) t[to[k]] = __longlong_as_double(__double_as_longlong(x[k]) ^ flip);
-      } else if (op == 0) {
-#pragma unroll
-        for (int k = 0; k < kPer; ++k)
-          if (in[k]) t[to[k]] = __dmul_rn(scale, x[k]);
-      } else {
-        double y[kPer];
-#pragma unroll
-        for (int k = 0; k < kPer; ++k) y[k] = in[k] ? t[to[k]] : 0.0;
-#pragma unroll
-        for (int k = 0; k < kPer; ++k)
-          if (in[k]) t[to[k]] = __fma_rn(scale, x[k], y[k]);
-      }
-    }
-  }
+  dev::move4_body<false>(descs, chunk_desc, nchunks, src, dst, alpha, allow_pairs, blockIdx.x, gridDim.x);
 }
 
 int run_moves_scaled(const MoveSet& ms, const double* src, double* dst, double alpha, cudaStream_t st) {
   if (ms.ndesc == 0 || ms.nchunks == 0) return GBX_OK;
+  ProgRecorder* rec = prog_recording();
   if (ms.d_desc4) {
     const int grid = (int)std::min<uint32_t>(ms.nchunks, 152u * 8u);
     // pairs need 16-byte aligned buffer bases (descriptor offsets are even)
     const int pairs = (((uintptr_t)src | (uintptr_t)dst) & 15) == 0 ? 1 : 0;
+    if (rec) {
+      ProgArgs a;
+      a.move4 = {ms.d_desc4, ms.d_chunk_desc, ms.nchunks, pairs, src, dst, alpha};
+      return prog_mem(rec, PK_MOVE4, (uint32_t)grid, a, {{src, false}, {dst, true}});
+    }
     tile_move4_kernel<<<grid, kMoveThreads, 0, st>>>(ms.d_desc4, ms.d_chunk_desc, ms.nchunks, src, dst, alpha,
                                                      pairs);
     GBX_CUDA(cudaGetLastError());
     return GBX_OK;
   }
   int grid = (int)std::min<uint32_t>(ms.nchunks, 152u * 16u);
+  if (rec) {
+    ProgArgs a;
+    a.move = {ms.d_desc, ms.d_first, ms.ndesc, ms.nchunks, src, dst, alpha};
+    return prog_mem(rec, PK_MOVE, (uint32_t)grid, a, {{src, false}, {dst, true}});
+  }
   tile_move_kernel<<<grid, kMoveThreads, 0, st>>>(ms.d_desc, ms.d_first, ms.ndesc, ms.nchunks, src, dst, alpha);
   GBX_CUDA(cudaGetLastError());
   return GBX_OK;
@@ -368,157 +216,31 @@ int run_moves(const MoveSet& ms, const double* src, double* dst, cudaStream_t st
   return run_moves_scaled(ms, src, dst, 1.0, st);
 }
 
-namespace {
-constexpr int kFsThreads = 256;
-constexpr int kFsPer = kFsItemElems / kFsThreads;
-// transposed slabs of one item, rows padded to an odd length: a whole-slab
-// item of n elements needs at most n + n / ea <= 2n doubles
-constexpr int kFsStage = 2 * kFsItemElems;
-static_assert(kFsPer * kFsThreads == kFsItemElems, "item size");
-}  // namespace
-
-// One CTA per work item (grid-stride over items).  Threads hold kFsPer
-// destination elements each, in destination order, and add the terms one
-// after the other: rows of slabs that are contiguous in the source's own
-// order are read directly (coalesced); slabs stored transposed are first
-// copied into shared memory in source order and read back transposed, so
-// both sides stay coalesced; anything else is gathered.  Stores are
-// coalesced along the destination.
-__global__ void __launch_bounds__(kFsThreads, 3)
+// One CTA per work item of the fused sum (dev::fused_sum_body).
+__global__ void __launch_bounds__(dev::kFsThreads, 3)
     fused_sum_kernel(const FsItem* __restrict__ items, int nitems, const FsTerm* __restrict__ terms, FsSrc src,
                      const double* __restrict__ scale, double* __restrict__ out) {
-  __shared__ double stage[kFsStage];
-  __shared__ const double* base[kFsMaxSlots];  // indexed by the term's slot
-  // the item and its terms, read field by field (keeps registers free for
-  // the elements in flight)
-  __shared__ FsItem s_item;
-  __shared__ FsTerm s_terms[kFsMaxTerms];
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int k = 0; k < kFsMaxSlots; ++k) base[k] = src.p[k];
-  }
-  for (int i = blockIdx.x; i < nitems; i += gridDim.x) {
-    __syncthreads();  // the previous item is finished with s_item, s_terms and stage
-    if (threadIdx.x == 0) s_item = items[i];
-    __syncthreads();
-    const FsItem& it = s_item;
-    if (threadIdx.x < it.nterm) s_terms[threadIdx.x] = terms[it.term0 + threadIdx.x];
-    __syncthreads();
-    const uint32_t E = it.fE.d, ea = it.fea.d, eb = it.feb.d, O1 = it.fo1.d;
-    double acc[kFsPer];
-    // element k of this thread: e = tid + k * threads (lanes past the end
-    // repeat the last element: valid addresses, no store); the outer indices
-    // of its slab, packed as o0 << 16 | o1, and its index q within the slab
-    uint32_t oo[kFsPer], qk[kFsPer];
-#pragma unroll
-    for (int k = 0; k < kFsPer; ++k) {
-      acc[k] = 0.0;
-      const uint32_t f = it.f0 + min((uint32_t)(threadIdx.x + k * kFsThreads), it.n - 1);
-      const uint32_t sg = it.fE.div(f);
-      const uint32_t o0 = it.fo1.div(sg);
-      qk[k] = f - sg * E;
-      oo[k] = (o0 << 16) | (sg - o0 * O1);
-    }
-#define FS_ELEM(k, o0, o1, q)      \
-  const uint32_t o0 = oo[k] >> 16;  \
-  const uint32_t o1 = oo[k] & 0xFFFFu; \
-  const uint32_t q = qk[k]
-    // offsets inside a source tile are 32-bit (a tile holds fewer than 2^31
-    // elements): one multiply-add each instead of 64-bit products
-    auto gather = [&](const FsTerm& tm, double* x) {
-      const double* __restrict__ p = base[tm.slot] + tm.off;
-      const uint32_t so0 = (uint32_t)tm.so0, so1 = (uint32_t)tm.so1;
-      if (tm.mode == 1 && it.whole) {
-        const uint32_t pa = ea | 1u, sp = eb * pa;
-        const uint32_t s_first = it.fE.div(it.f0);
-        __syncthreads();  // earlier reads of stage are done
-#pragma unroll
-        for (int k = 0; k < kFsPer; ++k) {
-          const uint32_t e = min((uint32_t)(threadIdx.x + k * kFsThreads), it.n - 1);
-          const uint32_t sl = it.fE.div(e);
-          const uint32_t sg = s_first + sl, o0 = it.fo1.div(sg), o1 = sg - o0 * O1;
-          x[k] = __ldg(p + (o0 * so0 + o1 * so1 + (e - sl * E)));
-        }
-#pragma unroll
-        for (int k = 0; k < kFsPer; ++k) {
-          const uint32_t e = threadIdx.x + k * kFsThreads;
-          if (e < it.n) {
-            const uint32_t sl = it.fE.div(e);
-            const uint32_t qq = e - sl * E;  // source order within the slab: b * ea + a
-            const uint32_t b = it.fea.div(qq);
-            stage[sl * sp + b * pa + (qq - b * ea)] = x[k];
-          }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < kFsPer; ++k) {
-          const uint32_t e = min((uint32_t)(threadIdx.x + k * kFsThreads), it.n - 1);
-          const uint32_t sl = it.fE.div(e), q = qk[k];
-          const uint32_t a = it.feb.div(q);
-          x[k] = stage[sl * sp + (q - a * eb) * pa + a];
-        }
-      } else if (tm.mode == 0) {
-#pragma unroll
-        for (int k = 0; k < kFsPer; ++k) {
-          FS_ELEM(k, o0, o1, q);
-          x[k] = __ldg(p + (o0 * so0 + o1 * so1 + q));
-        }
-      } else {
-        const uint32_t sa = (uint32_t)tm.sa, sb = (uint32_t)tm.sb;
-#pragma unroll
-        for (int k = 0; k < kFsPer; ++k) {
-          FS_ELEM(k, o0, o1, q);
-          const uint32_t a = it.feb.div(q);
-          x[k] = __ldg(p + (o0 * so0 + o1 * so1 + a * sa + (q - a * eb) * sb));
-        }
-      }
-    };
-    // FP64 instructions are the scarce resource here (the FP64 pipe issues
-    // about 1.6 per clock per SM, fewer than the elements HBM delivers): the
-    // first term of a +-1 coefficient is a sign flip on the bits (0 + c x
-    // with -0 turned into +0), every other term one fused multiply-add --
-    // the separately rounded product and sum whenever c x is exact, as it is
-    // for c = +-2^k
-    uint32_t t0 = 0;
-    if (it.nterm > 0) {
-      const unsigned long long cbits = (unsigned long long)__double_as_longlong(s_terms[0].coef);
-      if ((cbits & 0x7FFFFFFFFFFFFFFFull) == 0x3FF0000000000000ull) {
-        double x[kFsPer];
-        gather(s_terms[0], x);
-        const unsigned long long sign = cbits & 0x8000000000000000ull;
-#pragma unroll
-        for (int k = 0; k < kFsPer; ++k) {
-          const unsigned long long b = (unsigned long long)__double_as_longlong(x[k]) ^ sign;
-          acc[k] = __longlong_as_double((long long)(b == 0x8000000000000000ull ? 0ull : b));
-        }
-        t0 = 1;
-      }
-    }
-    for (uint32_t t = t0; t < it.nterm; ++t) {
-      double x[kFsPer];
-      gather(s_terms[t], x);
-      const double c = s_terms[t].coef;
-#pragma unroll
-      for (int k = 0; k < kFsPer; ++k) acc[k] = __fma_rn(c, x[k], acc[k]);
-    }
-#undef FS_ELEM
-#pragma unroll
-    for (int k = 0; k < kFsPer; ++k) {
-      const uint32_t e = threadIdx.x + k * kFsThreads;
-      if (e < it.n) {
-        double v = acc[k];
-        if (scale) v = __dmul_rn(v, __ldg(scale + it.dst + e));
-        out[it.dst + e] = v;
-      }
-    }
-  }
+  __shared__ dev::FsSmem sm;
+  dev::fused_sum_body<false>(items, nitems, terms, src, scale, out, blockIdx.x, gridDim.x, sm);
 }
 
 int run_fused_sum(const FsItem* items, int nitems, const FsTerm* terms, const FsSrc& src, const double* scale,
                   double* out, cudaStream_t st) {
   if (nitems == 0) return GBX_OK;
   const int grid = std::min(nitems, 152 * 6);
-  fused_sum_kernel<<<grid, kFsThreads, 0, st>>>(items, nitems, terms, src, scale, out);
+  if (ProgRecorder* rec = prog_recording()) {
+    ProgArgs a;
+    a.fused.items = items;
+    a.fused.terms = terms;
+    a.fused.scale = scale;
+    a.fused.out = out;
+    a.fused.nitems = nitems;
+    a.fused.src = src;
+    std::vector<ProgTouch> t = {{scale, false}, {out, true}};
+    for (int k = 0; k < kFsMaxSlots; ++k) t.push_back({src.p[k], false});
+    return prog_mem(rec, PK_FUSED, (uint32_t)grid, a, t);
+  }
+  fused_sum_kernel<<<grid, dev::kFsThreads, 0, st>>>(items, nitems, terms, src, scale, out);
   GBX_CUDA(cudaGetLastError());
   return GBX_OK;
 }

@@ -30,7 +30,11 @@ typedef struct {
     int method;          /* GBX_CC_CCD or GBX_CC_CCSD */
     int engine;          /* GBX_MODE_FP64 or GBX_MODE_SPLIT */
     int slices;          /* split engine: bf16 slices per operand (0 = default) */
-    int use_graph;       /* capture one iteration as a CUDA graph */
+    int use_graph;       /* 0: launch kernel by kernel; 1: capture one iteration as a CUDA graph of its
+                            kernels; 2: run the iteration as a persistent program -- a few persistent
+                            launches driven by a device-side work queue (one per dependency level of
+                            the memory-bound work, one per GEMM kernel and level) -- captured as the
+                            graph; each contraction then keeps its own workspace */
     int split_all;       /* split engine on every GEMM, however small (default: large ones only) */
     uint64_t seed;
     double eps_occ_lo, eps_occ_hi, eps_vir_lo, eps_vir_hi;
@@ -129,6 +133,18 @@ GBX_API int gbx_cc_time_gemm(gbx_cc_job* job, int contraction, int reps, float* 
  * allocates its scratch and waits for the stream. */
 GBX_API int gbx_cc_contraction_error(gbx_cc_job* job, int contraction, double* rel_frob_err, double* max_abs_err,
                                      void* stream);
+/* The persistent program of a use_graph 2 job (recorded on first use):
+ * records (memory work items, GEMM launches, other launches), dependency
+ * levels and launches per iteration.  Zeros for other jobs.
+ * Replaces: the exec / Barrier structure of ccd_t2 / ccsd_t1 / ccsd_t2
+ * (DLTC/ccd-t2.cc:97-134) -- a task pool per dependency layer, barriers
+ * between layers -- with a device-side work queue. */
+GBX_API int gbx_cc_program_info(gbx_cc_job* job, int* records, int* levels, int* launches);
+/* Self-test of the persistent program's bounded dependency wait: runs a
+ * two-record launch whose one wait can never be met, bounded by
+ * limit_cycles; returns GBX_ETIMEOUT when the wait ran out as it must (the
+ * context stays usable), GBX_OK if it did not. */
+GBX_API int gbx_cc_program_selftest(long long limit_cycles, void* stream);
 GBX_API int gbx_cc_destroy(gbx_cc_job* job);
 
 #ifdef __cplusplus
