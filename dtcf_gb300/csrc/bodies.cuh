@@ -155,45 +155,45 @@ __device__ __forceinline__ void move4_body(const MoveDesc4* __restrict__ descs, 
       // kPer pairs per thread
 #pragma unroll 1
       for (int bt = 0; bt < kPairBatches; ++bt) {
-      int64_t so[kPer], to[kPer];
-      bool in[kPer];
+        int64_t so[kPer], to[kPer];
+        bool in[kPer];
 #pragma unroll
-      for (int k = 0; k < kPer; ++k) {
-        const uint32_t e = base + 2u * ((uint32_t)((bt * kPer + k) * kMoveThreads) + threadIdx.x);
-        in[k] = e < n;
-        const uint32_t r = in[k] ? e : 0;
-        const uint32_t q3 = d3.div(r), c3 = r - q3 * d3.d;
-        const uint32_t q2 = d2.div(q3), c2 = q3 - q2 * d2.d;
-        const uint32_t c0 = d1.div(q2), c1 = q2 - c0 * d1.d;
-        so[k] = (int64_t)c0 * s0 + (int64_t)c1 * s1 + (int64_t)c2 * s2 + (int64_t)c3 * s3;
-        to[k] = (int64_t)c0 * t0 + (int64_t)c1 * t1 + (int64_t)c2 * t2 + (int64_t)c3 * t3;
-      }
-      double2 x[kPer];
-#pragma unroll
-      for (int k = 0; k < kPer; ++k)
-        x[k] = in[k] ? ldin<kCoh>(reinterpret_cast<const double2*>(s + so[k])) : make_double2(0.0, 0.0);
-      if (unit) {
+        for (int k = 0; k < kPer; ++k) {
+          const uint32_t e = base + 2u * ((uint32_t)((bt * kPer + k) * kMoveThreads) + threadIdx.x);
+          in[k] = e < n;
+          const uint32_t r = in[k] ? e : 0;
+          const uint32_t q3 = d3.div(r), c3 = r - q3 * d3.d;
+          const uint32_t q2 = d2.div(q3), c2 = q3 - q2 * d2.d;
+          const uint32_t c0 = d1.div(q2), c1 = q2 - c0 * d1.d;
+          so[k] = (int64_t)c0 * s0 + (int64_t)c1 * s1 + (int64_t)c2 * s2 + (int64_t)c3 * s3;
+          to[k] = (int64_t)c0 * t0 + (int64_t)c1 * t1 + (int64_t)c2 * t2 + (int64_t)c3 * t3;
+        }
+        double2 x[kPer];
 #pragma unroll
         for (int k = 0; k < kPer; ++k)
-          if (in[k])
-            *reinterpret_cast<double2*>(t + to[k]) =
-                make_double2(__longlong_as_double(__double_as_longlong(x[k].x) ^ flip),
-                             __longlong_as_double(__double_as_longlong(x[k].y) ^ flip));
-      } else if (op == 0) {
+          x[k] = in[k] ? ldin<kCoh>(reinterpret_cast<const double2*>(s + so[k])) : make_double2(0.0, 0.0);
+        if (unit) {
 #pragma unroll
-        for (int k = 0; k < kPer; ++k)
-          if (in[k]) *reinterpret_cast<double2*>(t + to[k]) = make_double2(__dmul_rn(scale, x[k].x), __dmul_rn(scale, x[k].y));
-      } else {
-        double2 y[kPer];
+          for (int k = 0; k < kPer; ++k)
+            if (in[k])
+              *reinterpret_cast<double2*>(t + to[k]) =
+                  make_double2(__longlong_as_double(__double_as_longlong(x[k].x) ^ flip),
+                               __longlong_as_double(__double_as_longlong(x[k].y) ^ flip));
+        } else if (op == 0) {
 #pragma unroll
-        for (int k = 0; k < kPer; ++k)
-          y[k] = in[k] ? ldrw<kCoh>(reinterpret_cast<const double2*>(t + to[k])) : make_double2(0.0, 0.0);
+          for (int k = 0; k < kPer; ++k)
+            if (in[k]) *reinterpret_cast<double2*>(t + to[k]) = make_double2(__dmul_rn(scale, x[k].x), __dmul_rn(scale, x[k].y));
+        } else {
+          double2 y[kPer];
 #pragma unroll
-        for (int k = 0; k < kPer; ++k)
-          if (in[k])
-            *reinterpret_cast<double2*>(t + to[k]) =
-                make_double2(__fma_rn(scale, x[k].x, y[k].x), __fma_rn(scale, x[k].y, y[k].y));
-      }
+          for (int k = 0; k < kPer; ++k)
+            y[k] = in[k] ? ldrw<kCoh>(reinterpret_cast<const double2*>(t + to[k])) : make_double2(0.0, 0.0);
+#pragma unroll
+          for (int k = 0; k < kPer; ++k)
+            if (in[k])
+              *reinterpret_cast<double2*>(t + to[k]) =
+                  make_double2(__fma_rn(scale, x[k].x, y[k].x), __fma_rn(scale, x[k].y, y[k].y));
+        }
       }
       continue;
     }
