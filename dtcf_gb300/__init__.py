@@ -9,5 +9,5 @@ fallback: importing ``lib()`` fails loudly when the library is missing.
 from ._lib import lib, check, GbxError, LIB_PATH  # noqa: F401
 from .leaves import (  # noqa: F401
     transpose, transpose_blocks, dltc_transpose, local_contraction, dltc_compute,
-    create_big_matrix, revert_big_matrix, grouped_gemm_f64, split_gemm,
+    create_big_matrix, create_big_matrix_nl, revert_big_matrix, grouped_gemm_f64, split_gemm,
 )

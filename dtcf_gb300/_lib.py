@@ -21,6 +21,9 @@ SIGNATURES = {
     "gbx_local_contraction_noalloc": (_i, [_i, _i, _i, _p, _p, _p, _i, _i, _d, _p]),
     "gbx_dltc_compute": (_i, [_p, _p, _p, _i, _i, _i, _p]),
     "gbx_create_big_matrix": (_i, [_i, _p, _p, _i, _p, _p, _i, _i, _i, _p, _ip, _ip, _p]),
+    "gbx_rrr_unique_tiles": (_i, [_i, ctypes.c_char_p, _p, _p, _i, _ip, _p]),
+    "gbx_rrr_initialize": (_i, [_i, _p, _p, _i, ctypes.c_int64, _p, _p]),
+    "gbx_create_big_matrix_nl": (_i, [_i, _p, _p, _i, _p, _i, _p, _i, _i, _i, _p, _p, _i, _p, _ip, _ip, _p]),
     "gbx_revert_big_matrix": (_i, [_i, _p, _p, _i, _p, _i, _i, _i, _p, _p, _p]),
     "gbx_plan_create": (_i, [_p, _p, _p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, _i, _i, _i,
                              ctypes.POINTER(_p)]),

@@ -254,9 +254,11 @@ static int big_matrix_order(int dims, const int* vgrid, const int* p_map, int nu
   return GBX_OK;
 }
 
+// loc (optional): the tile data of placement entry t sits at tile slot
+// loc[t] instead of t (create_big_matrix_nl's address_to_location).
 static int big_matrix_moves(int dims, const int* vgrid, const int* p_map, int num_tiles, const int* paddr,
                             int rpb, int cpb, int nrd, bool to_big, std::vector<MoveDesc>& moves, int* nrows_out,
-                            int* ncols_out) {
+                            int* ncols_out, const std::vector<int>* loc = nullptr) {
   if (dims < 1 || dims > kMaxDims || num_tiles < 0 || rpb < 0 || cpb < 0 || nrd < 0 || nrd > dims)
     return fail(GBX_EINVAL, "bad big-matrix arguments");
   GBX_TRY(check_perm(dims, p_map));
@@ -268,7 +270,7 @@ static int big_matrix_moves(int dims, const int* vgrid, const int* p_map, int nu
   for (int r = 0; r < nrows; ++r)
     for (int c = 0; c < ncols; ++c) {
       int t = order[(size_t)r * ncols + c];
-      int64_t tile_off = (int64_t)t * bs;
+      int64_t tile_off = (int64_t)(loc ? (*loc)[t] : t) * bs;
       int64_t big_off = (int64_t)r * rpb * total_col + (int64_t)c * cpb;
       int64_t ext[2] = {rpb, cpb};
       int64_t ts[2] = {cpb, 1}, bstr[2] = {total_col, 1};
@@ -362,6 +364,41 @@ int gbx_create_big_matrix(int dims, const int* vgrid, const int* p_map, int num_
   std::vector<MoveDesc> mv;
   GBX_TRY(big_matrix_moves(dims, vgrid, p_map, num_tiles, permuted_address, row_per_block, col_per_block,
                            num_row_dim, true, mv, nrows, ncols));
+  return run_moves_async(mv, d_tiles, d_big, (cudaStream_t)stream);
+}
+
+int gbx_create_big_matrix_nl(int dims, const int* vgrid, const int* p_map, int num_tiles, const double* d_tiles,
+                             int num_slots, const int* permuted_address, int row_per_block, int col_per_block,
+                             int num_row_dim,
+                             const int* loc_ranks, const int* loc_slots, int num_locations, double* d_big,
+                             int* nrows, int* ncols, void* stream) {
+  if (dims < 1 || dims > kMaxDims || num_tiles < 0 || num_locations < 0 || (num_locations && (!loc_ranks || !loc_slots)))
+    return fail(GBX_EINVAL, "bad big-matrix arguments");
+  GBX_TRY(check_perm(dims, p_map));
+  // address_to_location: rank of a tile's permuted address in the permuted
+  // grid -> its slot in d_tiles (every placed tile must have one; the
+  // reference asserts, transpose_helper.cc:250-251)
+  int grid_T[kMaxDims];
+  for (int d = 0; d < dims; ++d) grid_T[p_map[d]] = vgrid[d];
+  std::map<int64_t, int> where;
+  for (int i = 0; i < num_locations; ++i) where.emplace(loc_ranks[i], loc_slots[i]);
+  std::vector<int> loc(num_tiles);
+  for (int t = 0; t < num_tiles; ++t) {
+    const int* a = permuted_address + (int64_t)t * dims;
+    int64_t x = 1, r = 0;
+    for (int i = dims - 1; i >= 0; --i) {
+      r += (int64_t)a[i] * x;
+      x *= grid_T[i];
+    }
+    auto it = where.find(r);
+    if (it == where.end()) return fail(GBX_EINVAL, "tile %d (rank %lld) has no location", t, (long long)r);
+    if (it->second < 0 || it->second >= num_slots)
+      return fail(GBX_EINVAL, "location %d of tile %d outside [0, %d)", it->second, t, num_slots);
+    loc[t] = it->second;
+  }
+  std::vector<MoveDesc> mv;
+  GBX_TRY(big_matrix_moves(dims, vgrid, p_map, num_tiles, permuted_address, row_per_block, col_per_block,
+                           num_row_dim, true, mv, nrows, ncols, &loc));
   return run_moves_async(mv, d_tiles, d_big, (cudaStream_t)stream);
 }
 

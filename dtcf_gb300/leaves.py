@@ -77,6 +77,26 @@ def create_big_matrix(vgrid, p_map, tiles, permuted_address, row_per_block, col_
     return nr.value, nc.value
 
 
+def create_big_matrix_nl(vgrid, p_map, tiles, permuted_address, row_per_block, col_per_block, num_row_dim,
+                         address_to_location, big, stream=None):
+    """create_big_matrix_nl (transpose_helper.cc:184): the tile data of each
+    placed address comes from slot address_to_location[rank] of tiles (a dict
+    or (ranks, slots) pairs); returns (nrows, ncols) block counts."""
+    addr = np.asarray(permuted_address, dtype=np.int32)
+    g, gp = _iarr(vgrid)
+    pm, pmp = _iarr(p_map)
+    a, ap = _iarr(addr)
+    items = sorted(address_to_location.items()) if isinstance(address_to_location, dict) else address_to_location
+    kr, krp = _iarr([k for k, _ in items])
+    kv, kvp = _iarr([v for _, v in items])
+    bs = row_per_block * col_per_block
+    nr, nc = ctypes.c_int(), ctypes.c_int()
+    check(lib().gbx_create_big_matrix_nl(len(g), gp, pmp, addr.shape[0], _ptr(tiles), tiles.numel() // max(1, bs), ap,
+                                         row_per_block, col_per_block, num_row_dim, krp, kvp, len(kr), _ptr(big),
+                                         ctypes.byref(nr), ctypes.byref(nc), _stream(stream)))
+    return nr.value, nc.value
+
+
 def revert_big_matrix(vgrid, p_map, permuted_address, row_per_block, col_per_block, num_row_dim, big, tiles,
                       stream=None):
     """revert_big_matrix (transpose_helper.cc:331)."""

@@ -8,7 +8,6 @@ Contraction::contract (contraction.h:262) and runs the node-local work through
 the C ABI (gbx_plan_create / gbx_execute).
 """
 import ctypes
-import itertools
 
 import numpy as np
 import torch
@@ -24,18 +23,23 @@ class TensorDesc(ctypes.Structure):
                 ("vgrid", ctypes.c_void_p), ("num_tiles", ctypes.c_int), ("tile_address", ctypes.c_void_p)]
 
 
-def unique_blocks(sym, vgrid):
+def _stream(stream):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def unique_blocks(sym, vgrid, stream=None):
     """Block addresses RRR stores on one process (Tensor::generate_data /
-    isValid, tensor.cc:617-694): lexicographic, non-increasing within each
-    symmetry group ('a'/'A' group 0, 'b'/'B' group 1)."""
-    groups = [0 if c in "aA" else 1 if c in "bB" else -1 for c in sym]
-    out = []
-    for a in itertools.product(*[range(v) for v in vgrid]):
-        ok = all(not (groups[i] >= 0 and groups[i] == groups[j] and a[i] < a[j])
-                 for i in range(len(a)) for j in range(i + 1, len(a)))
-        if ok:
-            out.append(a)
-    return np.array(out, dtype=np.int32).reshape(-1, len(sym))
+    isValid, tensor.cc:617-694), generated on the device
+    (gbx_rrr_unique_tiles): (num_tiles, dims) int32 CUDA tensor."""
+    g = np.ascontiguousarray(vgrid, dtype=np.int32)
+    n = ctypes.c_int()
+    check(lib().gbx_rrr_unique_tiles(len(sym), sym.encode(), g.ctypes.data_as(ctypes.c_void_p), None, 0,
+                                     ctypes.byref(n), _stream(stream)))
+    out = torch.zeros((max(1, n.value), len(sym)), dtype=torch.int32, device="cuda")
+    check(lib().gbx_rrr_unique_tiles(len(sym), sym.encode(), g.ctypes.data_as(ctypes.c_void_p),
+                                     ctypes.c_void_p(out.data_ptr()), n.value, ctypes.byref(n), _stream(stream)))
+    return out[: n.value]
 
 
 class Tensor:
@@ -45,19 +49,23 @@ class Tensor:
         self.vgrid = list(vgrid)
         self.block_range = [s // v for s, v in zip(size, vgrid)]
         self.block_size = int(np.prod(self.block_range))
-        self.addrs = unique_blocks(sym, vgrid) if addrs is None else np.ascontiguousarray(addrs, dtype=np.int32)
+        if addrs is None:
+            self.d_addrs = unique_blocks(sym, vgrid)
+            self.addrs = self.d_addrs.cpu().numpy()
+        else:
+            self.addrs = np.ascontiguousarray(addrs, dtype=np.int32)
+            self.d_addrs = torch.from_numpy(self.addrs.copy()).to(device)
         self.num_tiles = self.addrs.shape[0]
         self.tiles = torch.zeros(self.num_tiles * self.block_size, dtype=torch.float64, device=device)
         self._keep = []
 
-    def initialize(self):
-        """Tensor::initialize (tensor.cc:315-335): each block holds the
-        constant sum_d sin(block_address_d) (tensor.cc:744-758)."""
-        v = np.zeros(self.num_tiles)
-        for d in range(len(self.sym) - 1, -1, -1):
-            v += np.sin(self.addrs[:, d].astype(np.float64))
-        vals = torch.from_numpy(np.repeat(v, self.block_size)).to(self.tiles.device)
-        self.tiles.copy_(vals)
+    def initialize(self, stream=None):
+        """Tensor::initialize (tensor.cc:315-335) on the device: each block
+        holds the constant sum_d sin(block_address_d) (tensor.cc:744-758)."""
+        g = np.ascontiguousarray(self.vgrid, dtype=np.int32)
+        check(lib().gbx_rrr_initialize(len(self.sym), g.ctypes.data_as(ctypes.c_void_p),
+                                       ctypes.c_void_p(self.d_addrs.data_ptr()), self.num_tiles, self.block_size,
+                                       ctypes.c_void_p(self.tiles.data_ptr()), _stream(stream)))
         return self
 
     def desc(self):

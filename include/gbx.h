@@ -109,6 +109,23 @@ GBX_API int gbx_create_big_matrix(int dims, const int* vgrid, const int* p_map, 
                           const int* permuted_address, int row_per_block, int col_per_block, int num_row_dim,
                           double* d_big, int* nrows, int* ncols, void* stream);
 
+/* The same placement with the tile data looked up by address: entry t of
+ * permuted_address takes its data from tile slot address_to_location[rank]
+ * of d_tiles (which holds num_slots tiles), rank = the block rank of the
+ * entry's permuted address in the permuted grid (grid[p_map[d]] = vgrid[d]).
+ * The map is passed as num_locations (loc_ranks[i] -> loc_slots[i]) pairs;
+ * a placed tile without a location, or a slot outside [0, num_slots), is
+ * GBX_EINVAL (the reference asserts).
+ * Replaces: create_big_matrix_nl(Tensor*&, double*&, int*&, int*&, int, int,
+ *           int, int, map<int,map<int,int>>*&, double*&, map<int,int>*&)
+ *           transpose_helper.h:35 (transpose_helper.cc:184-328), as called by
+ *           Contraction::contract, contraction.cc:2399-2410. */
+GBX_API int gbx_create_big_matrix_nl(int dims, const int* vgrid, const int* p_map, int num_tiles,
+                                     const double* d_tiles, int num_slots, const int* permuted_address,
+                                     int row_per_block, int col_per_block, int num_row_dim, const int* loc_ranks,
+                                     const int* loc_slots, int num_locations, double* d_big, int* nrows, int* ncols,
+                                     void* stream);
+
 /* The inverse placement.
  * Replaces: revert_big_matrix(...)  transpose_helper.h:43 (transpose_helper.cc:331-409). */
 GBX_API int gbx_revert_big_matrix(int dims, const int* vgrid, const int* p_map, int num_tiles,
@@ -131,6 +148,27 @@ typedef struct {
     int num_tiles;
     const int* tile_address;
 } gbx_tensor_desc;
+
+/* RRR tensor initialization on one process, on the device.
+ *
+ * The unique tiles of a tensor with this symmetry string ('a'/'A' and
+ * 'b'/'B' mark the two symmetry groups, any other letter a free index) and
+ * block grid, in the order RRR generates them: lexicographic, kept when the
+ * coordinates do not increase inside a group.  d_tile_address (device, dims
+ * ints per tile, room for capacity tiles) receives them; *num_tiles their
+ * count (the call waits for the stream).  capacity 0 counts only;
+ * GBX_EINVAL when more tiles exist than capacity.
+ * Replaces: the addresses of Tensor::initialize (tensor.cc:315-335) --
+ *           generate_data / isValid / get_bound, tensor.cc:617-694. */
+GBX_API int gbx_rrr_unique_tiles(int dims, const char* sym, const int* vgrid, int* d_tile_address, int capacity,
+                                 int* num_tiles, void* stream);
+/* Every element of tile t (block_size elements at d_tiles + t * block_size)
+ * set to the reference's value of its address, sum over d from dims - 1 down
+ * to 0 of sin(address_d), bit for bit.  d_tile_address on the device.
+ * Replaces: the values of Tensor::initialize / generate_data
+ *           (tensor.cc:674-681) and Tensor::get_value (tensor.cc:744-758). */
+GBX_API int gbx_rrr_initialize(int dims, const int* vgrid, const int* d_tile_address, int num_tiles,
+                               int64_t block_size, double* d_tiles, void* stream);
 
 typedef struct gbx_plan gbx_plan;
 

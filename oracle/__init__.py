@@ -171,6 +171,27 @@ def create_big_matrix(vgrid, p_map, tiles, permuted_address, row_per_block, col_
     return big.reshape(nr.value * row_per_block, nc.value * col_per_block)
 
 
+def create_big_matrix_nl(vgrid, p_map, tiles, permuted_address, row_per_block, col_per_block, num_row_dim,
+                         address_to_location):
+    """create_big_matrix_nl (transpose_helper.cc:184).  tiles: (slots, block_size);
+    address_to_location: {rank in the permuted grid: slot}."""
+    tiles = np.ascontiguousarray(tiles, dtype=np.float64)
+    addr = _ip(permuted_address)
+    n = addr.shape[0]
+    items = sorted(address_to_location.items())
+    kr, kv = _ip([k for k, _ in items]), _ip([v for _, v in items])
+    big = np.zeros(n * tiles.shape[1], dtype=np.float64)
+    nr, nc = _i(), _i()
+    r = lib().orc_create_big_matrix_nl(_i(addr.shape[1]), _ptr(_ip(vgrid)), _ptr(_ip(p_map)), _i(n), _ptr(tiles),
+                                       _ptr(addr), _i(row_per_block), _i(col_per_block), _i(num_row_dim), _ptr(kr),
+                                       _ptr(kv), _i(len(items)), _ptr(big), ctypes.byref(nr), ctypes.byref(nc))
+    if r == -2:
+        raise KeyError("a placed tile has no location")
+    if r < 0:
+        raise ValueError("tile pattern is not rectangular")
+    return big.reshape(nr.value * row_per_block, nc.value * col_per_block)
+
+
 def revert_big_matrix(vgrid, p_map, permuted_address, row_per_block, col_per_block, num_row_dim, big):
     addr = _ip(permuted_address)
     n = addr.shape[0]

@@ -219,6 +219,45 @@ long orc_create_big_matrix(int dims, const int* vgrid, const int* p_map, int num
     return n;
 }
 
+/* create_big_matrix_nl, transpose_helper.cc:184-328: the placement of
+ * create_big_matrix, with the data of entry i taken from tile slot
+ * location(rank_i) of tiles, rank_i the block rank of permuted_address[i] in
+ * the permuted grid (transpose_helper.cc:237-255); the address_to_location map
+ * comes as nloc (ranks[k] -> slots[k]) pairs.  Returns -2 when a placed
+ * tile has no location. */
+long orc_create_big_matrix_nl(int dims, const int* vgrid, const int* p_map, int num_tiles,
+                              const double* tiles, const int* permuted_address,
+                              int row_per_block, int col_per_block, int num_row_dim,
+                              const int* ranks, const int* slots, int nloc,
+                              double* big, int* nrows_out, int* ncols_out) {
+    int grid_T[ORC_MAXD];
+    for (int d = 0; d < dims; ++d) grid_T[p_map[d]] = vgrid[d];
+    int* loc = (int*)malloc(sizeof(int) * (size_t)(num_tiles > 0 ? num_tiles : 1));
+    for (int i = 0; i < num_tiles; ++i) {
+        long r = orc_block_rank(permuted_address + (long)i * dims, dims, grid_T);
+        int k = 0;
+        while (k < nloc && ranks[k] != r) ++k;
+        if (k == nloc) { free(loc); return -2; }
+        loc[i] = slots[k];
+    }
+    int* order = (int*)malloc(sizeof(int) * (size_t)(num_tiles > 0 ? num_tiles : 1));
+    long n = orc_big_matrix_order(dims, vgrid, p_map, num_tiles, permuted_address, num_row_dim,
+                                  order, nrows_out, ncols_out);
+    if (n < 0) { free(order); free(loc); return n; }
+    long bs = (long)row_per_block * col_per_block;
+    long total_col = (long)(*ncols_out) * col_per_block;
+    for (int r = 0; r < *nrows_out; ++r)
+        for (int c = 0; c < *ncols_out; ++c) {
+            const double* t = tiles + (long)loc[order[r * (*ncols_out) + c]] * bs;
+            for (int i = 0; i < row_per_block; ++i)
+                memcpy(big + ((long)r * row_per_block + i) * total_col + (long)c * col_per_block,
+                       t + (long)i * col_per_block, sizeof(double) * (size_t)col_per_block);
+        }
+    free(order);
+    free(loc);
+    return n;
+}
+
 /* revert_big_matrix, transpose_helper.cc:331-409: the inverse placement. */
 long orc_revert_big_matrix(int dims, const int* vgrid, const int* p_map, int num_tiles,
                            const int* permuted_address, int row_per_block, int col_per_block,

@@ -3,6 +3,7 @@
  * grid.cc, DLTC/transp-kernel-omp.cc).  Loaded by tests/ to pin the oracle's
  * restatement to the reference itself.  Test infrastructure only. */
 #include <cstring>
+#include <map>
 #include <string>
 #include "tensor.h"
 #include "transpose_helper.h"
@@ -88,6 +89,23 @@ long ref_create_big_matrix(const char* sym, int* sizes, int* vgrid, double* tile
   std::memcpy(big_out, big, sizeof(double) * (size_t)num_tiles * t->get_block_size());
   delete[] big;
   delete bm;
+  return num_tiles;
+}
+
+long ref_create_big_matrix_nl(const char* sym, int* sizes, int* vgrid, double* tiles, int* perm_addr, int* p_map,
+                              int num_tiles, int row_per_block, int col_per_block, int num_row_dim, int* loc_ranks,
+                              int* loc_slots, int nloc, double* big_out) {
+  RRR::Tensor* t = make_tensor(sym, sizes, vgrid);
+  std::map<int, std::map<int, int> >* bm = nullptr;
+  double* big = nullptr;
+  std::map<int, int>* where = new std::map<int, int>();
+  for (int i = 0; i < nloc; ++i) (*where)[loc_ranks[i]] = loc_slots[i];
+  RRR::create_big_matrix_nl(t, tiles, perm_addr, p_map, num_tiles, row_per_block, col_per_block, num_row_dim, bm,
+                            big, where);
+  std::memcpy(big_out, big, sizeof(double) * (size_t)num_tiles * t->get_block_size());
+  delete[] big;
+  delete bm;
+  delete where;
   return num_tiles;
 }
 

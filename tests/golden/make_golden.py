@@ -188,6 +188,55 @@ def main():
         out[pre + "C_out"] = C
     out["lc_count"] = np.array(len(lcases))
 
+    # 7. create_big_matrix_nl (transpose_helper.cc:184-328): the addresses in
+    #    a shuffled order, the tile data in a second, independent order of
+    #    slots (plus unused slots), the address_to_location map from each
+    #    address's rank in the permuted grid to its slot -- as
+    #    Contraction::contract builds it (contraction.cc:2399-2410).  Own
+    #    generator, so the fixtures above stay as they were.
+    rng7 = np.random.default_rng(20261204)
+    ncases = [("cccc", (12, 8, 12, 8), (3, 2, 3, 2), (2, 0, 3, 1), 2),
+              ("cccc", (6, 8, 10, 4), (3, 2, 5, 2), (1, 3, 0, 2), 1),
+              ("ccc", (6, 8, 10), (3, 2, 5), (2, 0, 1), 2)]
+    for n_i, (sym, sizes, vgrid, p_map, nrd) in enumerate(ncases):
+        dims = len(sym)
+        br = [s // v for s, v in zip(sizes, vgrid)]
+        bs = int(np.prod(br))
+        addrs = np.array(list(itertools.product(*[range(v) for v in vgrid])), np.int32)
+        addrs = addrs[rng7.permutation(len(addrs))]
+        perm_addr = np.zeros_like(addrs)
+        for d in range(dims):
+            perm_addr[:, p_map[d]] = addrs[:, d]
+        grid_T = [0] * dims
+        for d in range(dims):
+            grid_T[p_map[d]] = vgrid[d]
+        ranks = [int(ref.ref_block_rank(ptr(i32(a)), ctypes.c_int(dims), ptr(i32(grid_T)))) for a in perm_addr]
+        nslots = len(addrs) + 3
+        slots = rng7.permutation(nslots)[: len(addrs)]
+        tiles = rng7.standard_normal((nslots, bs))
+        pbr = [0] * dims
+        for d in range(dims):
+            pbr[p_map[d]] = br[d]
+        rpb = int(np.prod(pbr[:nrd]))
+        cpb = int(np.prod(pbr[nrd:]))
+        big = np.zeros(len(addrs) * bs)
+        ref.ref_create_big_matrix_nl(sym.encode(), ptr(i32(sizes)), ptr(i32(vgrid)), ptr(tiles), ptr(i32(perm_addr)),
+                                     ptr(i32(p_map)), ctypes.c_int(len(addrs)), ctypes.c_int(rpb), ctypes.c_int(cpb),
+                                     ctypes.c_int(nrd), ptr(i32(ranks)), ptr(i32(slots)), ctypes.c_int(len(addrs)),
+                                     ptr(big))
+        pre = f"nl{n_i}_"
+        out[pre + "vgrid"] = np.array(vgrid, np.int32)
+        out[pre + "p_map"] = np.array(p_map, np.int32)
+        out[pre + "perm_addr"] = perm_addr
+        out[pre + "ranks"] = np.array(ranks, np.int32)
+        out[pre + "slots"] = np.array(slots, np.int32)
+        out[pre + "tiles"] = tiles
+        out[pre + "rpb"] = np.array(rpb)
+        out[pre + "cpb"] = np.array(cpb)
+        out[pre + "nrd"] = np.array(nrd)
+        out[pre + "big"] = big
+    out["nl_count"] = np.array(len(ncases))
+
     path = os.path.join(ROOT, "tests", "golden", "ref_leaves.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, os.path.getsize(path), "bytes,", len(out), "arrays")

@@ -70,6 +70,27 @@ def test_big_matrix_bit_exact_vs_reference(gbx, golden):
         assert np.array_equal(host(back).reshape(golden[pre + "back"].shape), golden[pre + "back"])
 
 
+def test_big_matrix_nl_bit_exact_vs_reference(gbx, golden):
+    """create_big_matrix_nl: tile data in slots of a shuffled order (plus
+    unused slots), found through address_to_location, as the compiled
+    reference places them; a missing location is GBX_EINVAL."""
+    for b in range(int(golden["nl_count"])):
+        pre = f"nl{b}_"
+        tiles = dev(golden[pre + "tiles"])
+        big = torch.full((golden[pre + "big"].size,), np.nan, dtype=torch.float64, device="cuda")
+        loc = dict(zip(golden[pre + "ranks"].tolist(), golden[pre + "slots"].tolist()))
+        gbx.create_big_matrix_nl(golden[pre + "vgrid"], golden[pre + "p_map"], tiles, golden[pre + "perm_addr"],
+                                 int(golden[pre + "rpb"]), int(golden[pre + "cpb"]), int(golden[pre + "nrd"]), loc, big)
+        assert np.array_equal(host(big), golden[pre + "big"])
+    pre = "nl0_"
+    loc = dict(zip(golden[pre + "ranks"].tolist()[1:], golden[pre + "slots"].tolist()[1:]))
+    with pytest.raises(Exception):
+        gbx.create_big_matrix_nl(golden[pre + "vgrid"], golden[pre + "p_map"], dev(golden[pre + "tiles"]),
+                                 golden[pre + "perm_addr"], int(golden[pre + "rpb"]), int(golden[pre + "cpb"]),
+                                 int(golden[pre + "nrd"]), loc, torch.zeros(golden[pre + "big"].size,
+                                                                           dtype=torch.float64, device="cuda"))
+
+
 def test_big_matrix_rejects_ragged(gbx):
     tiles = dev(np.zeros(3 * 4))
     big = torch.zeros_like(tiles)
@@ -134,6 +155,34 @@ def test_transpose_blocks_symmetric_unflip(gbx):
     got = host(out).reshape(blocks.shape)
     for i in range(len(addrs)):
         assert np.array_equal(got[i], oracle.transpose(blocks[i].reshape(w), perms[i]).reshape(-1))
+
+
+def test_rrr_initialize_on_device_bit_exact_vs_reference(gbx, golden):
+    """Tensor::initialize on one process (tensor.cc:315-335) on the device:
+    the unique tile addresses in generation order and the block values,
+    bit for bit as the compiled reference made them; counting only, and a
+    too-small capacity, are checked too."""
+    from dtcf_gb300.rrr import Tensor, unique_blocks
+    for t in range(int(golden["tt_count"])):
+        sym = bytes(golden[f"tt{t}_sym"]).decode()
+        sizes, vgrid = golden[f"tt{t}_sizes"], golden[f"tt{t}_vgrid"]
+        addr = unique_blocks(sym, vgrid)
+        assert np.array_equal(addr.cpu().numpy(), golden[f"tt{t}_addr"]), sym
+        T = Tensor(sym, sizes, vgrid).initialize()
+        torch.cuda.synchronize()
+        assert np.array_equal(T.addrs, golden[f"tt{t}_addr"])
+        assert np.array_equal(host(T.tiles).reshape(golden[f"tt{t}_tiles"].shape), golden[f"tt{t}_tiles"]), sym
+    import ctypes
+    g = np.array([5, 5], dtype=np.int32)
+    n = ctypes.c_int()
+    lib = gbx.lib()
+    assert lib.gbx_rrr_unique_tiles(2, b"aa", g.ctypes.data_as(ctypes.c_void_p), None, 0, ctypes.byref(n), None) == 0
+    assert n.value == 15
+    small = torch.zeros(4 * 2, dtype=torch.int32, device="cuda")
+    rc = lib.gbx_rrr_unique_tiles(2, b"aa", g.ctypes.data_as(ctypes.c_void_p), ctypes.c_void_p(small.data_ptr()), 4,
+                                  ctypes.byref(n), None)
+    assert rc != 0 and n.value == 15
+    assert np.array_equal(small.cpu().numpy().reshape(4, 2), [[0, 0], [1, 0], [1, 1], [2, 0]])
 
 
 def _rrr_case(sym_a, sym_b, sym_c, sizes, vgrids, seed):

@@ -62,6 +62,25 @@ def test_big_matrix_matches_reference_fixtures(golden):
         assert np.array_equal(rt, golden[pre + "tiles"])
 
 
+
+def test_big_matrix_nl_matches_reference_fixtures(golden):
+    """create_big_matrix_nl (transpose_helper.cc:184-328): tile data looked
+    up through address_to_location, against the compiled reference."""
+    for b in range(int(golden["nl_count"])):
+        pre = f"nl{b}_"
+        loc = dict(zip(golden[pre + "ranks"].tolist(), golden[pre + "slots"].tolist()))
+        big = oracle.create_big_matrix_nl(golden[pre + "vgrid"], golden[pre + "p_map"], golden[pre + "tiles"],
+                                          golden[pre + "perm_addr"], int(golden[pre + "rpb"]), int(golden[pre + "cpb"]),
+                                          int(golden[pre + "nrd"]), loc)
+        assert np.array_equal(big.reshape(-1), golden[pre + "big"])
+    # a placed address without a location is an error, as the reference asserts
+    pre = "nl0_"
+    loc = dict(zip(golden[pre + "ranks"].tolist()[1:], golden[pre + "slots"].tolist()[1:]))
+    with pytest.raises(KeyError):
+        oracle.create_big_matrix_nl(golden[pre + "vgrid"], golden[pre + "p_map"], golden[pre + "tiles"],
+                                    golden[pre + "perm_addr"], int(golden[pre + "rpb"]), int(golden[pre + "cpb"]),
+                                    int(golden[pre + "nrd"]), loc)
+
 def test_local_contraction_matches_reference_fixtures(golden):
     for c in range(int(golden["lc_count"])):
         pre = f"lc{c}_"
