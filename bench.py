@@ -46,7 +46,7 @@ def parse():
                         "iterations of the default workload, inside the 1e-10 Eh bound; 6: ~1e-16)")
     p.add_argument("--autotune", type=int, default=1,
                    help="1: the split job times each contraction's output tile widths when it is built")
-    p.add_argument("--graph", type=int, default=1, choices=[1, 2],
+    p.add_argument("--graph", type=int, default=2, choices=[1, 2],
                    help="iteration of the headline number -- 1: one CUDA graph of the iteration's kernels; "
                         "2: the persistent program (a few persistent launches off a device-side work queue, "
                         "captured as the graph); the other mode is timed beside it")
@@ -544,6 +544,14 @@ def main():
     iters = 1000.0 / P["ms"]
     value = sum_over_ranks(iters)
 
+    # one more replayed iteration of the headline job (untimed) inside the
+    # NVTX range "graph_iteration", so that a profiler can capture exactly
+    # the launches of one iteration as the timed loop runs them
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("graph_iteration")
+    P["job"].enqueue(1, stream)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     # dominant kernel: per-step breakdown of one iteration (CUDA events on the launching stream)
     # one eager iteration, step by step, inside an NVTX range so that a
     # profiler can be pointed at exactly these launches (--nvtx-include iteration/)

@@ -597,6 +597,57 @@ __device__ __forceinline__ void digits_body(const SplitRowSet* __restrict__ sets
   }
 }
 
+// Rows of medium length (kShortRow < K <= kMidRow): one CTA per row takes
+// the row's largest exponent (block reduction, written to exps directly)
+// and then writes the digits, every thread re-reading the elements it read
+// for the maximum -- from L1 or L2 instead of HBM, so the row crosses HBM
+// once.  The row sets here carry first_row in rows.
+constexpr int64_t kMidRow = 16384;
+
+template <bool kCoh>
+__device__ __forceinline__ void split_rows_body(const SplitRowSet* __restrict__ sets, int nsets, int64_t total_rows,
+                                                int S, uint32_t bid, uint32_t nblk, uint32_t* red) {
+  const int F = 7 + 8 * (S - 1);
+  for (int64_t rg = bid; rg < total_rows; rg += nblk) {
+    int lo = 0, hi = nsets - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (sets[mid].first_row <= rg) lo = mid; else hi = mid - 1;
+    }
+    const SplitRowSet& rs = sets[lo];
+    const int64_t row = rg - rs.first_row;
+    const double* src = rs.src + row * rs.ld;
+    const int64_t K = rs.K;
+    uint32_t emax = 0;
+    for (int64_t k = threadIdx.x; k < K; k += 4 * 256) {
+      long long v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) v[u] = k + u * 256 < K ? __double_as_longlong(ldin<kCoh>(src + k + u * 256)) : 0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) emax = max(emax, (uint32_t)((v[u] >> 52) & 0x7FF));
+    }
+    for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+    __syncthreads();  // the previous row is done with red
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = emax;
+    __syncthreads();
+    uint32_t m = 0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) m = max(m, red[w]);
+    if (threadIdx.x == 0) rs.exps[row] = (int)m;
+    __nv_bfloat16* dst = rs.dst + row * rs.Kp;
+    for (int64_t k = threadIdx.x; k < K; k += 4 * 256) {
+      long long v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) v[u] = k + u * 256 < K ? __double_as_longlong(ldin<kCoh>(src + k + u * 256)) : 0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (k + u * 256 < K) write_digits(v[u], m, F, S, dst + k + u * 256, rs.slice_stride);
+    }
+    for (int64_t k = K + threadIdx.x; k < rs.Kp; k += 256)
+      for (int s = 0; s < S; ++s) dst[s * rs.slice_stride + k] = __int2bfloat16_rn(0);
+  }
+}
+
 // Short rows: one warp handles a whole row (exponent by warp shuffles, then
 // the digits); the row sets here carry first_row in rows.
 template <bool kCoh>

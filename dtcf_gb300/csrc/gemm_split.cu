@@ -55,6 +55,7 @@ constexpr int kFoldChunks = 127;   // int32 drain sums fold into FP64 before ove
 constexpr long long kWaitCycles = 2000000000ll;  // ~1 s at 2 GHz
 constexpr int kSplitFill = 152 * 2;  // work items that keep every SM busy
 
+using dev::kMidRow;
 using dev::kShortRow;
 using dev::kSplitChunk;
 
@@ -940,6 +941,12 @@ __global__ void __launch_bounds__(256) digits_kernel(const SplitRowSet* __restri
   dev::digits_body<false>(sets, nsets, total_chunks, S, blockIdx.x, gridDim.x);
 }
 
+__global__ void __launch_bounds__(256) split_rows_kernel(const SplitRowSet* __restrict__ sets, int nsets,
+                                                         int64_t total_rows, int S) {
+  __shared__ uint32_t red[8];
+  dev::split_rows_body<false>(sets, nsets, total_rows, S, blockIdx.x, gridDim.x, red);
+}
+
 __global__ void __launch_bounds__(256) split_short_rows_kernel(const SplitRowSet* __restrict__ sets, int nsets,
                                                                int64_t total_rows, int S) {
   dev::short_rows_body<false>(sets, nsets, total_rows, S, blockIdx.x, gridDim.x);
@@ -1028,8 +1035,10 @@ struct SplitPlan {
   SplitRowSet* d_sets_b = nullptr;  // long rows from the plan's packed B
   SplitRowSet* d_short_a = nullptr;  // short rows (first_row counts rows)
   SplitRowSet* d_short_b = nullptr;
-  int nlong_a = 0, nlong_b = 0, nshort_a = 0, nshort_b = 0;
-  int64_t short_rows_a = 0, short_rows_b = 0;
+  SplitRowSet* d_mid_a = nullptr;  // medium rows, one CTA per row (first_row counts rows)
+  SplitRowSet* d_mid_b = nullptr;
+  int nlong_a = 0, nlong_b = 0, nshort_a = 0, nshort_b = 0, nmid_a = 0, nmid_b = 0;
+  int64_t short_rows_a = 0, short_rows_b = 0, mid_rows_a = 0, mid_rows_b = 0;
   int nsets = 0;
   int64_t rows_a = 0, rows_b = 0;  // (row, K chunk) work items per side
   std::vector<std::pair<void*, size_t>> exp_ranges_a, exp_ranges_b;  // exponent words reset before a split
@@ -1050,6 +1059,8 @@ struct SplitPlan {
     dev_free(d_sets_b);
     dev_free(d_short_a);
     dev_free(d_short_b);
+    dev_free(d_mid_a);
+    dev_free(d_mid_b);
     dev_free(d_all);
     for (auto& l : launches) {
       dev_free(l.d_probs);
@@ -1210,8 +1221,8 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
   auto exp_ptr = [&](int r, int64_t off) { return (int*)(base[r] + lay.exps_at(r)) + off; };
   double* part_base = b1 ? (double*)(base[1] + lay.part_at()) : nullptr;
   sp->bytes = (double)b0 + (double)b1;
-  std::vector<SplitRowSet> sa, sb, ssa, ssb;
-  int64_t sra = 0, srb = 0;
+  std::vector<SplitRowSet> sa, sb, ssa, ssb, msa, msb;
+  int64_t sra = 0, srb = 0, mra = 0, mrb = 0;
   std::vector<DevProblem> dp;
   std::vector<CUtensorMap> maps;
   int64_t ra = 0, rb = 0;
@@ -1234,6 +1245,10 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
       to_a.first_row = sra;
       sra += to_a.rows;
       ssa.push_back(to_a);
+    } else if (to_a.K <= kMidRow) {
+      to_a.first_row = mra;
+      mra += to_a.rows;
+      msa.push_back(to_a);
     } else {
       to_a.first_row = ra;
       ra += to_a.rows * ((to_a.K + kSplitChunk - 1) / kSplitChunk);
@@ -1244,6 +1259,10 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
       to_b.first_row = srb;
       srb += to_b.rows;
       ssb.push_back(to_b);
+    } else if (to_b.K <= kMidRow) {
+      to_b.first_row = mrb;
+      mrb += to_b.rows;
+      msb.push_back(to_b);
     } else {
       to_b.first_row = rb;
       rb += to_b.rows * ((to_b.K + kSplitChunk - 1) / kSplitChunk);
@@ -1296,6 +1315,10 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
   sp->nlong_b = (int)sb.size();
   sp->nshort_a = (int)ssa.size();
   sp->nshort_b = (int)ssb.size();
+  sp->mid_rows_a = mra;
+  sp->mid_rows_b = mrb;
+  sp->nmid_a = (int)msa.size();
+  sp->nmid_b = (int)msb.size();
   auto up = [&](const void* h, size_t bytes, void** d) -> int {
     if (bytes == 0) return GBX_OK;
     GBX_TRY(dev_alloc(d, bytes));
@@ -1306,6 +1329,8 @@ int create_split_plan(const std::vector<SplitProblem>& probs, int slices, SplitP
   GBX_TRY(up(sb.data(), sizeof(SplitRowSet) * sb.size(), (void**)&sp->d_sets_b));
   GBX_TRY(up(ssa.data(), sizeof(SplitRowSet) * ssa.size(), (void**)&sp->d_short_a));
   GBX_TRY(up(ssb.data(), sizeof(SplitRowSet) * ssb.size(), (void**)&sp->d_short_b));
+  GBX_TRY(up(msa.data(), sizeof(SplitRowSet) * msa.size(), (void**)&sp->d_mid_a));
+  GBX_TRY(up(msb.data(), sizeof(SplitRowSet) * msb.size(), (void**)&sp->d_mid_b));
   GBX_TRY(up(dp.data(), sizeof(DevProblem) * dp.size(), (void**)&sp->d_all));
   // one launch per output tile width, plus one for the thin-K problems of
   // each k-block (bn 0: 64, bn 1: 32)
@@ -1375,6 +1400,20 @@ int split_operands(SplitPlan* sp, bool plan_a, bool plan_b, cudaStream_t st) {
         row_exponent_kernel<<<grid, 256, 0, st>>>(sets, nsets, chunks);
         GBX_CUDA(cudaGetLastError());
         digits_kernel<<<grid, 256, 0, st>>>(sets, nsets, chunks, sp->S);
+        GBX_CUDA(cudaGetLastError());
+      }
+    }
+    const int64_t mrows = side == 0 ? sp->mid_rows_a : sp->mid_rows_b;
+    if (mrows > 0) {
+      const SplitRowSet* sets = side == 0 ? sp->d_mid_a : sp->d_mid_b;
+      const int nsets = side == 0 ? sp->nmid_a : sp->nmid_b;
+      const int grid = (int)std::min<int64_t>(mrows, 152 * 8);
+      if (rec) {
+        ProgArgs a;
+        a.sets = {sets, mrows, nsets, sp->S};
+        GBX_TRY(prog_mem(rec, PK_SPLITROWS, (uint32_t)grid, a, {}));
+      } else {
+        split_rows_kernel<<<grid, 256, 0, st>>>(sets, nsets, mrows, sp->S);
         GBX_CUDA(cudaGetLastError());
       }
     }

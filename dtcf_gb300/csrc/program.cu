@@ -106,6 +106,9 @@ __device__ __forceinline__ void run_record(const ProgRec& r, uint32_t vb, ProgSm
     case PK_SHORTROWS:
       dev::short_rows_body<true>(a.sets.sets, a.sets.nsets, a.sets.total, a.sets.S, vb, g);
       break;
+    case PK_SPLITROWS:
+      dev::split_rows_body<true>(a.sets.sets, a.sets.nsets, a.sets.total, a.sets.S, vb, g, sm.red8);
+      break;
     case PK_SPLITRED:
       dev::split_reduce_body<true>(a.splitred.probs, a.splitred.red_prob, a.splitred.red_first, a.splitred.nred,
                                    a.splitred.total, vb, g);

@@ -58,6 +58,7 @@ enum ProgKind : int32_t {
   PK_ROWEXP,
   PK_DIGITS,
   PK_SHORTROWS,
+  PK_SPLITROWS,
   PK_SPLITRED,
   PK_GEMV,
   PK_SMALLOUT,
