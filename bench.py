@@ -200,7 +200,9 @@ def cpu_arm(a, steps, warmup, one_core=False):
     import numpy as np
     from oracle import cc as occ, cc_cpu
     sysm = occ.System(a.nocc, a.nvir, nirrep=a.nirrep, max_block=a.max_block, min_block=a.min_block, seed=a.seed)
-    shapes = cc_cpu.gemm_shapes(sysm, "ccsd")
+    # every contracted block tuple, as the reference computes them (the
+    # GPU path runs the antisymmetric contracted pairs over x >= y only)
+    shapes = cc_cpu.gemm_shapes(sysm, "ccsd", pairs=False)
     fl = cc_cpu.flops(shapes)
     cores = os.cpu_count()
     L = cc_cpu.IterationLeaves(shapes, threads=cores)

@@ -191,16 +191,26 @@ struct gbx_cc_job {
     return true;
   }
 
+  // pair: two contracted labels in which A and B are both antisymmetric
+  // (the packed GEMMs then run over block pairs x >= y, the off-diagonal ones
+  // weighted 2 in the pack of the constant operand, or of the smaller one)
   int contract(const char* c, const char* lc, const char* a, const char* la, const char* b, const char* lb,
-               double alpha) {
+               double alpha, const char* pair = nullptr) {
     CCTensor *C = get(c), *A = get(a), *B = get(b);
     GBX_TRY(check_labels(C, lc, c));
     GBX_TRY(check_labels(A, la, a));
     GBX_TRY(check_labels(B, lb, b));
     std::unique_ptr<ContractionPlan> p;
     Engine e = cfg.engine == GBX_MODE_SPLIT ? Engine::Split : Engine::F64;
+    ContractionPair cp;
+    if (pair) {
+      cp.x = std::string(1, pair[0]);
+      cp.y = std::string(1, pair[1]);
+      const bool a_int = is_integral(a), b_int = is_integral(b);
+      cp.scale_b = b_int != a_int ? b_int : B->L.nelem <= A->L.nelem;
+    }
     GBX_TRY(plan_contraction(A->L, B->L, C->L, labels(la), labels(lb), labels(lc), e, cfg.slices, p,
-                             cfg.split_all != 0, /*defer=*/true));
+                             cfg.split_all != 0, /*defer=*/true, pair ? &cp : nullptr));
     // integrals never change: packed and split once, when the job is built
     // (a direct plan reads them where they are stored, so they stay resident)
     p->a_static = is_integral(a) && !p->direct;
@@ -445,10 +455,11 @@ int gbx_cc_job::plan_all() {
   // F_ae, F_mi, F_me
   GBX_TRY(zero("Fae"));
   if (sd) GBX_TRY(contract("Fae", "ae", "t1", "mf", "OVVV", "mafe", 1.0));
-  GBX_TRY(contract("Fae", "ae", TAUT, "mnaf", "OOVV", "mnef", -0.5));
+  // (taut, tau and t2 are antisymmetric in i <-> j and in a <-> b, like <pq||rs>)
+  GBX_TRY(contract("Fae", "ae", TAUT, "mnaf", "OOVV", "mnef", -0.5, "mn"));
   GBX_TRY(zero("Fmi"));
   if (sd) GBX_TRY(contract("Fmi", "mi", "t1", "ne", "OOOV", "mnie", 1.0));
-  GBX_TRY(contract("Fmi", "mi", TAUT, "inef", "OOVV", "mnef", 0.5));
+  GBX_TRY(contract("Fmi", "mi", TAUT, "inef", "OOVV", "mnef", 0.5, "ef"));
   if (sd) {
     GBX_TRY(zero("Fme"));
     GBX_TRY(contract("Fme", "me", "t1", "nf", "OOVV", "mnef", 1.0));
@@ -461,7 +472,7 @@ int gbx_cc_job::plan_all() {
   } else {
     GBX_TRY(fused("Wmnij", "mnij", {{"OOOO", "mnij", 1.0}}));
   }
-  GBX_TRY(contract("Wmnij", "mnij", TAU, "ijef", "OOVV", "mnef", 0.5));
+  GBX_TRY(contract("Wmnij", "mnij", TAU, "ijef", "OOVV", "mnef", 0.5, "ef"));
   // W_mbej
   GBX_TRY(fused("Wmbej", "mbej", {{"OVVO", "mbej", 1.0}}));
   if (sd) {
@@ -478,8 +489,8 @@ int gbx_cc_job::plan_all() {
     GBX_TRY(contract("R1", "ia", "t1", "ma", "Fmi", "mi", -1.0));
     GBX_TRY(contract("R1", "ia", "t2", "imae", "Fme", "me", 1.0));
     GBX_TRY(contract("R1", "ia", "t1", "nf", "OVOV", "naif", -1.0));
-    GBX_TRY(contract("R1", "ia", "t2", "imef", "OVVV", "maef", -0.5));
-    GBX_TRY(contract("R1", "ia", "t2", "mnae", "OOVO", "nmei", -0.5));
+    GBX_TRY(contract("R1", "ia", "t2", "imef", "OVVV", "maef", -0.5, "ef"));
+    GBX_TRY(contract("R1", "ia", "t2", "mnae", "OOVO", "nmei", -0.5, "mn"));
   }
   // T2 residual
   const char* FBE = "Fae";
@@ -504,12 +515,12 @@ int gbx_cc_job::plan_all() {
   // 1/2 tau_mn^ab W_mnij + 1/2 tau_ij^ef <ab||ef> (the ladder, integrals as
   // the static A operand), on canonical tiles, then into R2
   GBX_TRY(zero("Lad"));
-  GBX_TRY(contract("Lad", "ijab", TAU, "mnab", "Wmnij", "mnij", 0.5));
-  GBX_TRY(contract("Lad", "ijab", "VVVV", "abef", TAU, "ijef", 0.5));
+  GBX_TRY(contract("Lad", "ijab", TAU, "mnab", "Wmnij", "mnij", 0.5, "mn"));
+  GBX_TRY(contract("Lad", "ijab", "VVVV", "abef", TAU, "ijef", 0.5, "ef"));
   if (sd) {
     // -1/2 P(ab) t_m^b sum_ef tau_ij^ef <am||ef> = +1/2 P(ab) sum_m t_m^b Z'_ijma
     GBX_TRY(zero("Zp"));
-    GBX_TRY(contract("Zp", "ijma", TAU, "ijef", "OVVV", "maef", 1.0));
+    GBX_TRY(contract("Zp", "ijma", TAU, "ijef", "OVVV", "maef", 1.0, "ef"));
     GBX_TRY(contract("Xb", "ijab", "Zp", "ijma", "t1", "mb", 0.5));
   }
   // P(ij)P(ab) (t_im^ae W_mbej - t_i^e t_m^a <mb||ej>)

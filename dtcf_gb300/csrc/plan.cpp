@@ -290,7 +290,8 @@ ContractionPlan::~ContractionPlan() {
 int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorLayout& C,
                      const std::vector<std::string>& la, const std::vector<std::string>& lb,
                      const std::vector<std::string>& lc, Engine e, int nslices,
-                     std::unique_ptr<ContractionPlan>& out, bool split_all, bool defer) {
+                     std::unique_ptr<ContractionPlan>& out, bool split_all, bool defer,
+                     const ContractionPair* pair) {
   if ((int)la.size() != A.rank || (int)lb.size() != B.rank || (int)lc.size() != C.rank)
     return fail(GBX_EINVAL, "index strings do not match tensor ranks (%d/%d, %d/%d, %d/%d)", (int)la.size(), A.rank,
                 (int)lb.size(), B.rank, (int)lc.size(), C.rank);
@@ -327,8 +328,28 @@ int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorL
     rows[tuple_irrep(dA, r)].off[r] = 0;
     cols[tuple_irrep(dB, c)].off[c] = 0;
   }
-  for_tuples(dK, [&](const std::vector<int>& k) { ks[tuple_irrep(dK, k)].off[k] = 0; });
-  if (dK.empty()) ks[0].off[std::vector<int>()] = 0;
+  // ks_full: every contracted block tuple (the algorithmic flops, the direct
+  // engine); ks: the tuples the packed GEMMs run over -- with a symmetric
+  // contracted pair, block pairs X >= Y only
+  int px = -1, py = -1;
+  if (pair) {
+    for (size_t t = 0; t < s.contrA.size(); ++t) {
+      if (la[s.contrA[t]] == pair->x) px = (int)t;
+      if (la[s.contrA[t]] == pair->y) py = (int)t;
+    }
+    if (px < 0 || py < 0 || px == py)
+      return fail(GBX_EINVAL, "pair %s%s is not two contracted indices", pair->x.c_str(), pair->y.c_str());
+    if (!dK[px]->same_as(*dK[py])) return fail(GBX_EINVAL, "pair %s%s: blocking differs", pair->x.c_str(), pair->y.c_str());
+  }
+  std::map<int, TupleIndex> ks_full;
+  for_tuples(dK, [&](const std::vector<int>& k) {
+    ks_full[tuple_irrep(dK, k)].off[k] = 0;
+    if (px < 0 || k[px] >= k[py]) ks[tuple_irrep(dK, k)].off[k] = 0;
+  });
+  if (dK.empty()) {
+    ks[0].off[std::vector<int>()] = 0;
+    ks_full[0].off[std::vector<int>()] = 0;
+  }
   auto assign = [](TupleIndex& ti, const std::vector<const BlockDim*>& dims) {
     ti.total = 0;
     for (auto& kv : ti.off) {
@@ -339,6 +360,7 @@ int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorL
   for (auto& kv : rows) assign(kv.second, dA);
   for (auto& kv : cols) assign(kv.second, dB);
   for (auto& kv : ks) assign(kv.second, dK);
+  for (auto& kv : ks_full) assign(kv.second, dK);
   // irrep groups present in rows, cols and K
   int64_t ao = 0, bo = 0, co = 0;
   std::map<int, int> gidx;
@@ -366,7 +388,8 @@ int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorL
 
   // pack moves: A (rows = extA tuples of irrep h, cols = K tuples of irrep h)
   auto pack = [&](const TensorLayout& T, const std::vector<int>& ext_dims, const std::vector<int>& contr_dims,
-                  std::map<int, TupleIndex>& rowsets, bool isA, MoveSet& ms, bool& needs_zero) -> int {
+                  std::map<int, TupleIndex>& rowsets, bool isA, MoveSet& ms, bool& needs_zero,
+                  bool pair_scaled) -> int {
     std::vector<const BlockDim*> dR;
     for (int d : ext_dims) dR.push_back(T.dims[d].get());
     for (auto& kv : rowsets) {
@@ -407,6 +430,8 @@ int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorL
           for (size_t i = 0; i < ext_dims.size(); ++i) dstr[ext_dims[i]] = sR[i];
           for (size_t i = 0; i < contr_dims.size(); ++i) dstr[contr_dims[i]] = sK[i];
           int64_t dst = (isA ? g.a_off : g.b_off) + rv.second * g.K + kvv.second;
+          // off-diagonal block pairs of a symmetric contracted pair count twice
+          if (pair_scaled && px >= 0 && kvv.first[px] > kvv.first[py]) factor *= 2.0;
           ms.host.push_back(make_move(T.rank, ext, sstr, dstr, T.off[id], dst, 0, factor));
         }
       }
@@ -414,8 +439,8 @@ int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorL
     return GBX_OK;
   };
   std::vector<int> contrB_in_A_order = s.contrB;
-  GBX_TRY(pack(A, s.extA, s.contrA, rows, true, p->packA, p->a_needs_zero));
-  GBX_TRY(pack(B, s.extB, contrB_in_A_order, cols, false, p->packB, p->b_needs_zero));
+  GBX_TRY(pack(A, s.extA, s.contrA, rows, true, p->packA, p->a_needs_zero, pair && !pair->scale_b));
+  GBX_TRY(pack(B, s.extB, contrB_in_A_order, cols, false, p->packB, p->b_needs_zero, pair && pair->scale_b));
 
   // unpack C tiles
   for (size_t t = 0; t < C.tiles.size(); ++t) {
@@ -448,9 +473,9 @@ int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorL
   for (auto& g : p->groups) gf += 2.0 * (double)g.M * (double)g.N * (double)g.K;
   for (size_t t = 0; t < C.tiles.size(); ++t) {
     int hr = tuple_irrep(dA, c_row[t]);
-    if (!ks.count(hr)) continue;
+    if (!ks_full.count(hr)) continue;
     double mn = (double)tuple_size(dA, c_row[t]) * (double)tuple_size(dB, c_col[t]);
-    for (auto& kv : ks[hr].off) {
+    for (auto& kv : ks_full[hr].off) {
       int v[kMaxDims], sd[kMaxDims];
       double f;
       for (size_t i = 0; i < s.extA.size(); ++i) v[s.extA[i]] = c_row[t][i];
@@ -482,8 +507,8 @@ int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorL
       if (ntile >= ((int64_t)1 << 31)) ok = false;
       const int hr = tuple_irrep(dA, c_row[t]);
       const uint32_t pair0 = (uint32_t)pairs.size();
-      if (ok && ks.count(hr)) {
-        for (auto& kv : ks[hr].off) {
+      if (ok && ks_full.count(hr)) {
+        for (auto& kv : ks_full[hr].off) {
           int v[kMaxDims], w[kMaxDims], sdA[kMaxDims], sdB[kMaxDims];
           double fA, fB;
           for (size_t i = 0; i < s.extA.size(); ++i) v[s.extA[i]] = c_row[t][i];

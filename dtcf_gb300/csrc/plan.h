@@ -189,10 +189,21 @@ constexpr double kDirectMaxK = 16.0;
 // split_all: every packed GEMM of a split plan uses the split engine (tests),
 // and no contraction takes the direct engine.
 // defer: plan only (host); the caller sets the static flags and calls build().
+// Two contracted indices in which A and B are both antisymmetric (or both
+// symmetric): sum_{x,y} A_..xy B_..xy = 2 sum_{X>Y blocks} + sum_{X=Y blocks},
+// so the packed GEMMs run over block pairs X >= Y only, the off-diagonal ones
+// weighted 2 in one operand's pack (scale_b: B's, else A's) -- close to half
+// the contracted extent.  Both indices must have the same blocking.
+struct ContractionPair {
+  std::string x, y;
+  bool scale_b = true;
+};
+
 int plan_contraction(const TensorLayout& A, const TensorLayout& B, const TensorLayout& C,
                      const std::vector<std::string>& la, const std::vector<std::string>& lb,
                      const std::vector<std::string>& lc, Engine e, int nslices,
-                     std::unique_ptr<ContractionPlan>& out, bool split_all = false, bool defer = false);
+                     std::unique_ptr<ContractionPlan>& out, bool split_all = false, bool defer = false,
+                     const ContractionPair* pair = nullptr);
 
 // Tile moves accumulating alpha * permuted A into C: C[c] += alpha * A[a],
 // the DLTC Summation (DLTC/task.cc:51-81) over block-sparse layouts.

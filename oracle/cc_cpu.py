@@ -73,6 +73,15 @@ def contraction_list(method="ccsd"):
     return L
 
 
+# Contractions whose two operands are both antisymmetric in a pair of
+# contracted indices (tau, taut, t2, W_mnij and the <pq||rs> blocks): the
+# product's planner runs their GEMMs over block pairs x >= y only (the
+# off-diagonal pairs weighted 2).  Keyed by (C, la, lb).
+PAIRS = {("Fae", "mnaf", "mnef"): "mn", ("Fmi", "inef", "mnef"): "ef", ("Wmnij", "ijef", "mnef"): "ef",
+         ("R1", "imef", "maef"): "ef", ("R1", "mnae", "nmei"): "mn", ("Lad", "mnab", "mnij"): "mn",
+         ("Lad", "abef", "ijef"): "ef", ("Zp", "ijef", "maef"): "ef"}
+
+
 def _irrep_counts(system):
     n_irr = int(system.irrep.max()) + 1
     nirrep = 1
@@ -131,16 +140,24 @@ def _ext_counts(system, counts, nirrep, C, lc, X, lx):
     return _conv_canonical(system, sp, pairs, nirrep)
 
 
-def gemm_shapes(system, method="ccsd"):
-    """Per-irrep (M, N, K) of every contraction of one iteration."""
+def gemm_shapes(system, method="ccsd", pairs=True):
+    """Per-irrep (M, N, K) of every contraction of one iteration.  pairs:
+    contracted extents over the block pairs x >= y of PAIRS, as the
+    product's planner packs them; False: every contracted block tuple, as
+    the reference's algorithm computes them."""
     nirrep, counts = _irrep_counts(system)
     shapes = []
     for C, lc, A, la, B, lb in contraction_list(method):
         sa = spaces(A)
+        cl = [l for l in la if l in lb]
         con = "".join(sa[i] for i, l in enumerate(la) if l in lb)
         M = _ext_counts(system, counts, nirrep, C, lc, A, la)
         N = _ext_counts(system, counts, nirrep, C, lc, B, lb)
-        K = _conv(counts, con, nirrep)
+        pr = PAIRS.get((C, la, lb)) if pairs else None
+        if pr:
+            K = _conv_canonical(system, con, [(cl.index(pr[0]), cl.index(pr[1]))], nirrep)
+        else:
+            K = _conv(counts, con, nirrep)
         for h in range(nirrep):
             if M[h] and N[h] and K[h]:
                 shapes.append((int(M[h]), int(N[h]), int(K[h])))
