@@ -474,7 +474,8 @@ __global__ void __launch_bounds__(SplitCfg<BN>::kThreads, SplitCfg<BN>::kCtasPer
 // are padded to the k-block, so short K (a virtual block of ~30 orbitals)
 // streams half the bytes with the narrow block.
 constexpr int kThinBN = 32;
-constexpr int kThinThreads = 192;
+constexpr int kThinDrainWarps = 8;  // two groups of four (one per TMEM lane quarter), alternate tiles
+constexpr int kThinThreads = 64 + 32 * kThinDrainWarps;
 
 template <int TBK>
 struct ThinSmem {
@@ -490,9 +491,12 @@ struct ThinSmem {
 // 0 up (|X_l| <= 7 * 64 * 2^14 < 2^23, so |Y| < 2^63 for L <= 5; S = 7 keeps
 // the FP64 recombination); the accumulator buffer is released before the
 // scaled results are stored.
+// ea: the row's exponent, eb8: the first 8 column exponents, both loaded
+// by the caller before it waited for the accumulator (their latency hidden
+// behind the wait); columns past 8 are read here.
 template <int NC>
 __device__ __forceinline__ void thin_drain(uint32_t tb, int L, int ncol, const DevProblem& pr, int row,
-                                           uint64_t* accempty, int lane) {
+                                           uint64_t* accempty, int lane, int ea, const int* eb8) {
   long long Y[NC];
   double acc[NC];
 #pragma unroll
@@ -500,37 +504,53 @@ __device__ __forceinline__ void thin_drain(uint32_t tb, int L, int ncol, const D
     Y[j] = 0;
     acc[j] = 0.0;
   }
-  for (int l = L <= 5 ? 0 : L; L <= 5 ? l <= L : l >= 0; l += L <= 5 ? 1 : -1) {
-    uint32_t r[NC];
-    if (NC == 8) {
-      tmem_ld8(tb + (uint32_t)(l * kThinBN), r);
-    } else {
+  if (NC == 8 && L <= 3) {
+    // at most four levels of 8 columns (the usual thin tile: an occupied
+    // block of about 6): every load issued, then one wait
+    uint32_t rb[4][8];
 #pragma unroll
-      for (int h = 0; h < NC / 16; ++h)
-        tmem_ld16(tb + (uint32_t)(l * kThinBN + 16 * h), *reinterpret_cast<uint32_t(*)[16]>(r + 16 * h));
-    }
+    for (int l = 0; l < 4; ++l)
+      if (l <= L) tmem_ld8(tb + (uint32_t)(l * kThinBN), rb[l]);
     tmem_wait_ld();
-    if (L <= 5) {
 #pragma unroll
-      for (int j = 0; j < NC; ++j)
-        if (j < ncol) Y[j] = Y[j] * 256 + (long long)__float2int_rn(__uint_as_float(r[j]));
-    } else {
+    for (int l = 0; l < 4; ++l)
+      if (l <= L) {
 #pragma unroll
-      for (int j = 0; j < NC; ++j)
-        if (j < ncol) acc[j] = acc[j] * 0x1.0p-8 + (double)__uint_as_float(r[j]);
+        for (int j = 0; j < 8; ++j)
+          if (j < ncol) Y[j] = Y[j] * 256 + (long long)__float2int_rn(__uint_as_float(rb[l][j]));
+      }
+  } else {
+    for (int l = L <= 5 ? 0 : L; L <= 5 ? l <= L : l >= 0; l += L <= 5 ? 1 : -1) {
+      uint32_t r[NC];
+      if (NC == 8) {
+        tmem_ld8(tb + (uint32_t)(l * kThinBN), r);
+      } else {
+#pragma unroll
+        for (int h = 0; h < NC / 16; ++h)
+          tmem_ld16(tb + (uint32_t)(l * kThinBN + 16 * h), *reinterpret_cast<uint32_t(*)[16]>(r + 16 * h));
+      }
+      tmem_wait_ld();
+      if (L <= 5) {
+#pragma unroll
+        for (int j = 0; j < NC; ++j)
+          if (j < ncol) Y[j] = Y[j] * 256 + (long long)__float2int_rn(__uint_as_float(r[j]));
+      } else {
+#pragma unroll
+        for (int j = 0; j < NC; ++j)
+          if (j < ncol) acc[j] = acc[j] * 0x1.0p-8 + (double)__uint_as_float(r[j]);
+      }
     }
   }
   tc_fence_before();
   __syncwarp();
   if (lane == 0) mbar_arrive(accempty);
   if (row < pr.M) {
-    const int ea = pr.eA[row];
     double* crow = pr.C + (int64_t)row * pr.ldc;
     const int lshift = L <= 5 ? 8 * L : 0;  // the int64 path carries 2^(8L)
 #pragma unroll
     for (int j = 0; j < NC; ++j) {
       if (j < ncol) {
-        int ex = ea + pr.eB[j] - 2 * 1022 - 14 - lshift + 1023;
+        int ex = ea + (j < 8 ? eb8[j] : pr.eB[j]) - 2 * 1022 - 14 - lshift + 1023;
         ex = ex < 1 ? 1 : (ex > 2046 ? 2046 : ex);
         const double v = L <= 5 ? (double)Y[j] : acc[j];
         crow[j] = v * __longlong_as_double((long long)ex << 52);
@@ -653,31 +673,37 @@ __global__ void __launch_bounds__(kThinThreads, 1) split_thin_kernel(const GemmP
       mbar_wait(&sm.done, 0, P.err, 16);
     }
   } else {
+    // two drain groups of four warps: group g drains this CTA's tiles g,
+    // g + 2, g + 4, ... -- always from accumulator buffer g -- so that two
+    // tiles drain at once (a drain, with its exponent loads, TMEM reads and
+    // scattered row stores, takes longer than a tile's MMAs)
+    const int group = (warp - 2) >> 2;
     const int quarter = warp & 3;
     const uint32_t lane_addr = (uint32_t)(quarter * 32) << 16;
-    int buf = 0;
+    const int buf = group;
     uint32_t aphase = 0;
-    for (int tile = blockIdx.x; tile < P.total_tiles; tile += gridDim.x) {
+    for (int tile = blockIdx.x + group * (int)gridDim.x; tile < P.total_tiles; tile += 2 * (int)gridDim.x) {
       const TileInfo ti = decode_tile<kThinBN>(P, tile);
       const DevProblem& pr = P.probs[ti.p];
+      // only the tile's real columns are read and combined: a drain sized
+      // for 8, 16 or 32 columns (the thin problems of a block-sparse
+      // contraction often have an occupied block of ~6 as N)
+      const int ncol = min(kThinBN, pr.N - ti.n0);
+      const int row = ti.m0 + quarter * 32 + lane;
+      const int ea = row < pr.M ? pr.eA[row] : 0;
+      int eb8[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) eb8[j] = j < ncol ? pr.eB[j] : 0;  // thin tiles start at column 0
       int w_ok = lane == 0 ? (int)mbar_wait(&sm.accfull[buf], aphase, P.err, 14) : 1;
       w_ok = __shfl_sync(0xffffffffu, w_ok, 0);
       if (!w_ok) break;
       __syncwarp();
       tc_fence_after();
-      // only the tile's real columns are read and combined: a drain sized
-      // for 8, 16 or 32 columns (the thin problems of a block-sparse
-      // contraction often have an occupied block of ~6 as N)
-      const int ncol = min(kThinBN, pr.N - ti.n0);
       const uint32_t tb = tmem + lane_addr + (uint32_t)buf * buf_cols;
-      const int row = ti.m0 + quarter * 32 + lane;
-      if (ncol <= 8) thin_drain<8>(tb, L, ncol, pr, row, &sm.accempty[buf], lane);
-      else if (ncol <= 16) thin_drain<16>(tb, L, ncol, pr, row, &sm.accempty[buf], lane);
-      else thin_drain<32>(tb, L, ncol, pr, row, &sm.accempty[buf], lane);
-      if (++buf == 2) {
-        buf = 0;
-        aphase ^= 1;
-      }
+      if (ncol <= 8) thin_drain<8>(tb, L, ncol, pr, row, &sm.accempty[buf], lane, ea, eb8);
+      else if (ncol <= 16) thin_drain<16>(tb, L, ncol, pr, row, &sm.accempty[buf], lane, ea, eb8);
+      else thin_drain<32>(tb, L, ncol, pr, row, &sm.accempty[buf], lane, ea, eb8);
+      aphase ^= 1;
     }
   }
   tc_fence_before();
