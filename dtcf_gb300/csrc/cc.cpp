@@ -399,8 +399,11 @@ int gbx_cc_job::plan_all() {
   GBX_TRY(tensor("t2", "oovv"));
   GBX_TRY(tensor("Dinv2", "oovv"));  // 1 / (e_i + e_j - e_a - e_b)
   GBX_TRY(tensor("Xa", "oovv"));
-  GBX_TRY(tensor("Xb", "oovv"));
-  GBX_TRY(tensor("Xj", "oovv"));
+  // every term of X_b (t2 F', Z' t1, t1 <mb||ij>) is antisymmetric in ij,
+  // every term of X_j (t2 F', t1 <ab||ej>) in ab: both are formed on
+  // canonical tiles only (half the work), read back with sign factors
+  GBX_TRY(tensor("Xb", "oovv", {0, 0, -1, -1}));
+  GBX_TRY(tensor("Xj", "oovv", {-1, -1, 0, 0}));
   GBX_TRY(tensor("Fae", "vv"));
   GBX_TRY(tensor("Fmi", "oo"));
   // W_mnij is antisymmetric in mn and in ij: canonical tiles only

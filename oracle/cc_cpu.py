@@ -19,13 +19,14 @@ import time
 
 import numpy as np
 
-SPACES = {"t1": "ov", "t2": "oovv", "tau": "oovv", "taut": "oovv", "Xa": "oovv", "Q": "oovv", "R2": "oovv",
+SPACES = {"t1": "ov", "t2": "oovv", "tau": "oovv", "taut": "oovv", "Xa": "oovv", "Xb": "oovv", "Xj": "oovv",
+          "Q": "oovv", "R2": "oovv",
           "R1": "ov", "Fae": "vv", "Fbe": "vv", "Fmi": "oo", "Fmj": "oo", "Fme": "ov", "Wmnij": "oooo",
           "Xoooo": "oooo", "Wmbej": "ovvo", "Zp": "ooov", "V3": "oovo", "Lad": "oovv"}
 
 # Intermediates stored as canonical tiles only (antisymmetric index pairs, as
 # RRR stores unique blocks, tensor.cc:617-640): C positions of each pair.
-CANONICAL = {"Wmnij": [(0, 1), (2, 3)], "Lad": [(0, 1), (2, 3)], "Zp": [(0, 1)]}
+CANONICAL = {"Wmnij": [(0, 1), (2, 3)], "Lad": [(0, 1), (2, 3)], "Zp": [(0, 1)], "Xb": [(0, 1)], "Xj": [(2, 3)]}
 
 
 def spaces(name):
@@ -60,16 +61,16 @@ def contraction_list(method="ccsd"):
               ("R1", "ia", "t2", "imae", "Fme", "me"), ("R1", "ia", "t1", "nf", "OVOV", "naif"),
               ("R1", "ia", "t2", "imef", "OVVV", "maef"), ("R1", "ia", "t2", "mnae", "OOVO", "nmei"),
               ("Fbe", "be", "t1", "mb", "Fme", "me"), ("Fmj", "mj", "t1", "je", "Fme", "me")]
-    L += [("Xa", "ijab", "t2", "ijae", "Fbe" if sd else "Fae", "be"),
-          ("Xa", "ijab", "t2", "imab", "Fmj" if sd else "Fmi", "mj"),
+    L += [("Xb", "ijab", "t2", "ijae", "Fbe" if sd else "Fae", "be"),
+          ("Xj", "ijab", "t2", "imab", "Fmj" if sd else "Fmi", "mj"),
           ("Lad", "ijab", tau, "mnab", "Wmnij", "mnij"),
           ("Lad", "ijab", "VVVV", "abef", tau, "ijef")]
     if sd:
-        L += [("Zp", "ijma", tau, "ijef", "OVVV", "maef"), ("Xa", "ijab", "Zp", "ijma", "t1", "mb")]
+        L += [("Zp", "ijma", tau, "ijef", "OVVV", "maef"), ("Xb", "ijab", "Zp", "ijma", "t1", "mb")]
     L += [("Xa", "ijab", "t2", "imae", "Wmbej", "mbej")]
     if sd:
         L += [("V3", "imbj", "t1", "ie", "OVVO", "mbej"), ("Xa", "ijab", "t1", "ma", "V3", "imbj"),
-              ("Xa", "ijab", "t1", "ie", "VVVO", "abej"), ("Xa", "ijab", "t1", "ma", "OVOO", "mbij")]
+              ("Xj", "ijab", "t1", "ie", "VVVO", "abej"), ("Xb", "ijab", "t1", "ma", "OVOO", "mbij")]
     return L
 
 
