@@ -90,6 +90,7 @@ struct gbx_cc_job {
   std::map<std::string, std::unique_ptr<CCTensor>> T;
   std::vector<std::unique_ptr<ContractionPlan>> cplans;
   std::vector<std::unique_ptr<FusedSumPlan>> fplans;
+  std::vector<std::unique_ptr<MoveSet>> expansions;  // canonical tiles -> the others (fused with groups)
   // tau / taut / Q from t2 and t1 (CCSD): per-tile t1 offsets and work items
   std::vector<CCAmpTile> amp_tiles;
   std::vector<CCAmpItem> amp_items;
@@ -136,6 +137,7 @@ struct gbx_cc_job {
     prog.reset();
     cplans.clear();
     fplans.clear();
+    expansions.clear();
     amp.release();
     T.clear();
     tilesets.clear();
@@ -239,9 +241,19 @@ struct gbx_cc_job {
     const char* la;
     double coef;
   };
-  int fused(const char* out, const char* lc, const std::vector<Term>& terms, const char* scale = nullptr) {
+  // groups (optional): antisymmetric index groups of the result.  The terms
+  // are then formed on the canonical tiles only (block coordinates
+  // non-increasing within each group: about a quarter of an o^2 v^2 tensor
+  // with two groups) and every other tile is filled from its canonical
+  // partner by a permuted copy with the sign of the permutation -- the
+  // result is stored whole and is exactly antisymmetric.
+  int fused(const char* out, const char* lc, const std::vector<Term>& terms, const char* scale = nullptr,
+            const std::vector<int>& groups = {}) {
     CCTensor* C = get(out);
     GBX_TRY(check_labels(C, lc, out));
+    TensorLayout view;
+    std::unique_ptr<MoveSet> expand;
+    if (!groups.empty()) GBX_TRY(canonical_view(C->L, groups, view, expand));
     std::vector<FusedTermSpec> specs;
     std::vector<CCTensor*> src;
     std::string name = std::string(out) + "[" + lc + "]=";
@@ -275,16 +287,66 @@ struct gbx_cc_job {
     }
     dynamic_use.insert(out);
     std::unique_ptr<FusedSumPlan> p;
-    GBX_TRY(plan_fused_sum(C->L, labels(lc), specs, p));
+    GBX_TRY(plan_fused_sum(groups.empty() ? C->L : view, labels(lc), specs, p));
     FusedSumPlan* pp = p.get();
+    MoveSet* ex = expand.get();
+    if (expand) {
+      name += " (canonical tiles, expanded)";
+      expansions.push_back(std::move(expand));
+    }
     steps.push_back([=](cudaStream_t st) {
       const double* ptr[kFsMaxSlots] = {};
       for (size_t i = 0; i < src.size(); ++i) ptr[i] = src[i]->d;
-      return pp->execute(ptr, S ? S->d : nullptr, C->d, st);
+      GBX_TRY(pp->execute(ptr, S ? S->d : nullptr, C->d, st));
+      return ex ? run_moves(*ex, C->d, C->d, st) : GBX_OK;
     });
     info.push_back({name, 1, 0.0, bytes});
     launches += 1;
     fplans.push_back(std::move(p));
+    return GBX_OK;
+  }
+
+  // The canonical tiles of L for the antisymmetric groups (a layout view
+  // that keeps L's offsets) and the moves that fill L's other tiles from
+  // them: tile t gets sign * (its canonical partner, permuted).
+  static int canonical_view(const TensorLayout& L, const std::vector<int>& groups, TensorLayout& view,
+                            std::unique_ptr<MoveSet>& expand) {
+    const TensorLayout G = TensorLayout::full(L.dims, groups, -1, true);
+    view = TensorLayout();
+    view.rank = L.rank;
+    view.dims = L.dims;
+    view.nelem = L.nelem;
+    expand = std::make_unique<MoveSet>();
+    for (size_t t = 0; t < L.tiles.size(); ++t) {
+      const Coords& c = L.tiles[t];
+      if (G.find(c.data()) >= 0) {
+        view.index[coord_key(c.data(), L.rank)] = (int)view.tiles.size();
+        view.tiles.push_back(c);
+        view.off.push_back(L.off[t]);
+        continue;
+      }
+      int src_dim[kMaxDims];
+      double f;
+      const int id = G.resolve(c.data(), src_dim, &f);
+      if (id < 0) continue;  // a zero tile of the group structure
+      const int ct = L.find(G.tiles[id].data());
+      if (ct < 0) return fail(GBX_EINVAL, "canonical partner of a tile is not stored");
+      const Coords& sc = L.tiles[ct];
+      int64_t sst[kMaxDims], ext[kMaxDims], sstr[kMaxDims], dstr[kMaxDims];
+      sst[L.rank - 1] = 1;
+      dstr[L.rank - 1] = 1;
+      for (int d = L.rank - 2; d >= 0; --d) {
+        sst[d] = sst[d + 1] * L.dims[d + 1]->ext[sc[d + 1]];
+        dstr[d] = dstr[d + 1] * L.dims[d + 1]->ext[c[d + 1]];
+      }
+      for (int d = 0; d < L.rank; ++d) {
+        ext[d] = L.dims[d]->ext[c[d]];
+        sstr[d] = sst[src_dim[d]];
+      }
+      expand->host.push_back(make_move(L.rank, ext, sstr, dstr, L.off[ct], L.off[t], 0, f));
+    }
+    GBX_TRY(check_moves(*expand, L.nelem, L.nelem, "canonical expansion"));
+    if (expand->host.empty()) expand.reset();
     return GBX_OK;
   }
 
@@ -544,7 +606,7 @@ int gbx_cc_job::plan_all() {
                 {{"OOVV", "ijab", 1.0}, {"Lad", "ijab", 1.0}, {"Xb", "ijab", 1.0}, {"Xb", "ijba", -1.0},
                  {"Xj", "ijab", 1.0}, {"Xj", "jiab", -1.0}, {"Xa", "ijab", 1.0}, {"Xa", "jiab", -1.0},
                  {"Xa", "ijba", -1.0}, {"Xa", "jiba", 1.0}},
-                "Dinv2"));
+                "Dinv2", {0, 0, 1, 1}));
   if (sd) {
     GBX_TRY(denom("t1", "R1", "Dinv1"));
     GBX_TRY(tau_steps());
@@ -581,6 +643,7 @@ int gbx_cc_job::footprint(double* resident, double* peak) const {
     scratch = std::max(scratch, (double)sc);
   }
   for (auto& p : fplans) keep += up256d((double)(p->items.size() * sizeof(FsItem))) + up256d((double)(p->terms.size() * sizeof(FsTerm)));
+  for (auto& m : expansions) keep += up256d((double)m->device_bytes());
   keep += up256d((double)(amp_tiles.size() * sizeof(CCAmpTile))) + up256d((double)(amp_items.size() * sizeof(CCAmpItem)));
   auto tiles_bytes = [](const TensorLayout& L) {
     return up256d((double)L.tiles.size() * sizeof(CCTile)) + up256d(4.0 * (double)(L.tiles.size() + 1));
@@ -662,6 +725,7 @@ int gbx_cc_job::materialize(cudaStream_t st) {
   unsigned char* d_scratch = nullptr;
   if (scratch_bytes) GBX_TRY(dev_alloc((void**)&d_scratch, scratch_bytes));
   for (auto& p : fplans) GBX_TRY(p->upload());
+  for (auto& m : expansions) GBX_TRY(m->upload());
   if (!amp_items.empty()) GBX_TRY(amp.upload(amp_tiles, amp_items));
   for (size_t i = 0; i < cplans.size(); ++i) {
     ContractionPlan* p = cplans[i].get();
