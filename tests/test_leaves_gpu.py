@@ -290,10 +290,12 @@ def test_grouped_gemm_small_k(gbx, m, n, k):
     np.testing.assert_allclose(host(dC).reshape(m, n), C + 0.5 * A @ B.T, rtol=1e-13, atol=1e-13)
 
 
-@pytest.mark.parametrize("m,n,k,acc", [(6, 6, 20000, 1), (16, 16, 8192, 0), (3, 11, 5000, 1), (16, 1, 4096, 0)])
+@pytest.mark.parametrize("m,n,k,acc", [(6, 6, 20000, 1), (16, 16, 8192, 0), (3, 11, 5000, 1), (16, 1, 4096, 0),
+                                       (8, 8, 4096, 0), (1, 7, 4500, 1), (5, 2, 9001, 0), (7, 3, 12289, 1)])
 def test_grouped_gemm_small_output_long_k(gbx, m, n, k, acc):
     """Outputs of at most 16 x 16 with K >= 4096: one CTA per K chunk holds the
-    whole output, chunks reduced in a fixed order."""
+    whole output, chunks reduced in a fixed order (odd shapes and K that is
+    not a multiple of the chunk included)."""
     from dtcf_gb300.leaves import Triple
     rng = np.random.default_rng(m * n + k)
     A, B, C = rng.standard_normal((m, k)), rng.standard_normal((n, k)), rng.standard_normal((m, n))
