@@ -604,6 +604,40 @@ __device__ __forceinline__ void digits_body(const SplitRowSet* __restrict__ sets
 // once.  The row sets here carry first_row in rows.
 constexpr int64_t kMidRow = 16384;
 
+// A row of at most kPer * 256 elements: every element loaded at once (one
+// HBM round trip per row instead of one per 1024 elements and pass), the
+// exponent reduced across the CTA, the digits written from the registers.
+template <bool kCoh, int kPer>
+__device__ __forceinline__ void split_row_in_registers(const SplitRowSet& rs, int64_t row, const double* src, int F,
+                                                       int S, uint32_t* red) {
+  const int K = (int)rs.K;
+  long long v[kPer];
+#pragma unroll
+  for (int u = 0; u < kPer; ++u) {
+    const int k = (int)threadIdx.x + u * 256;
+    v[u] = k < K ? __double_as_longlong(ldin<kCoh>(src + k)) : 0;
+  }
+  uint32_t emax = 0;
+#pragma unroll
+  for (int u = 0; u < kPer; ++u) emax = max(emax, (uint32_t)((v[u] >> 52) & 0x7FF));
+  for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+  __syncthreads();  // the previous row is done with red
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = emax;
+  __syncthreads();
+  uint32_t m = 0;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) m = max(m, red[w]);
+  if (threadIdx.x == 0) rs.exps[row] = (int)m;
+  __nv_bfloat16* dst = rs.dst + row * rs.Kp;
+#pragma unroll
+  for (int u = 0; u < kPer; ++u) {
+    const int k = (int)threadIdx.x + u * 256;
+    if (k < K) write_digits(v[u], m, F, S, dst + k, rs.slice_stride);
+  }
+  for (int64_t k = K + threadIdx.x; k < rs.Kp; k += 256)
+    for (int s = 0; s < S; ++s) dst[s * rs.slice_stride + k] = __int2bfloat16_rn(0);
+}
+
 template <bool kCoh>
 __device__ __forceinline__ void split_rows_body(const SplitRowSet* __restrict__ sets, int nsets, int64_t total_rows,
                                                 int S, uint32_t bid, uint32_t nblk, uint32_t* red) {
@@ -618,6 +652,14 @@ __device__ __forceinline__ void split_rows_body(const SplitRowSet* __restrict__ 
     const int64_t row = rg - rs.first_row;
     const double* src = rs.src + row * rs.ld;
     const int64_t K = rs.K;
+    if (K <= 8 * 256) {
+      split_row_in_registers<kCoh, 8>(rs, row, src, F, S, red);
+      continue;
+    }
+    if (K <= 16 * 256) {
+      split_row_in_registers<kCoh, 16>(rs, row, src, F, S, red);
+      continue;
+    }
     uint32_t emax = 0;
     for (int64_t k = threadIdx.x; k < K; k += 4 * 256) {
       long long v[4];
