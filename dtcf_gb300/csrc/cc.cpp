@@ -195,9 +195,11 @@ struct gbx_cc_job {
 
   // pair: two contracted labels in which A and B are both antisymmetric
   // (the packed GEMMs then run over block pairs x >= y, the off-diagonal ones
-  // weighted 2 in the pack of the constant operand, or of the smaller one)
+  // weighted 2 in the pack of the constant operand, or of the smaller one).
+  // from_zero: C starts from zero -- the contraction stores alpha A B when it
+  // writes every element of C, else C is zero-filled first.
   int contract(const char* c, const char* lc, const char* a, const char* la, const char* b, const char* lb,
-               double alpha, const char* pair = nullptr) {
+               double alpha, const char* pair = nullptr, bool from_zero = false) {
     CCTensor *C = get(c), *A = get(a), *B = get(b);
     GBX_TRY(check_labels(C, lc, c));
     GBX_TRY(check_labels(A, la, a));
@@ -220,12 +222,15 @@ struct gbx_cc_job {
     if (!p->a_static) dynamic_use.insert(a);
     if (!p->b_static) dynamic_use.insert(b);
     dynamic_use.insert(c);
+    const bool stores = from_zero && p->set_overwrite(alpha, C->L.nelem);
+    if (from_zero && !stores) GBX_TRY(zero(c));
     flops += p->flops;
     gemm_flops += p->gemm_flops;
     ContractionPlan* pp = p.get();
     steps.push_back([=](cudaStream_t st) { return pp->execute(A->d, B->d, C->d, alpha, st); });
-    info.push_back({std::string(c) + "[" + lc + "]+=" + a + "[" + la + "]*" + b + "[" + lb + "]", 0, pp->flops,
-                    8.0 * (double)(A->L.nelem + B->L.nelem + 2 * C->L.nelem), (int)cplans.size()});
+    info.push_back({std::string(c) + "[" + lc + "]" + (stores ? "=" : "+=") + a + "[" + la + "]*" + b + "[" + lb + "]", 0,
+                    pp->flops, 8.0 * (double)(A->L.nelem + B->L.nelem + (stores ? 1 : 2) * C->L.nelem),
+                    (int)cplans.size()});
     launches += pp->direct ? 1 : 4;
     cplans.push_back(std::move(p));
     plan_operands.push_back({A, B});
@@ -518,21 +523,16 @@ int gbx_cc_job::plan_all() {
   // (tau, taut and Q of the current amplitudes exist: formed at the end of
   // the previous iteration, by the initial guess or by set_amplitudes)
   // F_ae, F_mi, F_me
-  GBX_TRY(zero("Fae"));
-  if (sd) GBX_TRY(contract("Fae", "ae", "t1", "mf", "OVVV", "mafe", 1.0));
+  // (the first contraction into each intermediate starts it from zero)
+  if (sd) GBX_TRY(contract("Fae", "ae", "t1", "mf", "OVVV", "mafe", 1.0, nullptr, true));
   // (taut, tau and t2 are antisymmetric in i <-> j and in a <-> b, like <pq||rs>)
-  GBX_TRY(contract("Fae", "ae", TAUT, "mnaf", "OOVV", "mnef", -0.5, "mn"));
-  GBX_TRY(zero("Fmi"));
-  if (sd) GBX_TRY(contract("Fmi", "mi", "t1", "ne", "OOOV", "mnie", 1.0));
-  GBX_TRY(contract("Fmi", "mi", TAUT, "inef", "OOVV", "mnef", 0.5, "ef"));
-  if (sd) {
-    GBX_TRY(zero("Fme"));
-    GBX_TRY(contract("Fme", "me", "t1", "nf", "OOVV", "mnef", 1.0));
-  }
+  GBX_TRY(contract("Fae", "ae", TAUT, "mnaf", "OOVV", "mnef", -0.5, "mn", !sd));
+  if (sd) GBX_TRY(contract("Fmi", "mi", "t1", "ne", "OOOV", "mnie", 1.0, nullptr, true));
+  GBX_TRY(contract("Fmi", "mi", TAUT, "inef", "OOVV", "mnef", 0.5, "ef", !sd));
+  if (sd) GBX_TRY(contract("Fme", "me", "t1", "nf", "OOVV", "mnef", 1.0, nullptr, true));
   // W_mnij (with the ladder's 1/8 tau <mn||ef> tau term folded in: 1/2 instead of 1/4)
   if (sd) {
-    GBX_TRY(zero("Xoooo"));
-    GBX_TRY(contract("Xoooo", "mnij", "t1", "je", "OOOV", "mnie", 1.0));
+    GBX_TRY(contract("Xoooo", "mnij", "t1", "je", "OOOV", "mnie", 1.0, nullptr, true));
     GBX_TRY(fused("Wmnij", "mnij", {{"OOOO", "mnij", 1.0}, {"Xoooo", "mnij", 1.0}, {"Xoooo", "mnji", -1.0}}));
   } else {
     GBX_TRY(fused("Wmnij", "mnij", {{"OOOO", "mnij", 1.0}}));
@@ -549,8 +549,7 @@ int gbx_cc_job::plan_all() {
   GBX_TRY(contract("Wmbej", "mbej", "Q", "jnfb", "OOVV", "mnef", -1.0));
   // T1 residual
   if (sd) {
-    GBX_TRY(zero("R1"));
-    GBX_TRY(contract("R1", "ia", "t1", "ie", "Fae", "ae", 1.0));
+    GBX_TRY(contract("R1", "ia", "t1", "ie", "Fae", "ae", 1.0, nullptr, true));
     GBX_TRY(contract("R1", "ia", "t1", "ma", "Fmi", "mi", -1.0));
     GBX_TRY(contract("R1", "ia", "t2", "imae", "Fme", "me", 1.0));
     GBX_TRY(contract("R1", "ia", "t1", "nf", "OVOV", "naif", -1.0));
@@ -570,29 +569,23 @@ int gbx_cc_job::plan_all() {
   }
   // Terms under the same antisymmetriser share one intermediate, expanded
   // into R2 once: Xb under P(ab), Xj under P(ij), Xa under P(ij)P(ab).
-  GBX_TRY(zero("Xb"));
-  GBX_TRY(zero("Xj"));
-  GBX_TRY(zero("Xa"));
   // P(ab) t_ij^ae F'_be
-  GBX_TRY(contract("Xb", "ijab", "t2", "ijae", FBE, "be", 1.0));
+  GBX_TRY(contract("Xb", "ijab", "t2", "ijae", FBE, "be", 1.0, nullptr, true));
   // -P(ij) t_im^ab F'_mj
-  GBX_TRY(contract("Xj", "ijab", "t2", "imab", FMJ, "mj", -1.0));
+  GBX_TRY(contract("Xj", "ijab", "t2", "imab", FMJ, "mj", -1.0, nullptr, true));
   // 1/2 tau_mn^ab W_mnij + 1/2 tau_ij^ef <ab||ef> (the ladder, integrals as
   // the static A operand), on canonical tiles, then into R2
-  GBX_TRY(zero("Lad"));
-  GBX_TRY(contract("Lad", "ijab", TAU, "mnab", "Wmnij", "mnij", 0.5, "mn"));
+  GBX_TRY(contract("Lad", "ijab", TAU, "mnab", "Wmnij", "mnij", 0.5, "mn", true));
   GBX_TRY(contract("Lad", "ijab", "VVVV", "abef", TAU, "ijef", 0.5, "ef"));
   if (sd) {
     // -1/2 P(ab) t_m^b sum_ef tau_ij^ef <am||ef> = +1/2 P(ab) sum_m t_m^b Z'_ijma
-    GBX_TRY(zero("Zp"));
-    GBX_TRY(contract("Zp", "ijma", TAU, "ijef", "OVVV", "maef", 1.0, "ef"));
+    GBX_TRY(contract("Zp", "ijma", TAU, "ijef", "OVVV", "maef", 1.0, "ef", true));
     GBX_TRY(contract("Xb", "ijab", "Zp", "ijma", "t1", "mb", 0.5));
   }
   // P(ij)P(ab) (t_im^ae W_mbej - t_i^e t_m^a <mb||ej>)
-  GBX_TRY(contract("Xa", "ijab", "t2", "imae", "Wmbej", "mbej", 1.0));
+  GBX_TRY(contract("Xa", "ijab", "t2", "imae", "Wmbej", "mbej", 1.0, nullptr, true));
   if (sd) {
-    GBX_TRY(zero("V3"));
-    GBX_TRY(contract("V3", "imbj", "t1", "ie", "OVVO", "mbej", 1.0));
+    GBX_TRY(contract("V3", "imbj", "t1", "ie", "OVVO", "mbej", 1.0, nullptr, true));
     GBX_TRY(contract("Xa", "ijab", "t1", "ma", "V3", "imbj", -1.0));
     // P(ij) t_i^e <ab||ej>
     GBX_TRY(contract("Xj", "ijab", "t1", "ie", "VVVO", "abej", 1.0));
@@ -1155,20 +1148,25 @@ int gbx_cc_time_gemm(gbx_cc_job* job, int contraction, int reps, float* ms, doub
   GBX_CUDA(cudaEventCreate(&e1));
   // the arena is shared by every plan: pack and split this plan's operands
   // again, then time only the GEMM launches (a direct plan: its one launch
-  // with alpha = 0, which leaves C as it is)
+  // accumulating with alpha = 0, which leaves C as it is)
   const double* dA = job->plan_operands[contraction].first->d;
   const double* dB = job->plan_operands[contraction].second->d;
   double* dC = job->plan_outputs[contraction]->d;
   GBX_TRY(p->stage(dA, dB, st));
+  const bool stores = p->dir_overwrite;
+  p->dir_overwrite = false;
   GBX_CUDA(cudaEventRecord(e0, st));
-  for (int r = 0; r < reps; ++r) {
+  int rc = GBX_OK;
+  for (int r = 0; r < reps && rc == GBX_OK; ++r) {
     if (p->direct) {
-      GBX_TRY(p->execute(dA, dB, dC, 0.0, st));
+      rc = p->execute(dA, dB, dC, 0.0, st);
       continue;
     }
-    if (p->split) GBX_TRY(run_split_plan(p->split, false, false, st));
-    GBX_TRY(p->f64.run(st));
+    if (p->split) rc = run_split_plan(p->split, false, false, st);
+    if (rc == GBX_OK) rc = p->f64.run(st);
   }
+  p->dir_overwrite = stores;
+  GBX_TRY(rc);
   GBX_CUDA(cudaEventRecord(e1, st));
   GBX_CUDA(cudaEventSynchronize(e1));
   float t = 0.f;
@@ -1236,9 +1234,10 @@ int gbx_cc_contraction_error(gbx_cc_job* job, int contraction, double* rel_frob_
     cudaMemsetAsync(c_job, 0, sizeof(double) * n, st);
     cudaMemsetAsync(c_ref, 0, sizeof(double) * n, st);
     // the job's plan on the current operands (constant ones are already
-    // packed and split and are not read again)
+    // packed and split and are not read again); a plan that stores its
+    // result does so with its own factor, which the FP64 plan then takes
     rc = p->execute(A->d, B->d, c_job, 1.0, st);
-    if (rc == GBX_OK) rc = ref->execute(rA, rB, c_ref, 1.0, st);
+    if (rc == GBX_OK) rc = ref->execute(rA, rB, c_ref, p->store_scale != 0.0 ? p->store_scale : 1.0, st);
     if (rc == GBX_OK) {
       cudaError_t e = cudaMemcpyAsync(h_job.data(), c_job, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
       if (e == cudaSuccess) e = cudaMemcpyAsync(h_ref.data(), c_ref, sizeof(double) * n, cudaMemcpyDeviceToHost, st);

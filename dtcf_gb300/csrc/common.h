@@ -180,8 +180,9 @@ struct DirItem {
   uint32_t pair0, npair;
 };
 
+// overwrite: C = alpha A B (the items cover all of C), else C += alpha A B
 int run_direct(const DirItem* items, int nitems, const DirPair* pairs, const double* A, const double* B, double* C,
-               double alpha, cudaStream_t st);
+               double alpha, bool overwrite, cudaStream_t st);
 
 // One FP64 GEMM problem of a grouped launch (element strides).
 struct GemmProblem {

@@ -21,21 +21,21 @@ constexpr int kDirThreads = 512;
 __global__ void __launch_bounds__(kDirThreads, 2)
     direct_contract_kernel(const DirItem* __restrict__ items, int nitems, const DirPair* __restrict__ pairs,
                            const double* __restrict__ A, const double* __restrict__ B, double* __restrict__ C,
-                           double alpha) {
+                           double alpha, int overwrite) {
   __shared__ dev::DirSmem sm;
-  dev::direct_body<kDirThreads, false>(items, nitems, pairs, A, B, C, alpha, blockIdx.x, gridDim.x, sm);
+  dev::direct_body<kDirThreads, false>(items, nitems, pairs, A, B, C, alpha, overwrite, blockIdx.x, gridDim.x, sm);
 }
 
 int run_direct(const DirItem* items, int nitems, const DirPair* pairs, const double* A, const double* B, double* C,
-               double alpha, cudaStream_t st) {
+               double alpha, bool overwrite, cudaStream_t st) {
   if (nitems == 0) return GBX_OK;
   const int grid = std::min(nitems, 152 * 6);
   if (ProgRecorder* rec = prog_recording()) {
     ProgArgs a;
-    a.direct = {items, pairs, A, B, C, alpha, nitems};
+    a.direct = {items, pairs, A, B, C, alpha, nitems, overwrite ? 1 : 0};
     return prog_mem(rec, PK_DIRECT, (uint32_t)grid, a, {{A, false}, {B, false}, {C, true}});
   }
-  direct_contract_kernel<<<grid, kDirThreads, 0, st>>>(items, nitems, pairs, A, B, C, alpha);
+  direct_contract_kernel<<<grid, kDirThreads, 0, st>>>(items, nitems, pairs, A, B, C, alpha, overwrite ? 1 : 0);
   GBX_CUDA(cudaGetLastError());
   return GBX_OK;
 }

@@ -867,7 +867,7 @@ int ContractionPlan::stage(const double* dA, const double* dB, cudaStream_t st) 
 int ContractionPlan::execute(const double* dA, const double* dB, double* dC, double alpha, cudaStream_t st) {
   if (direct) {
     if (!dA || !dB || !dC) return fail(GBX_EINVAL, "contraction operand without device memory");
-    return run_direct(d_dir_items, (int)dir_items.size(), d_dir_pairs, dA, dB, dC, alpha, st);
+    return run_direct(d_dir_items, (int)dir_items.size(), d_dir_pairs, dA, dB, dC, alpha, dir_overwrite, st);
   }
   if (f64.nprob == 0 && !split) return GBX_OK;
   const bool skipA = a_static && static_ready, skipB = b_static && static_ready;
@@ -883,6 +883,30 @@ int ContractionPlan::execute(const double* dA, const double* dB, double* dC, dou
   GBX_TRY(f64.run(st));
   if (split) GBX_TRY(run_split_plan(split, !skipA, !skipB, st));
   return run_moves_scaled(unpackC, d_Cbig, dC, alpha, st);
+}
+
+bool ContractionPlan::set_overwrite(double alpha, int64_t c_elems) {
+  int64_t covered = 0;
+  if (direct) {
+    for (const DirItem& it : dir_items) covered += it.n;
+  } else {
+    for (const MoveDesc& m : unpackC.host) {
+      if (m.op != 1 || m.scale != 1.0) return false;
+      covered += m.n;
+    }
+  }
+  if (covered != c_elems) return false;
+  if (direct) {
+    dir_overwrite = true;
+  } else {
+    // stores of alpha * the product (a store move ignores the run-time factor)
+    for (MoveDesc& m : unpackC.host) {
+      m.op = 0;
+      m.scale = alpha;
+    }
+    store_scale = alpha;
+  }
+  return true;
 }
 
 int SumPlan::execute(const double* dA, double* dC, double alpha, cudaStream_t st) {

@@ -152,6 +152,14 @@ struct ContractionPlan {
   std::vector<DirPair> dir_pairs;
   DirItem* d_dir_items = nullptr;
   DirPair* d_dir_pairs = nullptr;
+  bool dir_overwrite = false;  // C = alpha A B instead of C += (the items cover all of C)
+  // Nonzero: the unpack stores store_scale * A B into C, whatever factor
+  // execute is given (set_overwrite on a packed plan).
+  double store_scale = 0.0;
+  // Makes the plan write C = alpha A B instead of accumulating, when it writes
+  // every element of C (the direct items, or the unpack moves: one per C
+  // tile); call before build.  false: nothing changed.
+  bool set_overwrite(double alpha, int64_t c_elems);
 
   ~ContractionPlan();
   // Device bytes the plan keeps for itself, the arena bytes one execute

@@ -105,6 +105,7 @@ struct PaDirect {
   double* C;
   double alpha;
   int nitems;
+  int overwrite;
 };
 struct PaSplitSets {  // row exponents, digits, short rows
   const SplitRowSet* sets;
