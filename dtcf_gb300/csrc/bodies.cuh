@@ -951,7 +951,7 @@ __device__ __forceinline__ void cc_amp_body(const CCAmpTile* __restrict__ tiles,
     const uint32_t ej = tl.fj.d, ea = tl.fa.d, eb = tl.fb.d;
     const int64_t o_ia = tl.t1[0], o_jb = tl.t1[1], o_ib = tl.t1[2], o_ja = tl.t1[3];
     const bool h1 = o_ia >= 0 && o_jb >= 0, h2 = o_ib >= 0 && o_ja >= 0;
-    double x[kPer], p1[kPer], p2[kPer];
+    double x[kPer], p1[kPer], d[kPer];
 #pragma unroll
     for (int k = 0; k < kPer; ++k) {
       const uint32_t e = min((uint32_t)(threadIdx.x + k * kCcThreads), it.n - 1);
@@ -962,13 +962,17 @@ __device__ __forceinline__ void cc_amp_body(const CCAmpTile* __restrict__ tiles,
       x[k] = ldin<kCoh>(t2 + tl.off + f);
       p1[k] = h1 ? __dmul_rn(ldin<kCoh>(t1 + o_ia + (int64_t)ii * ea + a), ldin<kCoh>(t1 + o_jb + (int64_t)j * eb + b))
                  : 0.0;
-      p2[k] = h2 ? __dmul_rn(ldin<kCoh>(t1 + o_ib + (int64_t)ii * eb + b), ldin<kCoh>(t1 + o_ja + (int64_t)j * ea + a))
-                 : 0.0;
+      // d = t1_ia t1_jb - t1_ib t1_ja, the second product inside one fused
+      // multiply-add
+      d[k] = h2 ? __fma_rn(-ldin<kCoh>(t1 + o_ib + (int64_t)ii * eb + b), ldin<kCoh>(t1 + o_ja + (int64_t)j * ea + a),
+                           p1[k])
+                : p1[k];
     }
-    // seven FP64 instructions per element (the FP64 pipe, not HBM, bounds
-    // element-wise FP64 work on this part): the products p1, p2; tau as
-    // (t2 + p1) - p2; taut and Q with fused multiply-adds by 1/2 -- each the
-    // separately rounded product and sum, 0.5 x being exact
+    // five FP64 instructions per element (the FP64 pipe, not HBM, bounds
+    // element-wise FP64 work on this part): p1 and d above; tau = t2 + d,
+    // taut = t2 + d / 2 and Q = t2 / 2 + p1 (fused multiply-adds by 1/2,
+    // which is exact)
+    const bool hd = h1 || h2;
 #pragma unroll
     for (int k = 0; k < kPer; ++k) {
       const uint32_t e = threadIdx.x + k * kCcThreads;
@@ -977,19 +981,9 @@ __device__ __forceinline__ void cc_amp_body(const CCAmpTile* __restrict__ tiles,
       // 0 + t2 (turns -0 into +0) on the bits
       const unsigned long long xb = (unsigned long long)__double_as_longlong(x[k]);
       const double x0 = __longlong_as_double((long long)(xb == 0x8000000000000000ull ? 0ull : xb));
-      double a1 = x0, a2 = x0;
-      double q = __fma_rn(0.5, x[k], h1 ? p1[k] : 0.0);
-      if (h1) {
-        a1 = __dadd_rn(a1, p1[k]);
-        a2 = __fma_rn(0.5, p1[k], a2);
-      }
-      if (h2) {
-        a1 = __dsub_rn(a1, p2[k]);
-        a2 = __fma_rn(-0.5, p2[k], a2);
-      }
-      tau[at] = a1;
-      taut[at] = a2;
-      Q[at] = q;
+      tau[at] = hd ? __dadd_rn(x0, d[k]) : x0;
+      taut[at] = hd ? __fma_rn(0.5, d[k], x0) : x0;
+      Q[at] = __fma_rn(0.5, x[k], p1[k]);
     }
   }
 }
