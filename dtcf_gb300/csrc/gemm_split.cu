@@ -474,7 +474,8 @@ __global__ void __launch_bounds__(SplitCfg<BN>::kThreads, SplitCfg<BN>::kCtasPer
 // are padded to the k-block, so short K (a virtual block of ~30 orbitals)
 // streams half the bytes with the narrow block.
 constexpr int kThinBN = 32;
-constexpr int kThinDrainWarps = 8;  // two groups of four (one per TMEM lane quarter), alternate tiles
+constexpr int kThinBufs = 3;        // accumulator buffers (at most; S (S <= 5) levels of 32 columns each)
+constexpr int kThinDrainWarps = 4 * kThinBufs;  // one group of four (one per TMEM lane quarter) per buffer
 constexpr int kThinThreads = 64 + 32 * kThinDrainWarps;
 
 template <int TBK>
@@ -482,7 +483,7 @@ struct ThinSmem {
   static constexpr int kSlots = 10 * (BK / TBK);  // ring of (A slice, B slice) pairs, 200 KB of them
   alignas(1024) __nv_bfloat16 a[kSlots][BM * TBK];
   alignas(1024) __nv_bfloat16 b[kSlots][kThinBN * TBK];
-  uint64_t full[kSlots], empty[kSlots], accfull[2], accempty[2], done;
+  uint64_t full[kSlots], empty[kSlots], accfull[kThinBufs], accempty[kThinBufs], done;
   uint32_t tmem_base;
 };
 
@@ -494,33 +495,71 @@ struct ThinSmem {
 // ea: the row's exponent, eb8: the first 8 column exponents, both loaded
 // by the caller before it waited for the accumulator (their latency hidden
 // behind the wait); columns past 8 are read here.
+// Stores of one drained row: v[j] * 2^(its exponent), columns < ncol.
+template <int NC>
+__device__ __forceinline__ void thin_store(const double (&v)[NC], int L, int ncol, const DevProblem& pr, int row,
+                                           int ea, const int* eb8) {
+  if (row >= pr.M) return;
+  double* crow = pr.C + (int64_t)row * pr.ldc;
+  const int lshift = L <= 5 ? 8 * L : 0;  // the int64 path carries 2^(8L)
+#pragma unroll
+  for (int j = 0; j < NC; ++j) {
+    if (j < ncol) {
+      int ex = ea + (j < 8 ? eb8[j] : pr.eB[j]) - 2 * 1022 - 14 - lshift + 1023;
+      ex = ex < 1 ? 1 : (ex > 2046 ? 2046 : ex);
+      crow[j] = v[j] * __longlong_as_double((long long)ex << 52);
+    }
+  }
+}
+
 template <int NC>
 __device__ __forceinline__ void thin_drain(uint32_t tb, int L, int ncol, const DevProblem& pr, int row,
                                            uint64_t* accempty, int lane, int ea, const int* eb8) {
-  long long Y[NC];
-  double acc[NC];
+  double v[NC];
+  if (L <= 5) {
+    long long Y[NC];
 #pragma unroll
-  for (int j = 0; j < NC; ++j) {
-    Y[j] = 0;
-    acc[j] = 0.0;
-  }
-  if (NC == 8 && L <= 3) {
-    // at most four levels of 8 columns (the usual thin tile: an occupied
-    // block of about 6): every load issued, then one wait
-    uint32_t rb[4][8];
+    for (int j = 0; j < NC; ++j) Y[j] = 0;
+    if (NC == 8 && L <= 3) {
+      // at most four levels of 8 columns (the usual thin tile: an occupied
+      // block of about 6): every load issued, then one wait
+      uint32_t rb[4][8];
 #pragma unroll
-    for (int l = 0; l < 4; ++l)
-      if (l <= L) tmem_ld8(tb + (uint32_t)(l * kThinBN), rb[l]);
-    tmem_wait_ld();
+      for (int l = 0; l < 4; ++l)
+        if (l <= L) tmem_ld8(tb + (uint32_t)(l * kThinBN), rb[l]);
+      tmem_wait_ld();
 #pragma unroll
-    for (int l = 0; l < 4; ++l)
-      if (l <= L) {
+      for (int l = 0; l < 4; ++l)
+        if (l <= L) {
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
-          if (j < ncol) Y[j] = Y[j] * 256 + (long long)__float2int_rn(__uint_as_float(rb[l][j]));
+          for (int j = 0; j < 8; ++j)
+            if (j < ncol) Y[j] = Y[j] * 256 + (long long)__float2int_rn(__uint_as_float(rb[l][j]));
+        }
+    } else {
+      for (int l = 0; l <= L; ++l) {
+        uint32_t r[NC];
+        if (NC == 8) {
+          tmem_ld8(tb + (uint32_t)(l * kThinBN), r);
+        } else {
+#pragma unroll
+          for (int h = 0; h < NC / 16; ++h)
+            tmem_ld16(tb + (uint32_t)(l * kThinBN + 16 * h), *reinterpret_cast<uint32_t(*)[16]>(r + 16 * h));
+        }
+        tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < NC; ++j)
+          if (j < ncol) Y[j] = Y[j] * 256 + (long long)__float2int_rn(__uint_as_float(r[j]));
       }
+    }
+    tc_fence_before();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(accempty);
+#pragma unroll
+    for (int j = 0; j < NC; ++j) v[j] = (double)Y[j];
   } else {
-    for (int l = L <= 5 ? 0 : L; L <= 5 ? l <= L : l >= 0; l += L <= 5 ? 1 : -1) {
+#pragma unroll
+    for (int j = 0; j < NC; ++j) v[j] = 0.0;
+    for (int l = L; l >= 0; --l) {
       uint32_t r[NC];
       if (NC == 8) {
         tmem_ld8(tb + (uint32_t)(l * kThinBN), r);
@@ -530,33 +569,15 @@ __device__ __forceinline__ void thin_drain(uint32_t tb, int L, int ncol, const D
           tmem_ld16(tb + (uint32_t)(l * kThinBN + 16 * h), *reinterpret_cast<uint32_t(*)[16]>(r + 16 * h));
       }
       tmem_wait_ld();
-      if (L <= 5) {
 #pragma unroll
-        for (int j = 0; j < NC; ++j)
-          if (j < ncol) Y[j] = Y[j] * 256 + (long long)__float2int_rn(__uint_as_float(r[j]));
-      } else {
-#pragma unroll
-        for (int j = 0; j < NC; ++j)
-          if (j < ncol) acc[j] = acc[j] * 0x1.0p-8 + (double)__uint_as_float(r[j]);
-      }
+      for (int j = 0; j < NC; ++j)
+        if (j < ncol) v[j] = v[j] * 0x1.0p-8 + (double)__uint_as_float(r[j]);
     }
+    tc_fence_before();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(accempty);
   }
-  tc_fence_before();
-  __syncwarp();
-  if (lane == 0) mbar_arrive(accempty);
-  if (row < pr.M) {
-    double* crow = pr.C + (int64_t)row * pr.ldc;
-    const int lshift = L <= 5 ? 8 * L : 0;  // the int64 path carries 2^(8L)
-#pragma unroll
-    for (int j = 0; j < NC; ++j) {
-      if (j < ncol) {
-        int ex = ea + (j < 8 ? eb8[j] : pr.eB[j]) - 2 * 1022 - 14 - lshift + 1023;
-        ex = ex < 1 ? 1 : (ex > 2046 ? 2046 : ex);
-        const double v = L <= 5 ? (double)Y[j] : acc[j];
-        crow[j] = v * __longlong_as_double((long long)ex << 52);
-      }
-    }
-  }
+  thin_store<NC>(v, L, ncol, pr, row, ea, eb8);
 }
 
 template <int TBK>
@@ -578,7 +599,7 @@ __global__ void __launch_bounds__(kThinThreads, 1) split_thin_kernel(const GemmP
       mbar_init(&sm.full[i], 1);
       mbar_init(&sm.empty[i], 1);
     }
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < kThinBufs; ++b) {
       mbar_init(&sm.accfull[b], 1);
       mbar_init(&sm.accempty[b], 4);
     }
@@ -595,6 +616,8 @@ __global__ void __launch_bounds__(kThinThreads, 1) split_thin_kernel(const GemmP
   tc_fence_after();
   const uint32_t tmem = sm.tmem_base;
   const uint32_t buf_cols = (uint32_t)(S * kThinBN);
+  // accumulator buffers in the 512 columns: three for S <= 5, two above
+  const int nbuf = min(kThinBufs, (int)(kCols / buf_cols));
 
   if (warp == 0) {
     if (lane == 0) {
@@ -664,7 +687,7 @@ __global__ void __launch_bounds__(kThinThreads, 1) split_thin_kernel(const GemmP
           st = 0;
           phase ^= 1;
         }
-        if (++buf == 2) {
+        if (++buf == nbuf) {
           buf = 0;
           aphase ^= 1;
         }
@@ -673,16 +696,18 @@ __global__ void __launch_bounds__(kThinThreads, 1) split_thin_kernel(const GemmP
       mbar_wait(&sm.done, 0, P.err, 16);
     }
   } else {
-    // two drain groups of four warps: group g drains this CTA's tiles g,
-    // g + 2, g + 4, ... -- always from accumulator buffer g -- so that two
-    // tiles drain at once (a drain, with its exponent loads, TMEM reads and
-    // scattered row stores, takes longer than a tile's MMAs)
+    // nbuf drain groups of four warps: group g drains this CTA's tiles g,
+    // g + nbuf, g + 2 nbuf, ... -- always from accumulator buffer g -- so
+    // that nbuf tiles drain at once (a drain, with its exponent loads, TMEM
+    // reads and scattered row stores, takes longer than a tile's MMAs); a
+    // group without a buffer (S > 5) has no tiles
     const int group = (warp - 2) >> 2;
     const int quarter = warp & 3;
     const uint32_t lane_addr = (uint32_t)(quarter * 32) << 16;
     const int buf = group;
     uint32_t aphase = 0;
-    for (int tile = blockIdx.x + group * (int)gridDim.x; tile < P.total_tiles; tile += 2 * (int)gridDim.x) {
+    for (int tile = blockIdx.x + group * (int)gridDim.x; group < nbuf && tile < P.total_tiles;
+         tile += nbuf * (int)gridDim.x) {
       const TileInfo ti = decode_tile<kThinBN>(P, tile);
       const DevProblem& pr = P.probs[ti.p];
       // only the tile's real columns are read and combined: a drain sized
