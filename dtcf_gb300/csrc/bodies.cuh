@@ -403,13 +403,14 @@ struct DirSmem {
 // operand that carries the output's last dimension is read coalesced and the
 // other one is (mostly) a broadcast.  Every output element is the same
 // sequence of fused multiply-adds whatever kThr is.
-// overwrite: C = alpha * sum (the items cover every element of C, which
-// holds no earlier value), else C += alpha * sum.
-template <int kThr, bool kCoh>
+// kStore: C = alpha * sum (the items cover every element of C, which holds
+// no earlier value), else C += alpha * sum -- a template parameter, so that
+// the accumulating kernel's C loads are scheduled as without the choice.
+template <int kThr, bool kCoh, bool kStore>
 __device__ __forceinline__ void direct_body(const DirItem* __restrict__ items, int nitems,
                                             const DirPair* __restrict__ pairs, const double* __restrict__ A,
                                             const double* __restrict__ B, double* __restrict__ C, double alpha,
-                                            int overwrite, uint32_t bid, uint32_t nblk, DirSmem& sm) {
+                                            uint32_t bid, uint32_t nblk, DirSmem& sm) {
   constexpr int kPasses = kDirItemElems / (kThr * kDirPer);
   static_assert(kPasses * kThr * kDirPer == kDirItemElems, "item size");
   for (int i = (int)bid; i < nitems; i += (int)nblk) {
@@ -470,7 +471,8 @@ __device__ __forceinline__ void direct_body(const DirItem* __restrict__ items, i
         const uint32_t e = e0 + (uint32_t)(k * kThr);
         if (e < it.n) {
           double* c = C + it.coff + e;
-          *c = overwrite ? __dmul_rn(alpha, acc[k]) : __fma_rn(alpha, acc[k], ldrw<kCoh>(c));
+          if constexpr (kStore) *c = __dmul_rn(alpha, acc[k]);
+          else *c = __fma_rn(alpha, acc[k], ldrw<kCoh>(c));
         }
       }
     }

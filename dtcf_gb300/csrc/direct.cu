@@ -18,12 +18,13 @@ constexpr int kDirThreads = 512;
 }  // namespace
 
 // One CTA of 512 threads per work item (dev::direct_body).
+template <bool kStore>
 __global__ void __launch_bounds__(kDirThreads, 2)
     direct_contract_kernel(const DirItem* __restrict__ items, int nitems, const DirPair* __restrict__ pairs,
                            const double* __restrict__ A, const double* __restrict__ B, double* __restrict__ C,
-                           double alpha, int overwrite) {
+                           double alpha) {
   __shared__ dev::DirSmem sm;
-  dev::direct_body<kDirThreads, false>(items, nitems, pairs, A, B, C, alpha, overwrite, blockIdx.x, gridDim.x, sm);
+  dev::direct_body<kDirThreads, false, kStore>(items, nitems, pairs, A, B, C, alpha, blockIdx.x, gridDim.x, sm);
 }
 
 int run_direct(const DirItem* items, int nitems, const DirPair* pairs, const double* A, const double* B, double* C,
@@ -35,7 +36,8 @@ int run_direct(const DirItem* items, int nitems, const DirPair* pairs, const dou
     a.direct = {items, pairs, A, B, C, alpha, nitems, overwrite ? 1 : 0};
     return prog_mem(rec, PK_DIRECT, (uint32_t)grid, a, {{A, false}, {B, false}, {C, true}});
   }
-  direct_contract_kernel<<<grid, kDirThreads, 0, st>>>(items, nitems, pairs, A, B, C, alpha, overwrite ? 1 : 0);
+  if (overwrite) direct_contract_kernel<true><<<grid, kDirThreads, 0, st>>>(items, nitems, pairs, A, B, C, alpha);
+  else direct_contract_kernel<false><<<grid, kDirThreads, 0, st>>>(items, nitems, pairs, A, B, C, alpha);
   GBX_CUDA(cudaGetLastError());
   return GBX_OK;
 }

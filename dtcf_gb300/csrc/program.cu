@@ -94,8 +94,12 @@ __device__ __forceinline__ void run_record(const ProgRec& r, uint32_t vb, ProgSm
                                 vb, g, sm.fs);
       break;
     case PK_DIRECT:
-      dev::direct_body<kProgThreads, true>(a.direct.items, a.direct.nitems, a.direct.pairs, a.direct.A, a.direct.B,
-                                           a.direct.C, a.direct.alpha, a.direct.overwrite, vb, g, sm.dir);
+      if (a.direct.overwrite)
+        dev::direct_body<kProgThreads, true, true>(a.direct.items, a.direct.nitems, a.direct.pairs, a.direct.A,
+                                                   a.direct.B, a.direct.C, a.direct.alpha, vb, g, sm.dir);
+      else
+        dev::direct_body<kProgThreads, true, false>(a.direct.items, a.direct.nitems, a.direct.pairs, a.direct.A,
+                                                    a.direct.B, a.direct.C, a.direct.alpha, vb, g, sm.dir);
       break;
     case PK_ROWEXP:
       dev::row_exponent_body<true>(a.sets.sets, a.sets.nsets, a.sets.total, vb, g, sm.red8);
