@@ -36,7 +36,7 @@ constexpr int kSmallK = dev::kSmallK;
 constexpr int kSmallKElems = dev::kSmallKElems;  // output elements per CTA
 constexpr int kSmallOutDim = dev::kSmallOutDim;  // small outputs: at most 16 x 16 ...
 constexpr int kSmallOutMinK = 4096;  // ... with at least this K
-constexpr int kSmallOutChunk = 4096;  // K per work item
+constexpr int kSmallOutChunk = 2048;  // K per work item
 constexpr int kGemvDim = dev::kGemvDim;  // matrix-vector problems: one side at most this ...
 constexpr int kGemvMinK = 64;         // ... with K above this
 constexpr int kGemvItems = 152 * 4;   // work items that keep every SM busy
